@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FoilCFD solver step.
+
+Workload (the reference metric's configuration): the 640x192x192 = 23.6 M
+cell wall-modelled airfoil tunnel -- NACA 0012 at 6 deg, 256 cells/chord,
+u_lat 0.08, Re 2.4e6 (tau clamped at 0.5005), TRT + Smagorinsky Cs 0.1, iMEM
+wall model on every stair-step face, one 2:1 patch around the section
++- 0.1 chord, uniform-flow start (ramps off). A "step" is one coarse step
+(coarse collide, two fine sub-steps of fill + collide, restriction);
+stepN batches of 50 steps carry one force reduction and one wall-model
+update each, as the reference cadence does. GLUPS counts coarse + 2 x fine
+updates per step (the reference's perfStats accounting); the coarse-only
+figure is reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GLUPS, 23.6M-cell wall-modeled tunnel: FP16-store vs FP32, % of HBM peak"
+UNIT = "GLUPS"
+BYTES_PER_LUP = {"fp32": 153.0, "fp16": 77.0}  # 19 loads + 19 stores + 1 kind byte
+BATCH = 50
+# DRAM bytes per cell update of the collide kernel from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over cells of the launch) on
+# the small workload; profiles/collide_fp32.md and collide_fp16.md record it.
+NCU_DRAM_BYTES_PER_LUP = {"fp32": None, "fp16": None}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(small: bool):
+    from foil_cfd_gb300 import tunnels
+    if small:
+        return tunnels.airfoil_tunnel(nx=320, ny=96, nz=96, chord=128)
+    return tunnels.airfoil_tunnel()
+
+
+def make_solver(t, storage: str):
+    import foil_cfd_gb300 as fc
+    s = fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat)
+    sol = fc.LBMSolver()
+    sol.init(t.dims, s, t.flags, storage=storage, les_cs=0.1)
+    sol.set_wall_model_enabled(True)
+    sol.set_startup_ramp_enabled(False)
+    sol.reset()
+    if t.box is not None:
+        sol.init_refinement(t.box, t.factor, t.fine_flags)
+    return sol, s
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons (200 ms)."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = Path(os.environ.get("GRAFT_CLOCKS_FILE", "/tmp/foilcfd_clocks.csv"))
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", dev, f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def timed_steps(sol, steps):
+    """Run `steps` coarse steps in batches; returns device ms (CUDA events)."""
+    sol.synchronize()
+    sol.timer_start()
+    left = steps
+    while left > 0:
+        n = min(BATCH, left)
+        rc = sol.step_n(n)
+        if rc:
+            raise RuntimeError(f"step_n failed ({rc})")
+        left -= n
+    return sol.timer_stop()
+
+
+def measure(t, storage, steps, warmup, clocks=None):
+    sol, scaling = make_solver(t, storage)
+    assert sol.step_n(warmup) == 0
+    sol.synchronize()
+    l0 = sol.kernel_launches()
+    if clocks:
+        clocks.start()
+    ms = timed_steps(sol, steps)
+    clk = clocks.stop() if clocks else None
+    launches = sol.kernel_launches() - l0
+    # Dominant kernel: every collide launch bracketed by events, on the
+    # solver's stream, over a separate run of the same steps.
+    sol.enable_collide_timing(True)
+    timed_steps(sol, min(steps, 40))
+    col_ms, col_n, col_cells = sol.collide_time_ms()
+    sol.enable_collide_timing(False)
+    upd = t.updates_per_step()
+    res = dict(ms=ms, glups=upd * steps / (ms * 1e-3) / 1e9,
+               coarse_glups=float(np.prod(t.dims)) * steps / (ms * 1e-3) / 1e9, launches=launches, clocks=clk,
+               collide=dict(ms=col_ms, launches=col_n, cells=col_cells),
+               nan=sol.nan_detected(), force=sol.force_raw().tolist(), solver=sol, scaling=scaling)
+    return res
+
+
+def roofline(storage, col):
+    peak, kind = peaks()
+    avg_ms = col["ms"] / max(col["launches"], 1)
+    cells_per_launch = col["cells"] / max(col["launches"], 1)
+    alg = BYTES_PER_LUP[storage] * cells_per_launch
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    tb = NCU_DRAM_BYTES_PER_LUP[storage]
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": kind,
+            "traffic": None if tb is None else round(tb * cells_per_launch),
+            "kernel": f"collide_kernel ({storage}, coarse + fine launches)",
+            "bytes_per_lup": BYTES_PER_LUP[storage], "avg_launch_ms": round(avg_ms, 4),
+            "cells_per_launch": round(cells_per_launch)}
+
+
+def e2e(t, res, steps):
+    """Same metric through the C ABI with host buffers: import the state
+    from pinned host memory, run the steps, read rho/u/v/w and the force
+    back to pinned host memory -- all inside the timed region."""
+    from foil_cfd_gb300.solver import PinnedArray
+    sol = res["solver"]
+    n = int(np.prod(t.dims))
+    fcoarse = PinnedArray(19 * n)
+    fcoarse.array[:] = sol.export_f32()
+    ffine = None
+    if t.box is not None:
+        ffine = PinnedArray(19 * int(np.prod(t.fine_dims)))
+        ffine.array[:] = sol.export_fine_f32()
+    macro = [PinnedArray(n) for _ in range(4)]
+    sol.synchronize()
+    t0 = time.perf_counter()
+    sol.import_f32(fcoarse.array)
+    if ffine is not None:
+        sol.import_fine_f32(ffine.array)
+    left = steps
+    while left > 0:
+        k = min(BATCH, left)
+        assert sol.step_n(k) == 0
+        left -= k
+    assert sol.download_macro_into(*[m.array for m in macro]) == 0
+    force = sol.force_raw()
+    dt = time.perf_counter() - t0
+    h2d = fcoarse.array.nbytes + (ffine.array.nbytes if ffine is not None else 0)
+    d2h = sum(m.array.nbytes for m in macro) + force.nbytes
+    for a in [fcoarse, ffine, *macro]:
+        if a is not None:
+            a.close()
+    return {"value": round(t.updates_per_step() * steps / dt / 1e9, 3), "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps)}
+
+
+def cpu_host():
+    try:
+        model = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in model.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_reference(t, steps):
+    """The oracle port (C++ restatement, OpenMP, all host threads) on the
+    same tunnel: `steps` coarse steps after one warm-up batch."""
+    from oracle import oracle
+    import foil_cfd_gb300 as fc
+    oracle.build()
+    s = fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat)
+    f0 = oracle.init_equilibrium(t.dims, t.flags, np.float32(t.u_lat))
+    ot = oracle.OracleTunnel(t.dims, t.flags, f0, np.float32(s.tau), np.float32(t.u_lat), cs=0.1)
+    if t.box is not None:
+        ot.refine((t.box.x0, t.box.y0, t.box.x1, t.box.y1), t.factor, t.fine_flags)
+        ot.wall(1, fc.build_wall_list(t.fine_dims, t.fine_flags, sample_cells=3))
+    ot.wall(0, fc.build_wall_list(t.dims, t.flags, sample_cells=2))
+    ot.step_n(1)
+    t0 = time.perf_counter()
+    ot.step_n(steps)
+    dt = time.perf_counter() - t0
+    ot.close()
+    return {"value": round(t.updates_per_step() * steps / dt / 1e9, 5), "unit": UNIT,
+            "cores": oracle.threads(), "kind": "port",
+            "sample": f"{steps} coarse steps (+1 warm-up) of the full tunnel incl. patch, wall model and "
+                      f"force, C++ oracle with OpenMP on {cpu_host()}",
+            "seconds": round(dt, 2)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return dist, rank, ws
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="320x96x96 tunnel (profiling captures)")
+    ap.add_argument("--no-fp16", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    warmup = max(args.warmup, 3)
+    dist, rank, ws = dist_setup()
+    t = workload(args.small)
+
+    cfg = {"workload": f"airfoil tunnel {t.name}: NACA 0012 at 6 deg, 256 cells/chord, u_lat 0.08, "
+                       "Re 2.4e6 (tau 0.5005), TRT + Smagorinsky Cs 0.1, iMEM wall model, one 2:1 patch "
+                       "+-0.1 chord, uniform-flow start",
+           "dims": list(t.dims), "fine_dims": list(t.fine_dims) if t.box else None,
+           "updates_per_step": t.updates_per_step(), "batch": BATCH,
+           "counting": "coarse + 2 x fine lattice updates per coarse step",
+           "l2": "populations (>10 GB) exceed the 129 MB L2; no flush needed",
+           "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, min(args.steps, 3))
+        ref = cpu_reference(t, steps)
+        line = {"impl": "reference", "metric": METRIC, "value": ref["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": steps, "warmup": 1, "ms_per_step": round(ref["seconds"] * 1e3 / steps, 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": cfg,
+                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": ref["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    clocks = Clocks() if rank == 0 else None
+    r32 = measure(t, "fp32", args.steps, warmup, clocks)
+    ms = r32["ms"]
+    if dist is not None:
+        import torch
+        tt = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = ws * t.updates_per_step() * args.steps / (ms * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "coarse_only_glups": round(r32["coarse_glups"] * ws, 3),
+            "roofline": roofline("fp32", r32["collide"]),
+            "gpu_launches": int(r32["launches"]), "clocks": r32["clocks"],
+            "force_lattice": r32["force"], "nan": bool(r32["nan"])}
+    line["e2e"] = e2e(t, r32, args.steps)
+    r32["solver"] = None
+    del r32
+    if not args.no_fp16:
+        r16 = measure(t, "fp16", args.steps, warmup, None)
+        line["fp16"] = {"value": round(ws * r16["glups"], 3), "ratio_vs_fp32": round(r16["glups"] / (value / ws), 3),
+                        "ms_per_step": round(r16["ms"] / args.steps, 4),
+                        "roofline": roofline("fp16", r16["collide"]), "gpu_launches": int(r16["launches"]),
+                        "force_lattice": r16["force"]}
+        r16["solver"] = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_reference(t, 2).items() if k != "seconds"}
+    if dist is not None:
+        dist.barrier()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,93 @@
+"""Build recipe of the solver-step shared library (CUDA for sm_103a + host C++).
+
+Compiles every translation unit under ``csrc/`` in parallel and links
+``_build/libfoilcfd_gb300.so`` in the package directory. A content hash of
+the sources and flags is stored next to the library so an unchanged tree is
+not rebuilt. No cmake, no torch extension machinery: plain nvcc and g++.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = BUILD / "libfoilcfd_gb300.so"
+INCLUDE = PKG.parent / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "--expt-relaxed-constexpr"] + ARCH
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+
+
+def _cuda_home() -> Path:
+    env = os.environ.get("CUDA_HOME") or os.environ.get("CUDA_PATH")
+    if env:
+        return Path(env)
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return Path(nvcc).resolve().parent.parent
+    return Path("/usr/local/cuda")
+
+
+def _sources():
+    cu = sorted(CSRC.glob("*.cu"))
+    cpp = sorted(CSRC.glob("*.cpp"))
+    hdr = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+    return cu, cpp, hdr
+
+
+def _digest(files) -> str:
+    h = hashlib.sha256()
+    h.update(" ".join(NVCC_FLAGS + CXX_FLAGS).encode())
+    for f in files:
+        h.update(f.name.encode())
+        h.update(f.read_bytes())
+    return h.hexdigest()
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed: " + " ".join(map(str, cmd)) + "\n" + r.stdout + r.stderr)
+    return r
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the library if its sources changed; return the .so path."""
+    cu, cpp, hdr = _sources()
+    digest = _digest(cu + cpp + hdr)
+    stamp = BUILD / "digest.txt"
+    if not force and LIB.exists() and stamp.exists() and stamp.read_text() == digest:
+        return LIB
+    BUILD.mkdir(parents=True, exist_ok=True)
+    cuda = _cuda_home()
+    nvcc = str(cuda / "bin" / "nvcc")
+    inc = ["-I", str(CSRC), "-I", str(INCLUDE), "-I", str(cuda / "include")]
+    jobs = []
+    for src in cu:
+        obj = BUILD / (src.stem + ".cu.o")
+        jobs.append([nvcc, *NVCC_FLAGS, *inc, "-c", str(src), "-o", str(obj)])
+    for src in cpp:
+        obj = BUILD / (src.stem + ".cpp.o")
+        jobs.append(["g++", *CXX_FLAGS, *inc, "-c", str(src), "-o", str(obj)])
+    with ThreadPoolExecutor(max_workers=max(2, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for r in ex.map(_run, jobs):
+            if verbose and (r.stdout or r.stderr):
+                print(r.stdout + r.stderr)
+    objs = [str(BUILD / (s.stem + ".cu.o")) for s in cu] + [str(BUILD / (s.stem + ".cpp.o")) for s in cpp]
+    tmp = BUILD / (LIB.name + ".tmp")
+    _run([nvcc, "-shared", *ARCH, "-Xcompiler", "-fPIC", "-o", str(tmp), *objs, "-lpthread"])
+    os.replace(tmp, LIB)
+    stamp.write_text(digest)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

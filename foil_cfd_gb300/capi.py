@@ -1,0 +1,148 @@
+"""ctypes binding of include/foilcfd_step.h (the solver step's C ABI).
+
+Loading fails loudly when the compiled library is missing: there is no CPU
+fallback for the solver step. Build it with ``foil_cfd_gb300.build_lib``
+(or ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libfoilcfd_gb300.so"
+
+
+class Dims(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)]
+
+
+class Scaling(C.Structure):
+    _fields_ = [("chord_m", C.c_float), ("airspeed_ms", C.c_float), ("nu_m2s", C.c_float),
+                ("chord_cells", C.c_int), ("u_lat", C.c_float), ("dx", C.c_float), ("dt", C.c_float),
+                ("nu_lat_target", C.c_float), ("nu_lat", C.c_float), ("tau", C.c_float),
+                ("tau_clamped", C.c_int), ("re_target", C.c_float), ("re_effective", C.c_float)]
+
+
+class Options(C.Structure):
+    _fields_ = [("storage", C.c_int), ("les_cs", C.c_float), ("magic_lambda", C.c_float),
+                ("use_graphs", C.c_int)]
+
+
+class PatchBox(C.Structure):
+    _fields_ = [("x0", C.c_int), ("y0", C.c_int), ("x1", C.c_int), ("y1", C.c_int)]
+
+
+class ForceReadout(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("cl", "cd", "lift_to_drag")] + [("valid", C.c_int)] + [
+        (n, C.c_float) for n in ("flow_throughs", "cl_avg", "cl_min", "cl_max", "cl_median", "cd_avg", "cd_min",
+                                 "cd_max", "cd_median", "ld_avg", "ld_min", "ld_max", "ld_median")]
+
+
+class WMReadout(C.Structure):
+    _fields_ = [("enabled", C.c_int), ("from_fine", C.c_int), ("cells", C.c_int), ("mean_yplus", C.c_float),
+                ("max_yplus", C.c_float), ("clamped_frac", C.c_float), ("excluded_vg", C.c_int),
+                ("degenerate", C.c_int)]
+
+
+class Perf(C.Structure):
+    _fields_ = [("last_step_ms", C.c_double), ("mlups", C.c_double), ("updates_per_step", C.c_double)]
+
+
+class RefineInfo(C.Structure):
+    _fields_ = [("active", C.c_int), ("factor", C.c_int), ("box", PatchBox), ("fine_dims", Dims),
+                ("forces_from_fine", C.c_int), ("vram_bytes", C.c_double)]
+
+
+P = C.c_void_p
+_SIGS = {
+    "fcfd_compute_scaling": (Scaling, [C.c_float, C.c_float, C.c_float, C.c_int, C.c_float]),
+    "fcfd_refined_scaling": (Scaling, [C.POINTER(Scaling), C.c_int]),
+    "fcfd_ramped_tau": (C.c_float, [C.POINTER(Scaling), C.c_longlong, C.c_int]),
+    "fcfd_ramped_u": (C.c_float, [C.POINTER(Scaling), C.c_longlong, C.c_int]),
+    "fcfd_force_to_coefficient": (C.c_float, [C.POINTER(Scaling), C.c_float, C.c_int]),
+    "fcfd_create": (P, []),
+    "fcfd_destroy": (None, [P]),
+    "fcfd_init": (C.c_int, [P, C.POINTER(Dims), C.POINTER(Scaling), P, C.c_size_t, P, C.POINTER(Options),
+                            C.c_char_p, C.c_size_t]),
+    "fcfd_reset": (None, [P]),
+    "fcfd_set_flags": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_set_startup_ramp": (None, [P, C.c_int]),
+    "fcfd_set_force_ema_window": (None, [P, C.c_float]),
+    "fcfd_step_n": (C.c_int, [P, C.c_int]),
+    "fcfd_synchronize": (C.c_int, [P]),
+    "fcfd_step_count": (C.c_longlong, [P]),
+    "fcfd_current_tau": (C.c_float, [P]),
+    "fcfd_flow_throughs": (C.c_float, [P]),
+    "fcfd_forces": (C.c_int, [P, C.POINTER(ForceReadout)]),
+    "fcfd_force_raw": (C.c_int, [P, P]),
+    "fcfd_force_now": (C.c_int, [P, P]),
+    "fcfd_macro": (C.c_int, [P, P, P, P, P]),
+    "fcfd_download_macro": (C.c_int, [P, P, P, P, P]),
+    "fcfd_active_f": (P, [P]),
+    "fcfd_f_bytes": (C.c_size_t, [P]),
+    "fcfd_notify_restored": (None, [P, C.c_int]),
+    "fcfd_import_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_export_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_restore_from_macro": (C.c_int, [P, P, P, P, P]),
+    "fcfd_perf_stats": (C.c_int, [P, C.POINTER(Perf)]),
+    "fcfd_nan_detected": (C.c_int, [P]),
+    "fcfd_nan_kind": (C.c_int, [P]),
+    "fcfd_set_wall_model": (C.c_int, [P, C.c_int]),
+    "fcfd_set_surface_reference": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_set_refined_surface_reference": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_wall_model_readout": (C.c_int, [P, C.POINTER(WMReadout)]),
+    "fcfd_wall_count": (C.c_int, [P, C.c_int]),
+    "fcfd_export_wall_state": (C.c_int, [P, C.c_int, P, C.c_size_t, P, C.c_size_t]),
+    "fcfd_import_wall_state": (C.c_int, [P, C.c_int, P, C.c_size_t, P, C.c_size_t]),
+    "fcfd_wall_update_now": (C.c_int, [P, C.c_int, C.c_float, C.c_float]),
+    "fcfd_init_refinement": (C.c_int, [P, C.POINTER(PatchBox), C.c_int, P, C.c_size_t, C.c_char_p, C.c_size_t]),
+    "fcfd_shutdown_refinement": (None, [P]),
+    "fcfd_set_refined_flags": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_refinement_info": (C.c_int, [P, C.POINTER(RefineInfo)]),
+    "fcfd_import_fine_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_export_fine_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_build_wall_list": (C.c_longlong, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P]),
+    "fcfd_boundary_flags": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
+    "fcfd_naca4": (C.c_int, [C.c_char_p, C.c_int, P, C.c_int]),
+    "fcfd_voxelize_airfoil": (C.c_int, [C.POINTER(Dims), P, C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, P,
+                                        C.c_size_t]),
+    "fcfd_stamp_interface_shell": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
+    "fcfd_derive_patch_box": (PatchBox, [C.POINTER(Dims), P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "fcfd_kernel_launches": (C.c_longlong, [P]),
+    "fcfd_enable_collide_timing": (C.c_int, [P, C.c_int]),
+    "fcfd_collide_time_ms": (C.c_int, [P, P, P, P]),
+    "fcfd_timer_start": (C.c_int, [P]),
+    "fcfd_timer_stop": (C.c_int, [P, P]),
+    "fcfd_host_alloc": (P, [C.c_size_t]),
+    "fcfd_host_free": (None, [P]),
+    "fcfd_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def declared_symbols():
+    """Every function name include/foilcfd_step.h declares."""
+    return list(_SIGS)
+
+
+def load() -> C.CDLL:
+    """Load the solver-step library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"solver-step library not built ({LIB_PATH}); run foil_cfd_gb300.build_lib.build() "
+                "- there is no CPU fallback for the CUDA solver step")
+        lib = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def ptr(a):
+    """ctypes void* of a numpy array (None passes NULL)."""
+    return None if a is None else a.ctypes.data_as(C.c_void_p)

@@ -1,0 +1,123 @@
+// Host-callable launch functions of the GB300 solver-step kernels. Plain C++
+// (no CUDA-only syntax), so the orchestrator compiles as ordinary host code.
+// Every launcher returns the cudaGetLastError() of its launch, the contract of
+// the reference launch wrappers (src/sim/lbm_core.cuh:249-254).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime_api.h>
+
+#ifdef __CUDACC__
+#define FCFD_HD __host__ __device__
+#else
+#define FCFD_HD
+#endif
+
+namespace fcfd {
+
+/// Geometry of one lattice level: unpadded SoA, cell = x + nx*(y + ny*z).
+struct LevelDims {
+    int nx = 0, ny = 0, nz = 0;
+    FCFD_HD long long cells() const { return static_cast<long long>(nx) * ny * nz; }
+};
+
+/// Per-step collision parameters (reference StepParams, lbm_core.cuh:233-241).
+struct CollideParams {
+    float tau = 0.6f;
+    float magicLambda = 3.0f / 16.0f;
+    float smagPrefactor = 0.0f; ///< 18*sqrt(2)*Cs^2; 0 disables LES.
+    float uInlet = 0.08f;
+    int writeMacro = 0;
+};
+
+/// Half-bit slip field of a level (WallSlipView, lbm_core.cuh:201-208).
+struct SlipField {
+    const std::uint16_t* uwx = nullptr;
+    const std::uint16_t* uwy = nullptr;
+    const std::uint16_t* uwz = nullptr;
+    bool active() const { return uwx && uwy && uwz; }
+};
+
+enum class Storage : int { F32 = 0, F16 = 1 };
+
+// ---- step kernels (step_kernels.cu) ---------------------------------------
+cudaError_t launch_classify(const std::uint8_t* flags, std::uint8_t* kind,
+                            LevelDims d, cudaStream_t st);
+cudaError_t launch_collide(Storage s, const void* src, void* dst,
+                           const std::uint8_t* kind, LevelDims d,
+                           const CollideParams& p, float* rho, float* u,
+                           float* v, float* w, SlipField slip, cudaStream_t st);
+cudaError_t launch_init_equilibrium(Storage s, void* f, const std::uint8_t* kind,
+                                    LevelDims d, float uInlet, cudaStream_t st);
+cudaError_t launch_speck(Storage s, void* f, const std::uint8_t* kind, LevelDims d,
+                         float amplitude, unsigned seed, cudaStream_t st);
+cudaError_t launch_init_from_macro(Storage s, void* f, const std::uint8_t* kind,
+                                   LevelDims d, const float* rho, const float* u,
+                                   const float* v, const float* w, cudaStream_t st);
+cudaError_t launch_watchdog(Storage s, const void* f, LevelDims d, int* flag,
+                            long long offset, int flagBase, cudaStream_t st);
+cudaError_t launch_f32_to_store(Storage s, const float* in, void* out,
+                                long long cells, cudaStream_t st);
+cudaError_t launch_store_to_f32(Storage s, const void* in, float* out,
+                                long long cells, cudaStream_t st);
+cudaError_t launch_fill(float* dst, long long n, float v, cudaStream_t st);
+
+// ---- force reduction (force_kernels.cu) ------------------------------------
+/// Momentum exchange over a compact wall-link list: entry i is fluid cell
+/// cells[i] with bit q of masks[i] set when the neighbour at +c_q is solid.
+/// Block partials go to `partials` (3 doubles per block, blocks =
+/// force_blocks(count)); a second single-block pass sums them in a fixed
+/// order into out[3]. Deterministic, FP64 from the per-link terms up.
+int force_blocks(int count);
+cudaError_t launch_force(Storage s, const void* f, long long cells,
+                         const std::uint32_t* linkCells,
+                         const std::uint32_t* linkMasks, int count,
+                         SlipField slip, double* partials, double* out,
+                         cudaStream_t st);
+
+// ---- wall model (wall_kernels.cu) ------------------------------------------
+struct WallListDev {
+    const std::uint32_t* cellIdx = nullptr;
+    const std::uint32_t* sampleIdx = nullptr;
+    const float* nX = nullptr;
+    const float* nY = nullptr;
+    const float* nZ = nullptr;
+    const float* ys = nullptr;
+    const std::uint32_t* linkMask = nullptr;
+    float* uTau = nullptr;
+    int count = 0;
+};
+struct WallStatsDev {
+    float sumYplus;
+    int maxYplusBits;
+    int activeCells;
+    int clampedCells;
+};
+cudaError_t launch_wall_update(Storage s, const void* f, long long cells,
+                               WallListDev list, std::uint16_t* uwx,
+                               std::uint16_t* uwy, std::uint16_t* uwz,
+                               float nuLat, float utCutoff, float emaAlpha,
+                               WallStatsDev* stats, cudaStream_t st);
+
+// ---- refinement (refine_kernels.cu) ----------------------------------------
+struct RefineGeom {
+    LevelDims coarse, fine;
+    int boxX0 = 0, boxY0 = 0, boxX1 = 0, boxY1 = 0;
+    int factor = 2;
+};
+cudaError_t launch_fill_c2f(Storage s, const void* cT0, const void* cT1,
+                            const std::uint8_t* coarseKind, void* fineF,
+                            const std::uint32_t* targets, int count,
+                            const RefineGeom& g, float timeWeight,
+                            float neqScale, cudaStream_t st);
+/// Fine-to-coarse restriction. `scratch` holds 24 floats per coarse cell of
+/// the restricted sub-box (child-averaged fneq[19], rho, ux, uy, uz, valid).
+long long restrict_scratch_floats(const RefineGeom& g);
+cudaError_t launch_restrict_f2c(Storage s, const void* fineF,
+                                const std::uint8_t* fineKind, void* coarseF,
+                                const std::uint8_t* coarseKind,
+                                const RefineGeom& g, float neqScaleInv,
+                                float* scratch, float* rho, float* u, float* v,
+                                float* w, cudaStream_t st);
+
+} // namespace fcfd

@@ -1,0 +1,1244 @@
+// Host orchestrator of the GB300 solver step and the C ABI of
+// include/foilcfd_step.h. It keeps the reference solver's contract
+// (src/sim/lbm_solver.cpp): cold start at rest with the spanwise speck, the
+// startup viscosity and inlet ramps, stepN's order of work (collide, then m
+// fine sub-steps of fill + collide, then restriction, per coarse step; one
+// force reduction and one wall-model update per batch), the force EMA with
+// its flow-through gate and trailing statistics, and the NaN watchdog every
+// 200 steps. Buffers are unpadded (periodic wrap lives in the kernels), so
+// there is no ghost-plane refresh anywhere in the loop.
+#include "../../include/foilcfd_step.h"
+#include "host_geom.h"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace fcfd {
+namespace {
+
+constexpr int kWatchdogPeriod = 200;
+constexpr float kSpeckAmplitudeFrac = 1e-3f;
+constexpr unsigned kSpeckSeed = 0x5eedu;
+constexpr float kForceGateFT = 2.0f;
+constexpr float kWarmGateFT = 0.5f;
+constexpr long long kCompactSettleSteps = 1000;
+constexpr float kDefaultCs = 0.1733f;
+constexpr float kDefaultLambda = 3.0f / 16.0f;
+constexpr float kMinTau = 0.5005f;
+constexpr float kMaxULat = 0.12f;
+constexpr float kWallEma = 0.25f;
+constexpr int kRestrictBandHost = 2;
+
+void set_err(char* err, size_t len, const std::string& m) {
+    if (!err || len == 0) return;
+    std::snprintf(err, len, "%s", m.c_str());
+}
+
+template <class T>
+cudaError_t dalloc(T** p, size_t bytes) {
+    return cudaMalloc(reinterpret_cast<void**>(p), bytes == 0 ? 1 : bytes);
+}
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+struct WMLevel {
+    bool active = false;
+    int count = 0;
+    std::uint32_t *dCell = nullptr, *dSample = nullptr, *dMask = nullptr;
+    float *dNx = nullptr, *dNy = nullptr, *dNz = nullptr, *dYs = nullptr, *dUTau = nullptr;
+    std::uint16_t *dUwx = nullptr, *dUwy = nullptr, *dUwz = nullptr;
+    WallStatsDev* dStats = nullptr;
+    WallListStats build{};
+    SlipField slip() const { return active ? SlipField{dUwx, dUwy, dUwz} : SlipField{}; }
+    WallListDev list() const {
+        WallListDev l;
+        l.cellIdx = dCell; l.sampleIdx = dSample; l.nX = dNx; l.nY = dNy; l.nZ = dNz;
+        l.ys = dYs; l.linkMask = dMask; l.uTau = dUTau; l.count = count;
+        return l;
+    }
+    void free() {
+        dfree(dCell); dfree(dSample); dfree(dMask); dfree(dNx); dfree(dNy); dfree(dNz);
+        dfree(dYs); dfree(dUTau); dfree(dUwx); dfree(dUwy); dfree(dUwz); dfree(dStats);
+        *this = WMLevel{};
+    }
+};
+
+struct Level {
+    LevelDims d;
+    long long n = 0;
+    void* f[2] = {nullptr, nullptr};
+    std::uint8_t* flags = nullptr;
+    std::uint8_t* kind = nullptr;
+    int src = 0;
+    std::vector<std::uint8_t> hostFlags, surfaceRef;
+    std::uint32_t *dLinkCells = nullptr, *dLinkMasks = nullptr;
+    int linkCount = 0;
+    double* dPartials = nullptr;
+    WMLevel wm;
+
+    void free_all() {
+        dfree(f[0]); dfree(f[1]); dfree(flags); dfree(kind);
+        dfree(dLinkCells); dfree(dLinkMasks); dfree(dPartials);
+        wm.free();
+        hostFlags.clear(); surfaceRef.clear();
+        linkCount = 0; src = 0; n = 0; d = LevelDims{};
+    }
+};
+
+struct ForceSample {
+    long long step;
+    float fx, fy;
+};
+
+} // namespace
+} // namespace fcfd
+
+using namespace fcfd;
+
+struct fcfd_solver {
+    // ---- configuration ----
+    LevelDims dims;
+    fcfd_scaling scaling{};
+    cudaStream_t stream = nullptr;
+    Storage storage = Storage::F32;
+    float lesCs = kDefaultCs;
+    float lambda = kDefaultLambda;
+    bool initialized = false;
+
+    // ---- levels ----
+    Level coarse;
+    Level fine;
+    bool fineActive = false;
+    int factor = 2;
+    fcfd_patch_box box{};
+    fcfd_scaling fineScaling{};
+    std::uint32_t* dShell = nullptr;
+    int shellCount = 0;
+    std::uint32_t* dSeed = nullptr;
+    int seedCount = 0;
+    float* dScratch = nullptr;
+    bool forcesFromFine = false;
+
+    // ---- macroscopic fields + readbacks ----
+    float *rho = nullptr, *u = nullptr, *v = nullptr, *w = nullptr;
+    double* dForce = nullptr;
+    double* hForce = nullptr;
+    int* dNan = nullptr;
+    int* hNan = nullptr;
+    cudaEvent_t evT0 = nullptr, evT1 = nullptr, evForce = nullptr, evNan = nullptr;
+
+    // ---- state ----
+    long long steps = 0;
+    bool rampActive = true, rampEnabled = true;
+    long long rampStart = 0;
+    long long gateOpenAt = 0;
+    float emaWindowFT = 1.0f;
+    float emaFx = 0.f, emaFy = 0.f;
+    bool emaSeeded = false;
+    bool forcePending = false;
+    long long stepsAtForceLaunch = 0, stepsAtLastFold = 0;
+    double lastForce[3] = {0, 0, 0};
+    static constexpr int kRing = 256;
+    ForceSample ring[kRing]{};
+    int ringHead = 0, ringCount = 0;
+    bool timingPending = false;
+    int timingN = 0;
+    double emaStepMs = 0.0, lastStepMs = 0.0;
+    long long sinceWatchdog = 0;
+    bool nanPending = false, nanLatched = false;
+    int nanKind = 0;
+    bool wmEnabled = false;
+    bool zSlipWalls = false;
+
+    // ---- diagnostics ----
+    long long launches = 0;
+    bool collideTiming = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> colEv;
+    std::vector<double> colCells;
+    size_t colEvUsed = 0;
+    cudaEvent_t tmr0 = nullptr, tmr1 = nullptr;
+
+    // ------------------------------------------------------------------
+    float flowThroughSteps() const {
+        return static_cast<float>(dims.nx) / std::max(scaling.u_lat, 1e-6f);
+    }
+    float effTau() const {
+        return (rampActive && rampEnabled) ? fcfd_ramped_tau(&scaling, steps - rampStart, dims.nx)
+                                           : scaling.tau;
+    }
+    float effU() const {
+        return (rampActive && rampEnabled) ? fcfd_ramped_u(&scaling, steps - rampStart, dims.nx)
+                                           : scaling.u_lat;
+    }
+    float smagPre() const {
+        return lesCs > 0.0f ? 18.0f * 1.41421356f * lesCs * lesCs : 0.0f;
+    }
+    static float fineTau(float tc, int m) { return static_cast<float>(m) * (tc - 0.5f) + 0.5f; }
+
+    static bool eventDone(cudaEvent_t e) {
+        const cudaError_t st = cudaEventQuery(e);
+        if (st == cudaErrorNotReady) (void)cudaGetLastError();
+        return st == cudaSuccess;
+    }
+
+    void pollAsync() {
+        if (timingPending && eventDone(evT1)) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, evT0, evT1) == cudaSuccess && timingN > 0) {
+                lastStepMs = static_cast<double>(ms) / timingN;
+                emaStepMs = emaStepMs > 0.0 ? emaStepMs + 0.25 * (lastStepMs - emaStepMs) : lastStepMs;
+            }
+            timingPending = false;
+        }
+        if (forcePending && eventDone(evForce)) {
+            for (int i = 0; i < 3; ++i) lastForce[i] = hForce[i];
+            const float fx = static_cast<float>(hForce[0]), fy = static_cast<float>(hForce[1]);
+            const float window = std::max(1.0f, emaWindowFT * flowThroughSteps());
+            const float dS = static_cast<float>(stepsAtForceLaunch - stepsAtLastFold);
+            const float alpha = 1.0f - std::exp(-dS / window);
+            if (!emaSeeded) { emaFx = fx; emaFy = fy; emaSeeded = true; }
+            else { emaFx += alpha * (fx - emaFx); emaFy += alpha * (fy - emaFy); }
+            ring[ringHead] = {stepsAtForceLaunch, fx, fy};
+            ringHead = (ringHead + 1) % kRing;
+            if (ringCount < kRing) ++ringCount;
+            stepsAtLastFold = stepsAtForceLaunch;
+            forcePending = false;
+        }
+        if (nanPending && eventDone(evNan)) {
+            if (*hNan != 0) { nanLatched = true; nanKind = *hNan; }
+            nanPending = false;
+        }
+    }
+
+    // ---- level setup ----
+    cudaError_t allocLevel(Level& L, LevelDims d) {
+        L.d = d;
+        L.n = d.cells();
+        const size_t fb = static_cast<size_t>(L.n) * 19 * (storage == Storage::F32 ? 4 : 2);
+        for (void*& p : L.f)
+            if (auto e = cudaMalloc(&p, fb); e != cudaSuccess) return e;
+        if (auto e = dalloc(&L.flags, static_cast<size_t>(L.n)); e != cudaSuccess) return e;
+        if (auto e = dalloc(&L.kind, static_cast<size_t>(L.n)); e != cudaSuccess) return e;
+        return cudaSuccess;
+    }
+
+    cudaError_t uploadLevelFlags(Level& L, const std::uint8_t* flags) {
+        L.hostFlags.assign(flags, flags + L.n);
+        if (auto e = cudaMemcpyAsync(L.flags, flags, static_cast<size_t>(L.n), cudaMemcpyHostToDevice, stream);
+            e != cudaSuccess)
+            return e;
+        ++launches;
+        if (auto e = launch_classify(L.flags, L.kind, L.d, stream); e != cudaSuccess) return e;
+        // Compact force-link list of this level.
+        std::vector<std::uint32_t> cells, masks;
+        build_force_links(L.d, flags, cells, masks);
+        dfree(L.dLinkCells); dfree(L.dLinkMasks); dfree(L.dPartials);
+        L.linkCount = static_cast<int>(cells.size());
+        if (auto e = dalloc(&L.dLinkCells, cells.size() * 4); e != cudaSuccess) return e;
+        if (auto e = dalloc(&L.dLinkMasks, masks.size() * 4); e != cudaSuccess) return e;
+        if (auto e = dalloc(&L.dPartials, static_cast<size_t>(force_blocks(L.linkCount)) * 3 * sizeof(double));
+            e != cudaSuccess)
+            return e;
+        if (!cells.empty()) {
+            cudaMemcpyAsync(L.dLinkCells, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice, stream);
+            cudaMemcpyAsync(L.dLinkMasks, masks.data(), masks.size() * 4, cudaMemcpyHostToDevice, stream);
+        }
+        return cudaStreamSynchronize(stream);
+    }
+
+    cudaError_t buildWM(Level& L, int sampleCells) {
+        L.wm.free();
+        if (!wmEnabled || L.hostFlags.size() != static_cast<size_t>(L.n)) return cudaSuccess;
+        const std::vector<std::uint8_t>& clean =
+            L.surfaceRef.size() == L.hostFlags.size() ? L.surfaceRef : L.hostFlags;
+        WallListStats st;
+        WallList wl = build_wall_list(L.d, L.hostFlags.data(), clean.data(), sampleCells, &st);
+        L.wm.build = st;
+        if (wl.size() == 0) return cudaSuccess;
+        const size_t n = wl.size();
+        std::vector<std::uint32_t> ci(n), si(n);
+        for (size_t i = 0; i < n; ++i) {
+            ci[i] = static_cast<std::uint32_t>(wl.cellIdx[i]);
+            si[i] = static_cast<std::uint32_t>(wl.sampleIdx[i]);
+        }
+        WMLevel& m = L.wm;
+        const size_t cells = static_cast<size_t>(L.n);
+        cudaError_t e = cudaSuccess;
+        auto A = [&](auto** p, size_t b) { if (e == cudaSuccess) e = dalloc(p, b); };
+        A(&m.dCell, n * 4); A(&m.dSample, n * 4); A(&m.dMask, n * 4);
+        A(&m.dNx, n * 4); A(&m.dNy, n * 4); A(&m.dNz, n * 4); A(&m.dYs, n * 4); A(&m.dUTau, n * 4);
+        A(&m.dUwx, cells * 2); A(&m.dUwy, cells * 2); A(&m.dUwz, cells * 2);
+        A(&m.dStats, sizeof(WallStatsDev));
+        if (e != cudaSuccess) { m.free(); return e; }
+        auto U = [&](void* d, const void* h, size_t b) {
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, stream);
+        };
+        U(m.dCell, ci.data(), n * 4); U(m.dSample, si.data(), n * 4);
+        U(m.dMask, wl.linkMask.data(), n * 4);
+        U(m.dNx, wl.nX.data(), n * 4); U(m.dNy, wl.nY.data(), n * 4); U(m.dNz, wl.nZ.data(), n * 4);
+        U(m.dYs, wl.ys.data(), n * 4);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m.dUTau, 0, n * 4, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m.dUwx, 0, cells * 2, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m.dUwy, 0, cells * 2, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m.dUwz, 0, cells * 2, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m.dStats, 0, sizeof(WallStatsDev), stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) { m.free(); return e; }
+        m.count = static_cast<int>(n);
+        m.active = true;
+        return cudaSuccess;
+    }
+
+    void resetWMState() {
+        for (Level* L : {&coarse, &fine}) {
+            if (!L->wm.active) continue;
+            cudaMemsetAsync(L->wm.dUTau, 0, static_cast<size_t>(L->wm.count) * 4, stream);
+            cudaMemsetAsync(L->wm.dUwx, 0, static_cast<size_t>(L->n) * 2, stream);
+            cudaMemsetAsync(L->wm.dUwy, 0, static_cast<size_t>(L->n) * 2, stream);
+            cudaMemsetAsync(L->wm.dUwz, 0, static_cast<size_t>(L->n) * 2, stream);
+        }
+    }
+
+    RefineGeom geom() const {
+        RefineGeom g;
+        g.coarse = coarse.d; g.fine = fine.d;
+        g.boxX0 = box.x0; g.boxY0 = box.y0; g.boxX1 = box.x1; g.boxY1 = box.y1;
+        g.factor = factor;
+        return g;
+    }
+
+    cudaError_t seedFine() {
+        if (!fineActive) return cudaSuccess;
+        const float tc = effTau(), tf = fineTau(tc, factor);
+        for (int i = 0; i < 2; ++i) {
+            ++launches;
+            if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[coarse.src], coarse.kind,
+                                         fine.f[i], dSeed, seedCount, geom(), 0.0f,
+                                         tf / (static_cast<float>(factor) * tc), stream);
+                e != cudaSuccess)
+                return e;
+        }
+        return cudaSuccess;
+    }
+
+    void updateForcesFromFine() {
+        forcesFromFine = false;
+        if (!fineActive) return;
+        const int x0 = box.x0 + kRestrictBandHost, x1 = box.x1 - kRestrictBandHost;
+        const int y0 = box.y0 + kRestrictBandHost, y1 = box.y1 - kRestrictBandHost;
+        const LevelDims& d = dims;
+        for (int z = 0; z < d.nz; ++z)
+            for (int y = 0; y < d.ny; ++y)
+                for (int x = 0; x < d.nx; ++x) {
+                    const size_t i = static_cast<size_t>(x) + static_cast<size_t>(d.nx) * (y + static_cast<size_t>(d.ny) * z);
+                    if (coarse.hostFlags[i] != 1) continue;
+                    if (x < x0 || x >= x1 || y < y0 || y >= y1) return;
+                }
+        forcesFromFine = true;
+    }
+
+    void freeFine() {
+        fine.free_all();
+        dfree(dShell); dfree(dSeed); dfree(dScratch);
+        shellCount = seedCount = 0;
+        fineActive = false;
+        forcesFromFine = false;
+    }
+
+    void freeAll() {
+        if (stream) cudaStreamSynchronize(stream);
+        freeFine();
+        coarse.free_all();
+        dfree(rho); dfree(u); dfree(v); dfree(w); dfree(dForce); dfree(dNan);
+        if (hForce) { cudaFreeHost(hForce); hForce = nullptr; }
+        if (hNan) { cudaFreeHost(hNan); hNan = nullptr; }
+        for (cudaEvent_t* e : {&evT0, &evT1, &evForce, &evNan})
+            if (*e) { cudaEventDestroy(*e); *e = nullptr; }
+        for (auto& pr : colEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        colEv.clear();
+        colCells.clear();
+        for (cudaEvent_t* e : {&tmr0, &tmr1})
+            if (*e) { cudaEventDestroy(*e); *e = nullptr; }
+        colEvUsed = 0;
+        timingPending = forcePending = nanPending = false;
+        emaStepMs = lastStepMs = 0.0;
+        initialized = false;
+    }
+
+    // ---- stepping ----
+    cudaError_t collide(Level& L, const CollideParams& p, float* r, float* uu, float* vv, float* ww) {
+        cudaEvent_t e1 = nullptr, e2 = nullptr;
+        if (collideTiming) {
+            if (colEvUsed == colEv.size()) {
+                cudaEvent_t a, b;
+                cudaEventCreate(&a);
+                cudaEventCreate(&b);
+                colEv.emplace_back(a, b);
+                colCells.push_back(0.0);
+            }
+            e1 = colEv[colEvUsed].first;
+            e2 = colEv[colEvUsed].second;
+            colCells[colEvUsed] = static_cast<double>(L.n);
+            ++colEvUsed;
+            cudaEventRecord(e1, stream);
+        }
+        ++launches;
+        const cudaError_t e = launch_collide(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, p, r, uu,
+                                             vv, ww, L.wm.slip(), stream);
+        if (e2) cudaEventRecord(e2, stream);
+        return e;
+    }
+
+    cudaError_t forceReduce(Level& L) {
+        launches += 2;
+        return launch_force(storage, L.f[L.src], L.n, L.dLinkCells, L.dLinkMasks, L.linkCount,
+                            L.wm.slip(), L.dPartials, dForce, stream);
+    }
+
+    cudaError_t wallUpdate(Level& L, float nu) {
+        if (!L.wm.active) return cudaSuccess;
+        ++launches;
+        return launch_wall_update(storage, L.f[L.src], L.n, L.wm.list(), L.wm.dUwx, L.wm.dUwy,
+                                  L.wm.dUwz, nu, 1e-3f * scaling.u_lat, kWallEma, L.wm.dStats, stream);
+    }
+
+    int stepN(int n) {
+        if (!initialized) return cudaErrorNotReady;
+        if (n <= 0) return cudaSuccess;
+        pollAsync();
+        if (nanLatched) return cudaSuccess;
+        const bool timeIt = !timingPending;
+        if (timeIt) cudaEventRecord(evT0, stream);
+        for (int i = 0; i < n; ++i) {
+            CollideParams p;
+            p.tau = effTau();
+            p.magicLambda = lambda;
+            p.smagPrefactor = smagPre();
+            p.uInlet = effU();
+            p.writeMacro = (i == n - 1) ? 1 : 0;
+            if (auto e = collide(coarse, p, rho, u, v, w); e != cudaSuccess) return e;
+            if (fineActive) {
+                const int m = factor;
+                const float tc = p.tau, tf = fineTau(tc, m);
+                CollideParams fp = p;
+                fp.tau = tf;
+                fp.writeMacro = 0;
+                for (int k = 0; k < m; ++k) {
+                    ++launches;
+                    if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src],
+                                                 coarse.kind, fine.f[fine.src], dShell, shellCount, geom(),
+                                                 static_cast<float>(k) / static_cast<float>(m),
+                                                 tf / (static_cast<float>(m) * tc), stream);
+                        e != cudaSuccess)
+                        return e;
+                    if (auto e = collide(fine, fp, nullptr, nullptr, nullptr, nullptr); e != cudaSuccess)
+                        return e;
+                    fine.src = 1 - fine.src;
+                }
+                launches += 2;
+                const bool mac = p.writeMacro != 0;
+                if (auto e = launch_restrict_f2c(storage, fine.f[fine.src], fine.kind, coarse.f[1 - coarse.src],
+                                                 coarse.kind, geom(), (static_cast<float>(m) * tc) / tf,
+                                                 dScratch, mac ? rho : nullptr, mac ? u : nullptr,
+                                                 mac ? v : nullptr, mac ? w : nullptr, stream);
+                    e != cudaSuccess)
+                    return e;
+            }
+            coarse.src = 1 - coarse.src;
+            ++steps;
+            if (++sinceWatchdog >= kWatchdogPeriod && !nanPending) {
+                sinceWatchdog = 0;
+                cudaMemsetAsync(dNan, 0, sizeof(int), stream);
+                ++launches;
+                launch_watchdog(storage, coarse.f[coarse.src], coarse.d, dNan, steps * 977, 0, stream);
+                if (fineActive) {
+                    ++launches;
+                    launch_watchdog(storage, fine.f[fine.src], fine.d, dNan, steps * 977, 2, stream);
+                }
+                cudaMemcpyAsync(hNan, dNan, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                cudaEventRecord(evNan, stream);
+                nanPending = true;
+            }
+        }
+        if (timeIt) {
+            cudaEventRecord(evT1, stream);
+            timingPending = true;
+            timingN = n;
+        }
+        if (!forcePending) {
+            Level& L = (fineActive && forcesFromFine) ? fine : coarse;
+            if (forceReduce(L) == cudaSuccess) {
+                cudaMemcpyAsync(hForce, dForce, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream);
+                cudaEventRecord(evForce, stream);
+                forcePending = true;
+                stepsAtForceLaunch = steps;
+            }
+        }
+        const float tauNow = effTau();
+        if (coarse.wm.active) wallUpdate(coarse, (tauNow - 0.5f) / 3.0f);
+        if (fineActive && fine.wm.active) wallUpdate(fine, (fineTau(tauNow, factor) - 0.5f) / 3.0f);
+        return static_cast<int>(cudaGetLastError());
+    }
+
+    void reset() {
+        if (!initialized) return;
+        steps = 0;
+        coarse.src = 0;
+        fine.src = 0;
+        rampActive = true;
+        rampStart = 0;
+        gateOpenAt = static_cast<long long>(kForceGateFT * flowThroughSteps());
+        emaFx = emaFy = 0.f;
+        emaSeeded = false;
+        if (forcePending) { cudaStreamSynchronize(stream); forcePending = false; }
+        stepsAtForceLaunch = stepsAtLastFold = 0;
+        ringHead = ringCount = 0;
+        nanLatched = nanPending = false;
+        nanKind = 0;
+        sinceWatchdog = 0;
+        cudaMemsetAsync(dNan, 0, sizeof(int), stream);
+        const float initU = rampEnabled ? 0.0f : scaling.u_lat;
+        for (int i = 0; i < 2; ++i) {
+            launches += 2;
+            launch_init_equilibrium(storage, coarse.f[i], coarse.kind, coarse.d, initU, stream);
+            launch_speck(storage, coarse.f[i], coarse.kind, coarse.d, kSpeckAmplitudeFrac * scaling.u_lat,
+                         kSpeckSeed, stream);
+        }
+        seedFine();
+        resetWMState();
+    }
+
+    void notifyRestored(bool full) {
+        if (!initialized) return;
+        rampActive = false;
+        emaSeeded = false;
+        if (forcePending) { cudaStreamSynchronize(stream); forcePending = false; }
+        stepsAtLastFold = steps;
+        nanLatched = nanPending = false;
+        gateOpenAt = full ? steps + static_cast<long long>(0.25f * flowThroughSteps())
+                          : steps + kCompactSettleSteps
+                                + static_cast<long long>(kWarmGateFT * flowThroughSteps());
+    }
+
+    cudaError_t importF32(Level& L, const float* host, size_t count) {
+        if (count != static_cast<size_t>(L.n) * 19) return cudaErrorInvalidValue;
+        const size_t bytes = count * sizeof(float);
+        if (storage == Storage::F32)
+            return cudaMemcpy(L.f[L.src], host, bytes, cudaMemcpyHostToDevice);
+        float* stage = nullptr;
+        if (auto e = cudaMalloc(&stage, bytes); e != cudaSuccess) return e;
+        cudaError_t e = cudaMemcpy(stage, host, bytes, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_f32_to_store(storage, stage, L.f[L.src], L.n, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        cudaFree(stage);
+        return e;
+    }
+
+    cudaError_t exportF32(Level& L, float* host, size_t count) {
+        if (count != static_cast<size_t>(L.n) * 19) return cudaErrorInvalidValue;
+        const size_t bytes = count * sizeof(float);
+        if (auto e = cudaStreamSynchronize(stream); e != cudaSuccess) return e;
+        if (storage == Storage::F32)
+            return cudaMemcpy(host, L.f[L.src], bytes, cudaMemcpyDeviceToHost);
+        float* stage = nullptr;
+        if (auto e = cudaMalloc(&stage, bytes); e != cudaSuccess) return e;
+        cudaError_t e = launch_store_to_f32(storage, L.f[L.src], stage, L.n, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e == cudaSuccess) e = cudaMemcpy(host, stage, bytes, cudaMemcpyDeviceToHost);
+        cudaFree(stage);
+        return e;
+    }
+};
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+fcfd_scaling fcfd_compute_scaling(float chord_m, float airspeed_ms, float nu_m2s, int chord_cells,
+                                  float u_lat) {
+    fcfd_scaling s{};
+    s.chord_m = chord_m; s.airspeed_ms = airspeed_ms; s.nu_m2s = nu_m2s;
+    s.chord_cells = chord_cells;
+    s.u_lat = std::min(u_lat, kMaxULat);
+    s.dx = chord_m / static_cast<float>(chord_cells);
+    s.dt = s.u_lat * s.dx / airspeed_ms;
+    s.nu_lat_target = nu_m2s * s.dt / (s.dx * s.dx);
+    const float tauTarget = 3.0f * s.nu_lat_target + 0.5f;
+    s.tau = std::max(tauTarget, kMinTau);
+    s.tau_clamped = tauTarget < kMinTau ? 1 : 0;
+    s.nu_lat = (s.tau - 0.5f) / 3.0f;
+    s.re_target = airspeed_ms * chord_m / nu_m2s;
+    s.re_effective = s.u_lat * static_cast<float>(chord_cells) / s.nu_lat;
+    return s;
+}
+
+fcfd_scaling fcfd_refined_scaling(const fcfd_scaling* p, int factor) {
+    fcfd_scaling f = *p;
+    const float m = static_cast<float>(factor);
+    f.chord_cells = p->chord_cells * factor;
+    f.dx = p->dx / m;
+    f.dt = p->dt / m;
+    f.nu_lat_target = p->nu_lat_target * m;
+    f.nu_lat = p->nu_lat * m;
+    f.tau = 3.0f * f.nu_lat + 0.5f;
+    return f;
+}
+
+float fcfd_ramped_tau(const fcfd_scaling* s, long long step, int nx) {
+    const long long ramp = 2LL * nx;
+    if (step >= ramp) return s->tau;
+    const float t = static_cast<float>(step) / static_cast<float>(ramp);
+    const float nu = s->nu_lat * (4.0f + t * (1.0f - 4.0f));
+    return 3.0f * nu + 0.5f;
+}
+
+float fcfd_ramped_u(const fcfd_scaling* s, long long step, int nx) {
+    const long long ramp = static_cast<long long>(0.5f * 2.0f * static_cast<float>(nx));
+    if (ramp <= 0 || step >= ramp) return s->u_lat;
+    const float t = static_cast<float>(step) / static_cast<float>(ramp);
+    return s->u_lat * (t * t * (3.0f - 2.0f * t));
+}
+
+float fcfd_force_to_coefficient(const fcfd_scaling* s, float f, int span) {
+    const float q = 0.5f * s->u_lat * s->u_lat * static_cast<float>(s->chord_cells) * static_cast<float>(span);
+    return q > 0.0f ? f / q : 0.0f;
+}
+
+fcfd_solver* fcfd_create(void) { return new fcfd_solver(); }
+
+void fcfd_destroy(fcfd_solver* s) {
+    if (!s) return;
+    s->freeAll();
+    delete s;
+}
+
+int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling, const uint8_t* flags,
+              size_t n, void* stream, const fcfd_options* opts, char* err, size_t errlen) {
+    if (!s || !dims || !scaling || !flags) {
+        set_err(err, errlen, "null argument");
+        return cudaErrorInvalidValue;
+    }
+    s->freeAll();
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    if (d.nx < 3 || d.ny < 3 || d.nz < 1 || d.cells() <= 0) {
+        set_err(err, errlen, "grid dimensions out of range");
+        return cudaErrorInvalidValue;
+    }
+    if (d.cells() * 19 >= (1LL << 31) * 2 || d.cells() >= (1LL << 31)) {
+        set_err(err, errlen, "grid too large for 32-bit cell indices");
+        return cudaErrorInvalidValue;
+    }
+    if (n != static_cast<size_t>(d.cells())) {
+        set_err(err, errlen, "flag field size does not match grid dimensions");
+        return cudaErrorInvalidValue;
+    }
+    for (size_t i = 0; i < n; ++i)
+        if (flags[i] > FCFD_FLAG_OUTLET_EQ) {
+            set_err(err, errlen, "flag field holds an unknown cell flag value");
+            return cudaErrorInvalidValue;
+        }
+    s->dims = d;
+    s->scaling = *scaling;
+    s->stream = static_cast<cudaStream_t>(stream);
+    s->storage = Storage::F32;
+    s->lesCs = kDefaultCs;
+    s->lambda = kDefaultLambda;
+    if (opts) {
+        s->storage = opts->storage == FCFD_STORE_FP16 ? Storage::F16 : Storage::F32;
+        if (opts->les_cs != 0.0f) s->lesCs = opts->les_cs;
+        if (opts->magic_lambda > 0.0f) s->lambda = opts->magic_lambda;
+    }
+    auto fail = [&](const char* what, cudaError_t e) {
+        set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));
+        s->freeAll();
+        (void)cudaGetLastError();
+        return static_cast<int>(e);
+    };
+    if (auto e = s->allocLevel(s->coarse, d); e != cudaSuccess) return fail("population buffer allocation failed", e);
+    const size_t cells = static_cast<size_t>(d.cells());
+    for (float** p : {&s->rho, &s->u, &s->v, &s->w})
+        if (auto e = dalloc(p, cells * 4); e != cudaSuccess) return fail("macroscopic allocation failed", e);
+    if (auto e = dalloc(&s->dForce, 3 * sizeof(double)); e != cudaSuccess) return fail("force slot allocation failed", e);
+    if (auto e = dalloc(&s->dNan, sizeof(int)); e != cudaSuccess) return fail("watchdog allocation failed", e);
+    if (auto e = cudaMallocHost(&s->hForce, 3 * sizeof(double)); e != cudaSuccess) return fail("pinned allocation failed", e);
+    if (auto e = cudaMallocHost(&s->hNan, sizeof(int)); e != cudaSuccess) return fail("pinned allocation failed", e);
+    for (auto pr : {std::pair<cudaEvent_t*, unsigned>{&s->evT0, 0u}, {&s->evT1, 0u},
+                    {&s->evForce, static_cast<unsigned>(cudaEventDisableTiming)},
+                    {&s->evNan, static_cast<unsigned>(cudaEventDisableTiming)}})
+        if (auto e = cudaEventCreateWithFlags(pr.first, pr.second); e != cudaSuccess)
+            return fail("event creation failed", e);
+    *s->hNan = 0;
+    s->launches += 1;
+    launch_fill(s->rho, d.cells(), 1.0f, s->stream);
+    cudaMemsetAsync(s->u, 0, cells * 4, s->stream);
+    cudaMemsetAsync(s->v, 0, cells * 4, s->stream);
+    cudaMemsetAsync(s->w, 0, cells * 4, s->stream);
+    if (auto e = s->uploadLevelFlags(s->coarse, flags); e != cudaSuccess) return fail("flag upload failed", e);
+    s->zSlipWalls = false;
+    const size_t nxny = static_cast<size_t>(d.nx) * d.ny;
+    for (size_t i = 0; i < nxny; ++i)
+        if (flags[i] == FCFD_FLAG_SLIP_FRONT) { s->zSlipWalls = true; break; }
+    if (auto e = s->buildWM(s->coarse, kWallSampleCoarse); e != cudaSuccess) return fail("wall list upload failed", e);
+    s->initialized = true;
+    s->reset();
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return fail("initial field setup failed", e);
+    if (auto e = cudaGetLastError(); e != cudaSuccess) return fail("initial field setup failed", e);
+    set_err(err, errlen, "");
+    return 0;
+}
+
+void fcfd_reset(fcfd_solver* s) {
+    if (s) s->reset();
+}
+
+int fcfd_set_flags(fcfd_solver* s, const uint8_t* flags, size_t n) {
+    if (!s || !s->initialized || !flags || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
+    if (auto e = s->uploadLevelFlags(s->coarse, flags); e != cudaSuccess) return e;
+    s->updateForcesFromFine();
+    if (auto e = s->buildWM(s->coarse, kWallSampleCoarse); e != cudaSuccess) return e;
+    s->reset();
+    return 0;
+}
+
+void fcfd_set_startup_ramp(fcfd_solver* s, int enabled) {
+    if (s) s->rampEnabled = enabled != 0;
+}
+
+void fcfd_set_force_ema_window(fcfd_solver* s, float ft) {
+    if (s) s->emaWindowFT = std::max(0.05f, ft);
+}
+
+int fcfd_step_n(fcfd_solver* s, int n) { return s ? s->stepN(n) : cudaErrorInvalidValue; }
+
+int fcfd_synchronize(fcfd_solver* s) {
+    if (!s || !s->initialized) return cudaErrorNotReady;
+    const cudaError_t e = cudaStreamSynchronize(s->stream);
+    s->pollAsync();
+    return e;
+}
+
+long long fcfd_step_count(const fcfd_solver* s) { return s ? s->steps : 0; }
+float fcfd_current_tau(const fcfd_solver* s) { return (s && s->initialized) ? s->effTau() : 0.0f; }
+float fcfd_flow_throughs(const fcfd_solver* s) {
+    return (s && s->initialized) ? static_cast<float>(s->steps) / s->flowThroughSteps() : 0.0f;
+}
+
+int fcfd_forces(fcfd_solver* s, fcfd_force_readout* r) {
+    if (!s || !r) return cudaErrorInvalidValue;
+    *r = fcfd_force_readout{};
+    if (!s->initialized) return cudaErrorNotReady;
+    cudaStreamSynchronize(s->stream);
+    s->pollAsync();
+    r->flow_throughs = fcfd_flow_throughs(s);
+    const bool fineForces = s->fineActive && s->forcesFromFine;
+    const fcfd_scaling& fs = fineForces ? s->fineScaling : s->scaling;
+    const int span = fineForces ? s->fine.d.nz : (s->zSlipWalls ? std::max(1, s->dims.nz - 2) : s->dims.nz);
+    r->cd = fcfd_force_to_coefficient(&fs, s->emaFx, span);
+    r->cl = fcfd_force_to_coefficient(&fs, s->emaFy, span);
+    r->lift_to_drag = std::fabs(r->cd) > 1e-6f ? r->cl / r->cd : 0.0f;
+    r->valid = (s->emaSeeded && s->steps >= s->gateOpenAt) ? 1 : 0;
+    if (r->valid && s->ringCount > 0) {
+        const long long oneFT = static_cast<long long>(s->flowThroughSteps());
+        std::vector<float> cl, cd, ld;
+        for (int i = 0; i < s->ringCount; ++i) {
+            const int k = (s->ringHead - 1 - i + fcfd_solver::kRing) % fcfd_solver::kRing;
+            const ForceSample& sm = s->ring[k];
+            if (sm.step < oneFT) continue;
+            const float c1 = fcfd_force_to_coefficient(&fs, sm.fy, span);
+            const float c2 = fcfd_force_to_coefficient(&fs, sm.fx, span);
+            cl.push_back(c1); cd.push_back(c2);
+            ld.push_back(std::fabs(c2) > 1e-6f ? c1 / c2 : 0.0f);
+        }
+        if (!cl.empty()) {
+            auto stats = [](std::vector<float> v, float& avg, float& mn, float& mx, float& med) {
+                float sum = 0.f;
+                for (float x : v) sum += x;
+                avg = sum / static_cast<float>(v.size());
+                mn = *std::min_element(v.begin(), v.end());
+                mx = *std::max_element(v.begin(), v.end());
+                std::sort(v.begin(), v.end());
+                const size_t m = v.size() / 2;
+                med = v.size() % 2 == 0 ? 0.5f * (v[m - 1] + v[m]) : v[m];
+            };
+            stats(cl, r->cl_avg, r->cl_min, r->cl_max, r->cl_median);
+            stats(cd, r->cd_avg, r->cd_min, r->cd_max, r->cd_median);
+            stats(ld, r->ld_avg, r->ld_min, r->ld_max, r->ld_median);
+        }
+    }
+    return 0;
+}
+
+int fcfd_force_raw(fcfd_solver* s, double out[3]) {
+    if (!s || !out) return cudaErrorInvalidValue;
+    if (!s->initialized) return cudaErrorNotReady;
+    const cudaError_t e = cudaStreamSynchronize(s->stream);
+    s->pollAsync();
+    for (int i = 0; i < 3; ++i) out[i] = s->lastForce[i];
+    return e;
+}
+
+int fcfd_force_now(fcfd_solver* s, double out[3]) {
+    if (!s || !out) return cudaErrorInvalidValue;
+    if (!s->initialized) return cudaErrorNotReady;
+    cudaStreamSynchronize(s->stream);
+    s->pollAsync();
+    Level& L = (s->fineActive && s->forcesFromFine) ? s->fine : s->coarse;
+    if (auto e = s->forceReduce(L); e != cudaSuccess) return e;
+    double h[3];
+    if (auto e = cudaMemcpyAsync(h, s->dForce, sizeof h, cudaMemcpyDeviceToHost, s->stream); e != cudaSuccess)
+        return e;
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return e;
+    for (int i = 0; i < 3; ++i) out[i] = h[i];
+    return 0;
+}
+
+int fcfd_macro(fcfd_solver* s, const float** r, const float** u, const float** v, const float** w) {
+    if (!s || !s->initialized) return cudaErrorNotReady;
+    if (r) *r = s->rho;
+    if (u) *u = s->u;
+    if (v) *v = s->v;
+    if (w) *w = s->w;
+    return 0;
+}
+
+int fcfd_download_macro(fcfd_solver* s, float* r, float* u, float* v, float* w) {
+    if (!s || !s->initialized) return cudaErrorNotReady;
+    const size_t b = static_cast<size_t>(s->coarse.n) * 4;
+    struct { float* h; const float* d; } c[] = {{r, s->rho}, {u, s->u}, {v, s->v}, {w, s->w}};
+    for (auto& x : c)
+        if (x.h)
+            if (auto e = cudaMemcpyAsync(x.h, x.d, b, cudaMemcpyDeviceToHost, s->stream); e != cudaSuccess)
+                return e;
+    return cudaStreamSynchronize(s->stream);
+}
+
+void* fcfd_active_f(fcfd_solver* s) { return (s && s->initialized) ? s->coarse.f[s->coarse.src] : nullptr; }
+
+size_t fcfd_f_bytes(const fcfd_solver* s) {
+    if (!s || !s->initialized) return 0;
+    return static_cast<size_t>(s->coarse.n) * 19 * (s->storage == Storage::F32 ? 4 : 2);
+}
+
+void fcfd_notify_restored(fcfd_solver* s, int full) {
+    if (s) s->notifyRestored(full != 0);
+}
+
+int fcfd_import_f32(fcfd_solver* s, const float* f, size_t count) {
+    if (!s || !s->initialized || !f) return cudaErrorInvalidValue;
+    if (auto e = s->importF32(s->coarse, f, count); e != cudaSuccess) return e;
+    s->notifyRestored(true);
+    return 0;
+}
+
+int fcfd_export_f32(fcfd_solver* s, float* f, size_t count) {
+    if (!s || !s->initialized || !f) return cudaErrorInvalidValue;
+    return s->exportF32(s->coarse, f, count);
+}
+
+int fcfd_restore_from_macro(fcfd_solver* s, const float* r, const float* u, const float* v, const float* w) {
+    if (!s || !s->initialized || !r || !u || !v || !w) return cudaErrorInvalidValue;
+    const size_t b = static_cast<size_t>(s->coarse.n) * 4;
+    struct { const float* h; float* d; } c[] = {{r, s->rho}, {u, s->u}, {v, s->v}, {w, s->w}};
+    for (auto& x : c)
+        if (auto e = cudaMemcpyAsync(x.d, x.h, b, cudaMemcpyHostToDevice, s->stream); e != cudaSuccess) return e;
+    for (int i = 0; i < 2; ++i) {
+        ++s->launches;
+        if (auto e = launch_init_from_macro(s->storage, s->coarse.f[i], s->coarse.kind, s->coarse.d, s->rho,
+                                            s->u, s->v, s->w, s->stream);
+            e != cudaSuccess)
+            return e;
+    }
+    s->notifyRestored(false);
+    if (auto e = s->seedFine(); e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s->stream);
+}
+
+int fcfd_perf_stats(const fcfd_solver* s, fcfd_perf* p) {
+    if (!s || !p) return cudaErrorInvalidValue;
+    *p = fcfd_perf{};
+    double upd = static_cast<double>(s->coarse.n);
+    if (s->fineActive) upd += static_cast<double>(s->factor) * static_cast<double>(s->fine.n);
+    p->updates_per_step = upd;
+    p->last_step_ms = s->lastStepMs;
+    if (s->lastStepMs > 0.0) p->mlups = upd / (s->lastStepMs * 1000.0);
+    return 0;
+}
+
+int fcfd_nan_detected(fcfd_solver* s) {
+    if (!s || !s->initialized) return 0;
+    s->pollAsync();
+    return s->nanLatched ? 1 : 0;
+}
+
+int fcfd_nan_kind(fcfd_solver* s) {
+    if (!s || !s->initialized) return 0;
+    s->pollAsync();
+    return s->nanKind;
+}
+
+int fcfd_set_wall_model(fcfd_solver* s, int enabled) {
+    if (!s) return cudaErrorInvalidValue;
+    const bool en = enabled != 0;
+    if (s->wmEnabled == en) return 0;
+    s->wmEnabled = en;
+    if (!s->initialized) return 0;
+    cudaStreamSynchronize(s->stream);
+    if (auto e = s->buildWM(s->coarse, kWallSampleCoarse); e != cudaSuccess) return e;
+    if (s->fineActive)
+        if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return e;
+    return 0;
+}
+
+int fcfd_set_surface_reference(fcfd_solver* s, const uint8_t* clean, size_t n) {
+    if (!s || !s->initialized || !clean || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
+    cudaStreamSynchronize(s->stream);
+    s->coarse.surfaceRef.assign(clean, clean + n);
+    return s->buildWM(s->coarse, kWallSampleCoarse);
+}
+
+int fcfd_set_refined_surface_reference(fcfd_solver* s, const uint8_t* clean, size_t n) {
+    if (!s || !s->initialized || !s->fineActive || !clean || n != static_cast<size_t>(s->fine.n))
+        return cudaErrorInvalidValue;
+    cudaStreamSynchronize(s->stream);
+    s->fine.surfaceRef.assign(clean, clean + n);
+    return s->buildWM(s->fine, kWallSampleFine);
+}
+
+int fcfd_wall_model_readout(fcfd_solver* s, fcfd_wm_readout* r) {
+    if (!s || !r) return cudaErrorInvalidValue;
+    *r = fcfd_wm_readout{};
+    r->enabled = s->wmEnabled ? 1 : 0;
+    if (!s->initialized || !s->wmEnabled) return 0;
+    const WMLevel& wm = (s->fineActive && s->fine.wm.active) ? s->fine.wm : s->coarse.wm;
+    r->from_fine = (s->fineActive && s->fine.wm.active) ? 1 : 0;
+    r->excluded_vg = wm.build.excludedVG;
+    r->degenerate = wm.build.degenerate;
+    if (!wm.active) return 0;
+    WallStatsDev st{};
+    if (auto e = cudaMemcpyAsync(&st, wm.dStats, sizeof st, cudaMemcpyDeviceToHost, s->stream); e != cudaSuccess)
+        return e;
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return e;
+    r->cells = st.activeCells;
+    if (st.activeCells > 0) {
+        r->mean_yplus = st.sumYplus / static_cast<float>(st.activeCells);
+        float mx;
+        std::memcpy(&mx, &st.maxYplusBits, sizeof mx);
+        r->max_yplus = mx;
+        r->clamped_frac = static_cast<float>(st.clampedCells) / static_cast<float>(st.activeCells);
+    }
+    return 0;
+}
+
+static Level* level_of(fcfd_solver* s, int level) {
+    if (!s || !s->initialized) return nullptr;
+    if (level == 0) return &s->coarse;
+    if (level == 1 && s->fineActive) return &s->fine;
+    return nullptr;
+}
+
+int fcfd_wall_count(fcfd_solver* s, int level) {
+    Level* L = level_of(s, level);
+    return (L && L->wm.active) ? L->wm.count : 0;
+}
+
+int fcfd_export_wall_state(fcfd_solver* s, int level, float* utau, size_t nu, uint16_t* slip, size_t ns) {
+    Level* L = level_of(s, level);
+    if (!L || !L->wm.active) return cudaErrorInvalidValue;
+    cudaStreamSynchronize(s->stream);
+    if (utau) {
+        if (nu != static_cast<size_t>(L->wm.count)) return cudaErrorInvalidValue;
+        if (auto e = cudaMemcpy(utau, L->wm.dUTau, nu * 4, cudaMemcpyDeviceToHost); e != cudaSuccess) return e;
+    }
+    if (slip) {
+        const size_t n = static_cast<size_t>(L->n);
+        if (ns != 3 * n) return cudaErrorInvalidValue;
+        const std::uint16_t* src[3] = {L->wm.dUwx, L->wm.dUwy, L->wm.dUwz};
+        for (int k = 0; k < 3; ++k)
+            if (auto e = cudaMemcpy(slip + k * n, src[k], n * 2, cudaMemcpyDeviceToHost); e != cudaSuccess) return e;
+    }
+    return 0;
+}
+
+int fcfd_import_wall_state(fcfd_solver* s, int level, const float* utau, size_t nu, const uint16_t* slip,
+                           size_t ns) {
+    Level* L = level_of(s, level);
+    if (!L || !L->wm.active) return cudaErrorInvalidValue;
+    cudaStreamSynchronize(s->stream);
+    if (utau) {
+        if (nu != static_cast<size_t>(L->wm.count)) return cudaErrorInvalidValue;
+        if (auto e = cudaMemcpy(L->wm.dUTau, utau, nu * 4, cudaMemcpyHostToDevice); e != cudaSuccess) return e;
+    }
+    if (slip) {
+        const size_t n = static_cast<size_t>(L->n);
+        if (ns != 3 * n) return cudaErrorInvalidValue;
+        std::uint16_t* dst[3] = {L->wm.dUwx, L->wm.dUwy, L->wm.dUwz};
+        for (int k = 0; k < 3; ++k)
+            if (auto e = cudaMemcpy(dst[k], slip + k * n, n * 2, cudaMemcpyHostToDevice); e != cudaSuccess) return e;
+    }
+    return 0;
+}
+
+int fcfd_wall_update_now(fcfd_solver* s, int level, float nu, float cut) {
+    Level* L = level_of(s, level);
+    if (!L || !L->wm.active) return cudaErrorInvalidValue;
+    ++s->launches;
+    if (auto e = launch_wall_update(s->storage, L->f[L->src], L->n, L->wm.list(), L->wm.dUwx, L->wm.dUwy,
+                                    L->wm.dUwz, nu, cut, kWallEma, L->wm.dStats, s->stream);
+        e != cudaSuccess)
+        return e;
+    return cudaStreamSynchronize(s->stream);
+}
+
+int fcfd_init_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor, const uint8_t* ff, size_t n,
+                         char* err, size_t errlen) {
+    if (!s || !s->initialized) {
+        set_err(err, errlen, "solver not initialized");
+        return cudaErrorNotReady;
+    }
+    fcfd_shutdown_refinement(s);
+    if (!box || !ff) {
+        set_err(err, errlen, "null argument");
+        return cudaErrorInvalidValue;
+    }
+    if (factor < 2 || factor > 4) {
+        set_err(err, errlen, "refinement factor out of range (2..4)");
+        return cudaErrorInvalidValue;
+    }
+    if (box->x1 - box->x0 <= 8 || box->y1 - box->y0 <= 8 || box->x0 < 1 || box->y0 < 1
+        || box->x1 > s->dims.nx - 1 || box->y1 > s->dims.ny - 1) {
+        set_err(err, errlen, "refinement patch box out of range");
+        return cudaErrorInvalidValue;
+    }
+    LevelDims fd{factor * (box->x1 - box->x0), factor * (box->y1 - box->y0), factor * s->dims.nz};
+    if (n != static_cast<size_t>(fd.cells())) {
+        set_err(err, errlen, "fine flag field size does not match the patch");
+        return cudaErrorInvalidValue;
+    }
+    if (fd.cells() >= (1LL << 31)) {
+        set_err(err, errlen, "fine grid too large for 32-bit cell indices");
+        return cudaErrorInvalidValue;
+    }
+    cudaStreamSynchronize(s->stream);
+    s->factor = factor;
+    s->box = *box;
+    s->fineScaling = fcfd_refined_scaling(&s->scaling, factor);
+    auto fail = [&](const char* what, cudaError_t e) {
+        set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));
+        s->freeFine();
+        (void)cudaGetLastError();
+        return static_cast<int>(e);
+    };
+    if (auto e = s->allocLevel(s->fine, fd); e != cudaSuccess) return fail("fine buffer allocation failed", e);
+    if (auto e = s->uploadLevelFlags(s->fine, ff); e != cudaSuccess) return fail("fine flag upload failed", e);
+    std::vector<std::uint32_t> shell, seed;
+    for (size_t i = 0; i < n; ++i) {
+        if (ff[i] == FCFD_FLAG_INTERFACE) shell.push_back(static_cast<std::uint32_t>(i));
+        if (ff[i] != FCFD_FLAG_SOLID) seed.push_back(static_cast<std::uint32_t>(i));
+    }
+    s->shellCount = static_cast<int>(shell.size());
+    s->seedCount = static_cast<int>(seed.size());
+    if (auto e = dalloc(&s->dShell, shell.size() * 4); e != cudaSuccess) return fail("shell list allocation failed", e);
+    if (auto e = dalloc(&s->dSeed, seed.size() * 4); e != cudaSuccess) return fail("seed list allocation failed", e);
+    if (!shell.empty()) cudaMemcpy(s->dShell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice);
+    if (!seed.empty()) cudaMemcpy(s->dSeed, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
+    s->fineActive = true;
+    const long long sf = restrict_scratch_floats(s->geom());
+    if (sf <= 0) return fail("restriction sub-box is empty", cudaErrorInvalidValue);
+    if (auto e = dalloc(&s->dScratch, static_cast<size_t>(sf) * 4); e != cudaSuccess)
+        return fail("restriction scratch allocation failed", e);
+    s->updateForcesFromFine();
+    if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return fail("fine wall list failed", e);
+    if (auto e = s->seedFine(); e != cudaSuccess) return fail("fine level seeding failed", e);
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return fail("fine level seeding failed", e);
+    set_err(err, errlen, "");
+    return 0;
+}
+
+void fcfd_shutdown_refinement(fcfd_solver* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->freeFine();
+}
+
+int fcfd_set_refined_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {
+    if (!s || !s->initialized || !s->fineActive || !ff || n != static_cast<size_t>(s->fine.n))
+        return cudaErrorInvalidValue;
+    if (auto e = s->uploadLevelFlags(s->fine, ff); e != cudaSuccess) return e;
+    std::vector<std::uint32_t> shell, seed;
+    for (size_t i = 0; i < n; ++i) {
+        if (ff[i] == FCFD_FLAG_INTERFACE) shell.push_back(static_cast<std::uint32_t>(i));
+        if (ff[i] != FCFD_FLAG_SOLID) seed.push_back(static_cast<std::uint32_t>(i));
+    }
+    dfree(s->dShell); dfree(s->dSeed);
+    s->shellCount = static_cast<int>(shell.size());
+    s->seedCount = static_cast<int>(seed.size());
+    if (auto e = dalloc(&s->dShell, shell.size() * 4); e != cudaSuccess) return e;
+    if (auto e = dalloc(&s->dSeed, seed.size() * 4); e != cudaSuccess) return e;
+    if (!shell.empty()) cudaMemcpy(s->dShell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice);
+    if (!seed.empty()) cudaMemcpy(s->dSeed, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
+    s->updateForcesFromFine();
+    if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return e;
+    return s->seedFine();
+}
+
+int fcfd_refinement_info(const fcfd_solver* s, fcfd_refine_info* r) {
+    if (!s || !r) return cudaErrorInvalidValue;
+    *r = fcfd_refine_info{};
+    if (!s->fineActive) return 0;
+    r->active = 1;
+    r->factor = s->factor;
+    r->box = s->box;
+    r->fine_dims = fcfd_dims{s->fine.d.nx, s->fine.d.ny, s->fine.d.nz};
+    r->forces_from_fine = s->forcesFromFine ? 1 : 0;
+    r->vram_bytes = 2.0 * 19.0 * static_cast<double>(s->fine.n) * (s->storage == Storage::F32 ? 4 : 2)
+                  + 2.0 * static_cast<double>(s->fine.n);
+    return 0;
+}
+
+int fcfd_import_fine_f32(fcfd_solver* s, const float* f, size_t count) {
+    if (!s || !s->initialized || !s->fineActive || !f) return cudaErrorInvalidValue;
+    return s->importF32(s->fine, f, count);
+}
+
+int fcfd_export_fine_f32(fcfd_solver* s, float* f, size_t count) {
+    if (!s || !s->initialized || !s->fineActive || !f) return cudaErrorInvalidValue;
+    return s->exportF32(s->fine, f, count);
+}
+
+long long fcfd_build_wall_list(const fcfd_dims* dims, const uint8_t* active, const uint8_t* clean,
+                               int sample, long long* ci, long long* si, float* nx, float* ny, float* nz,
+                               float* ys, uint32_t* mask, long long cap, int* stats) {
+    if (!dims || !active) return -1;
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    WallListStats st;
+    const WallList wl = build_wall_list(d, active, clean ? clean : active, sample, &st);
+    if (stats) { stats[0] = st.listed; stats[1] = st.excludedVG; stats[2] = st.degenerate; }
+    const long long n = static_cast<long long>(wl.size());
+    if (n > cap) return -1;
+    for (long long i = 0; i < n; ++i) {
+        if (ci) ci[i] = wl.cellIdx[i];
+        if (si) si[i] = wl.sampleIdx[i];
+        if (nx) nx[i] = wl.nX[i];
+        if (ny) ny[i] = wl.nY[i];
+        if (nz) nz[i] = wl.nZ[i];
+        if (ys) ys[i] = wl.ys[i];
+        if (mask) mask[i] = wl.linkMask[i];
+    }
+    return n;
+}
+
+int fcfd_boundary_flags(const fcfd_dims* dims, uint8_t* flags, size_t n) {
+    if (!dims || !flags) return -1;
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    if (n != static_cast<size_t>(d.cells()) || d.nx < 2 || d.ny < 2) return -1;
+    boundary_flags(d, flags);
+    return 0;
+}
+
+int fcfd_naca4(const char* digits, int pps, float* xy, int cap) {
+    std::vector<float> v;
+    const int n = naca4(digits, pps, v);
+    if (n < 0 || n > cap || !xy) return -1;
+    std::memcpy(xy, v.data(), v.size() * sizeof(float));
+    return n;
+}
+
+int fcfd_voxelize_airfoil(const fcfd_dims* dims, const float* xy, int npts, float aoa, int chord,
+                          float ax, float ay, uint8_t* flags, size_t n) {
+    if (!dims || !xy || !flags) return -1;
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    if (n != static_cast<size_t>(d.cells())) return -1;
+    return voxelize_airfoil(d, xy, npts, aoa, chord, ax, ay, flags);
+}
+
+int fcfd_stamp_interface_shell(const fcfd_dims* dims, uint8_t* flags, size_t n) {
+    if (!dims || !flags) return -1;
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    if (n != static_cast<size_t>(d.cells())) return -1;
+    stamp_interface_shell(d, flags, kInterfaceShell);
+    return 0;
+}
+
+fcfd_patch_box fcfd_derive_patch_box(const fcfd_dims* dims, const uint8_t* flags, int mx0, int mx1, int my0,
+                                     int my1, int clearance) {
+    fcfd_patch_box b{};
+    if (!dims || !flags) return b;
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    int o[4];
+    derive_patch_box(d, flags, mx0, mx1, my0, my1, clearance, o);
+    b.x0 = o[0]; b.y0 = o[1]; b.x1 = o[2]; b.y1 = o[3];
+    return b;
+}
+
+long long fcfd_kernel_launches(const fcfd_solver* s) { return s ? s->launches : 0; }
+
+int fcfd_enable_collide_timing(fcfd_solver* s, int enabled) {
+    if (!s) return cudaErrorInvalidValue;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->collideTiming = enabled != 0;
+    s->colEvUsed = 0;
+    return 0;
+}
+
+int fcfd_collide_time_ms(fcfd_solver* s, double* total, long long* count, double* cells) {
+    if (!s || !total || !count) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return e;
+    double t = 0.0, c = 0.0;
+    for (size_t i = 0; i < s->colEvUsed; ++i) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->colEv[i].first, s->colEv[i].second) == cudaSuccess) t += ms;
+        c += s->colCells[i];
+    }
+    *total = t;
+    *count = static_cast<long long>(s->colEvUsed);
+    if (cells) *cells = c;
+    s->colEvUsed = 0;
+    return 0;
+}
+
+int fcfd_timer_start(fcfd_solver* s) {
+    if (!s || !s->initialized) return cudaErrorNotReady;
+    for (cudaEvent_t* e : {&s->tmr0, &s->tmr1})
+        if (!*e)
+            if (auto r = cudaEventCreate(e); r != cudaSuccess) return r;
+    return cudaEventRecord(s->tmr0, s->stream);
+}
+
+int fcfd_timer_stop(fcfd_solver* s, double* ms) {
+    if (!s || !s->initialized || !ms || !s->tmr0) return cudaErrorNotReady;
+    if (auto r = cudaEventRecord(s->tmr1, s->stream); r != cudaSuccess) return r;
+    if (auto r = cudaEventSynchronize(s->tmr1); r != cudaSuccess) return r;
+    float f = 0.f;
+    if (auto r = cudaEventElapsedTime(&f, s->tmr0, s->tmr1); r != cudaSuccess) return r;
+    *ms = f;
+    return 0;
+}
+
+void* fcfd_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void fcfd_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+const char* fcfd_version(void) { return "foilcfd-gb300 0.1 (sm_103a)"; }
+
+} // extern "C"

@@ -1,0 +1,403 @@
+"""Host-side mirror of the reference solver interface (src/sim/lbm_solver.h,
+src/sim/units.h) over the C ABI. Method names follow the reference class
+(init, reset, set_flags, step_n, forces, ...), arguments keep their meaning,
+and errors keep the reference behaviour: ``init``/``init_refinement`` report
+failure with a reason (raised here as ``SolverError``), ``step_n`` returns a
+cudaError_t code (0 = success).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from .capi import ptr
+
+Q = 19
+FLAG = dict(fluid=0, solid=1, inlet=2, outlet=3, slip_top=4, slip_bottom=5, slip_front=6, slip_back=7,
+            interface=8, outlet_eq=9)
+STORE = dict(fp32=0, fp16=1)
+K_SMAGORINSKY_CS = 0.1733
+K_TRT_MAGIC = 3.0 / 16.0
+K_NU_AIR = 1.48e-5
+
+
+class SolverError(RuntimeError):
+    pass
+
+
+def compute_scaling(chord_m: float, airspeed_ms: float, nu_m2s: float, chord_cells: int,
+                    u_lat: float = 0.08) -> capi.Scaling:
+    """units.h computeScaling: dx, dt, nu_lat, tau (clamped at 0.5005)."""
+    return capi.load().fcfd_compute_scaling(chord_m, airspeed_ms, nu_m2s, chord_cells, u_lat)
+
+
+def scaling_for_nu(nu_lat: float, u_lat: float, chord_cells: int, chord_m: float = 1.0) -> capi.Scaling:
+    """Scaling whose lattice viscosity lands on nu_lat (the tests' reverse
+    engineering of the physical inputs, tests/m0_taylor_green.cpp:37-47)."""
+    airspeed = K_NU_AIR * u_lat * chord_cells / (nu_lat * chord_m)
+    return compute_scaling(chord_m, airspeed, K_NU_AIR, chord_cells, u_lat)
+
+
+def scaling_direct(tau: float, u_lat: float, chord_cells: int = 64) -> capi.Scaling:
+    """Scaling with a given relaxation time and lattice speed (test harness
+    helper: parity runs replay a fixed tau / u_lat exactly)."""
+    s = capi.Scaling()
+    s.chord_m, s.airspeed_ms, s.nu_m2s = 1.0, 1.0, 1.0
+    s.chord_cells, s.u_lat, s.tau = chord_cells, u_lat, tau
+    s.nu_lat = (tau - 0.5) / 3.0
+    s.nu_lat_target = s.nu_lat
+    s.dx = 1.0 / chord_cells
+    s.dt = u_lat * s.dx
+    s.re_target = s.re_effective = u_lat * chord_cells / s.nu_lat
+    return s
+
+
+def refined_scaling(parent: capi.Scaling, factor: int) -> capi.Scaling:
+    return capi.load().fcfd_refined_scaling(C.byref(parent), factor)
+
+
+def force_to_coefficient(s: capi.Scaling, force_lat: float, span_cells: int) -> float:
+    return capi.load().fcfd_force_to_coefficient(C.byref(s), force_lat, span_cells)
+
+
+@dataclass
+class Box:
+    x0: int
+    y0: int
+    x1: int
+    y1: int
+
+    def as_c(self) -> capi.PatchBox:
+        return capi.PatchBox(self.x0, self.y0, self.x1, self.y1)
+
+
+def fine_dims_for(box: Box, dims, factor: int = 2):
+    return (factor * (box.x1 - box.x0), factor * (box.y1 - box.y0), factor * dims[2])
+
+
+class LBMSolver:
+    """One wind tunnel on one GPU (reference foilcfd::LBMSolver)."""
+
+    def __init__(self):
+        self._lib = capi.load()
+        self._h = self._lib.fcfd_create()
+        self.dims = None
+        self.scaling = None
+        self.storage = "fp32"
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.fcfd_destroy(h)
+            self._h = None
+
+    # ---- lifecycle -------------------------------------------------------
+    def init(self, dims, scaling: capi.Scaling, flags: np.ndarray, stream=None, storage: str = "fp32",
+             les_cs: float | None = None, magic_lambda: float | None = None) -> None:
+        flags = np.ascontiguousarray(flags, np.uint8)
+        d = capi.Dims(*dims)
+        opt = capi.Options(STORE[storage], 0.0 if les_cs is None else (les_cs if les_cs > 0 else -1.0),
+                           0.0 if magic_lambda is None else magic_lambda, 0)
+        err = C.create_string_buffer(512)
+        rc = self._lib.fcfd_init(self._h, C.byref(d), C.byref(scaling), ptr(flags), flags.size, stream,
+                                 C.byref(opt), err, 512)
+        if rc != 0:
+            raise SolverError(err.value.decode() or f"init failed ({rc})")
+        self.dims = tuple(dims)
+        self.scaling = scaling
+        self.storage = storage
+
+    @property
+    def ncells(self) -> int:
+        return int(np.prod(self.dims))
+
+    def reset(self):
+        self._lib.fcfd_reset(self._h)
+
+    def set_flags(self, flags):
+        flags = np.ascontiguousarray(flags, np.uint8)
+        return self._lib.fcfd_set_flags(self._h, ptr(flags), flags.size)
+
+    def set_startup_ramp_enabled(self, enabled: bool):
+        self._lib.fcfd_set_startup_ramp(self._h, int(enabled))
+
+    def set_force_ema_window(self, flow_throughs: float):
+        self._lib.fcfd_set_force_ema_window(self._h, flow_throughs)
+
+    # ---- stepping --------------------------------------------------------
+    def step_n(self, n: int) -> int:
+        return self._lib.fcfd_step_n(self._h, n)
+
+    def synchronize(self) -> int:
+        return self._lib.fcfd_synchronize(self._h)
+
+    def step_count(self) -> int:
+        return self._lib.fcfd_step_count(self._h)
+
+    def current_tau(self) -> float:
+        return self._lib.fcfd_current_tau(self._h)
+
+    def flow_throughs_completed(self) -> float:
+        return self._lib.fcfd_flow_throughs(self._h)
+
+    # ---- read-back -------------------------------------------------------
+    def forces(self) -> capi.ForceReadout:
+        r = capi.ForceReadout()
+        self._lib.fcfd_forces(self._h, C.byref(r))
+        return r
+
+    def force_raw(self) -> np.ndarray:
+        out = np.zeros(3, np.float64)
+        rc = self._lib.fcfd_force_raw(self._h, ptr(out))
+        if rc:
+            raise SolverError(f"force readback failed ({rc})")
+        return out
+
+    def force_now(self) -> np.ndarray:
+        out = np.zeros(3, np.float64)
+        rc = self._lib.fcfd_force_now(self._h, ptr(out))
+        if rc:
+            raise SolverError(f"force reduction failed ({rc})")
+        return out
+
+    def download_macro(self):
+        n = self.ncells
+        arrs = [np.empty(n, np.float32) for _ in range(4)]
+        rc = self._lib.fcfd_download_macro(self._h, *[ptr(a) for a in arrs])
+        if rc:
+            raise SolverError(f"macro download failed ({rc})")
+        return arrs
+
+    def download_macro_into(self, rho, u, v, w) -> int:
+        return self._lib.fcfd_download_macro(self._h, ptr(rho), ptr(u), ptr(v), ptr(w))
+
+    def import_f32(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, np.float32)
+        rc = self._lib.fcfd_import_f32(self._h, ptr(f), f.size)
+        if rc:
+            raise SolverError(f"import failed ({rc})")
+
+    def export_f32(self) -> np.ndarray:
+        f = np.empty(Q * self.ncells, np.float32)
+        rc = self._lib.fcfd_export_f32(self._h, ptr(f), f.size)
+        if rc:
+            raise SolverError(f"export failed ({rc})")
+        return f
+
+    def notify_snapshot_restored(self, full_state: bool):
+        self._lib.fcfd_notify_restored(self._h, int(full_state))
+
+    def restore_from_macroscopic(self, rho, u, v, w):
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (rho, u, v, w)]
+        rc = self._lib.fcfd_restore_from_macro(self._h, *[ptr(a) for a in arrs])
+        if rc:
+            raise SolverError(f"macroscopic restore failed ({rc})")
+
+    def f_buffer_bytes(self) -> int:
+        return self._lib.fcfd_f_bytes(self._h)
+
+    def perf_stats(self) -> capi.Perf:
+        p = capi.Perf()
+        self._lib.fcfd_perf_stats(self._h, C.byref(p))
+        return p
+
+    def nan_detected(self) -> bool:
+        return bool(self._lib.fcfd_nan_detected(self._h))
+
+    def nan_kind(self) -> int:
+        return self._lib.fcfd_nan_kind(self._h)
+
+    # ---- wall model ------------------------------------------------------
+    def set_wall_model_enabled(self, enabled: bool):
+        rc = self._lib.fcfd_set_wall_model(self._h, int(enabled))
+        if rc:
+            raise SolverError(f"wall model setup failed ({rc})")
+
+    def set_surface_reference(self, clean):
+        clean = np.ascontiguousarray(clean, np.uint8)
+        return self._lib.fcfd_set_surface_reference(self._h, ptr(clean), clean.size)
+
+    def set_refined_surface_reference(self, clean):
+        clean = np.ascontiguousarray(clean, np.uint8)
+        return self._lib.fcfd_set_refined_surface_reference(self._h, ptr(clean), clean.size)
+
+    def wall_model_readout(self) -> capi.WMReadout:
+        r = capi.WMReadout()
+        self._lib.fcfd_wall_model_readout(self._h, C.byref(r))
+        return r
+
+    def wall_count(self, level: int = 0) -> int:
+        return self._lib.fcfd_wall_count(self._h, level)
+
+    def export_wall_state(self, level: int = 0):
+        cnt = self.wall_count(level)
+        n = self.ncells if level == 0 else int(np.prod(self.refinement_info_dims()))
+        utau = np.empty(cnt, np.float32)
+        slip = np.empty(3 * n, np.uint16)
+        rc = self._lib.fcfd_export_wall_state(self._h, level, ptr(utau), cnt, ptr(slip), slip.size)
+        if rc:
+            raise SolverError(f"wall state export failed ({rc})")
+        return utau, slip.reshape(3, n)
+
+    def import_wall_state(self, level: int, utau, slip):
+        utau = np.ascontiguousarray(utau, np.float32)
+        slip = np.ascontiguousarray(slip, np.uint16).ravel()
+        rc = self._lib.fcfd_import_wall_state(self._h, level, ptr(utau), utau.size, ptr(slip), slip.size)
+        if rc:
+            raise SolverError(f"wall state import failed ({rc})")
+
+    def wall_update_now(self, level: int, nu_lat: float, ut_cutoff: float):
+        rc = self._lib.fcfd_wall_update_now(self._h, level, nu_lat, ut_cutoff)
+        if rc:
+            raise SolverError(f"wall update failed ({rc})")
+
+    # ---- refinement ------------------------------------------------------
+    def init_refinement(self, box: Box, factor: int, fine_flags) -> None:
+        ff = np.ascontiguousarray(fine_flags, np.uint8)
+        err = C.create_string_buffer(512)
+        b = box.as_c()
+        rc = self._lib.fcfd_init_refinement(self._h, C.byref(b), factor, ptr(ff), ff.size, err, 512)
+        if rc != 0:
+            raise SolverError(err.value.decode() or f"initRefinement failed ({rc})")
+
+    def shutdown_refinement(self):
+        self._lib.fcfd_shutdown_refinement(self._h)
+
+    def set_refined_flags(self, fine_flags):
+        ff = np.ascontiguousarray(fine_flags, np.uint8)
+        return self._lib.fcfd_set_refined_flags(self._h, ptr(ff), ff.size)
+
+    def refinement_info(self) -> capi.RefineInfo:
+        r = capi.RefineInfo()
+        self._lib.fcfd_refinement_info(self._h, C.byref(r))
+        return r
+
+    def refinement_info_dims(self):
+        r = self.refinement_info()
+        return (r.fine_dims.nx, r.fine_dims.ny, r.fine_dims.nz)
+
+    def import_fine_f32(self, f):
+        f = np.ascontiguousarray(f, np.float32)
+        rc = self._lib.fcfd_import_fine_f32(self._h, ptr(f), f.size)
+        if rc:
+            raise SolverError(f"fine import failed ({rc})")
+
+    def export_fine_f32(self) -> np.ndarray:
+        n = int(np.prod(self.refinement_info_dims()))
+        f = np.empty(Q * n, np.float32)
+        rc = self._lib.fcfd_export_fine_f32(self._h, ptr(f), f.size)
+        if rc:
+            raise SolverError(f"fine export failed ({rc})")
+        return f
+
+    # ---- diagnostics -----------------------------------------------------
+    def kernel_launches(self) -> int:
+        return self._lib.fcfd_kernel_launches(self._h)
+
+    def enable_collide_timing(self, enabled: bool):
+        self._lib.fcfd_enable_collide_timing(self._h, int(enabled))
+
+    def collide_time_ms(self):
+        """(total ms, launches, cells updated) of the timed collide launches."""
+        t = C.c_double()
+        n = C.c_longlong()
+        c = C.c_double()
+        self._lib.fcfd_collide_time_ms(self._h, C.byref(t), C.byref(n), C.byref(c))
+        return t.value, n.value, c.value
+
+    def timer_start(self):
+        rc = self._lib.fcfd_timer_start(self._h)
+        if rc:
+            raise SolverError(f"timer start failed ({rc})")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        rc = self._lib.fcfd_timer_stop(self._h, C.byref(ms))
+        if rc:
+            raise SolverError(f"timer stop failed ({rc})")
+        return ms.value
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory (released on close/GC)."""
+
+    def __init__(self, n: int, dtype=np.float32):
+        self._lib = capi.load()
+        nbytes = int(n) * np.dtype(dtype).itemsize
+        self._p = self._lib.fcfd_host_alloc(nbytes)
+        if not self._p:
+            raise SolverError("pinned host allocation failed")
+        buf = (C.c_char * nbytes).from_address(self._p)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(n))
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self.array = None
+            self._lib.fcfd_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        self.close()
+
+
+# ---- host fixture builders (no GPU needed) ------------------------------------
+
+def boundary_flags(dims) -> np.ndarray:
+    """voxelizer.h buildBoundaryFlags: inlet x=0, outlet x=nx-1, slip y faces."""
+    f = np.zeros(int(np.prod(dims)), np.uint8)
+    d = capi.Dims(*dims)
+    if capi.load().fcfd_boundary_flags(C.byref(d), ptr(f), f.size) != 0:
+        raise SolverError("bad dims")
+    return f
+
+
+def naca4(digits: str, points_per_surface: int = 200) -> np.ndarray:
+    cap = 2 * max(points_per_surface, 20)
+    xy = np.zeros(2 * cap, np.float32)
+    n = capi.load().fcfd_naca4(digits.encode(), points_per_surface, ptr(xy), cap)
+    if n < 0:
+        raise SolverError(f"bad NACA digits {digits!r}")
+    return xy[: 2 * n].reshape(n, 2).copy()
+
+
+def voxelize_airfoil(dims, flags, xy, aoa_deg, chord_cells, anchor_x, anchor_y) -> int:
+    xy = np.ascontiguousarray(xy, np.float32)
+    d = capi.Dims(*dims)
+    return capi.load().fcfd_voxelize_airfoil(C.byref(d), ptr(xy), xy.shape[0], aoa_deg, chord_cells, anchor_x,
+                                             anchor_y, ptr(flags), flags.size)
+
+
+def stamp_interface_shell(dims, flags):
+    d = capi.Dims(*dims)
+    capi.load().fcfd_stamp_interface_shell(C.byref(d), ptr(flags), flags.size)
+    return flags
+
+
+def derive_patch_box(dims, flags, mx0, mx1, my0, my1, clearance) -> Box:
+    d = capi.Dims(*dims)
+    b = capi.load().fcfd_derive_patch_box(C.byref(d), ptr(np.ascontiguousarray(flags, np.uint8)), mx0, mx1, my0,
+                                          my1, clearance)
+    return Box(b.x0, b.y0, b.x1, b.y1)
+
+
+def build_wall_list(dims, active, clean=None, sample_cells: int = 2):
+    """wall_model.h buildWallCellList; returns dict of SoA arrays + stats."""
+    active = np.ascontiguousarray(active, np.uint8)
+    clean = active if clean is None else np.ascontiguousarray(clean, np.uint8)
+    cap = int(np.count_nonzero(active == 0)) + 1
+    out = dict(cell=np.zeros(cap, np.int64), sample=np.zeros(cap, np.int64), nx=np.zeros(cap, np.float32),
+               ny=np.zeros(cap, np.float32), nz=np.zeros(cap, np.float32), ys=np.zeros(cap, np.float32),
+               mask=np.zeros(cap, np.uint32))
+    stats = np.zeros(3, np.int32)
+    d = capi.Dims(*dims)
+    n = capi.load().fcfd_build_wall_list(C.byref(d), ptr(active), ptr(clean), sample_cells, ptr(out["cell"]),
+                                         ptr(out["sample"]), ptr(out["nx"]), ptr(out["ny"]), ptr(out["nz"]),
+                                         ptr(out["ys"]), ptr(out["mask"]), cap, ptr(stats))
+    if n < 0:
+        raise SolverError("wall list build failed")
+    res = {k: v[:n].copy() for k, v in out.items()}
+    res["stats"] = dict(listed=int(stats[0]), excluded_vg=int(stats[1]), degenerate=int(stats[2]))
+    return res

@@ -1,0 +1,87 @@
+"""ORACLE - test infrastructure only. Recipe that compiles the reference's
+own solver-step kernels for the CPU into ``oracle/_ref/`` (git-ignored).
+
+For each of src/sim/lbm_core.cu, lbm_wallmodel.cu and lbm_refine.cu the
+kernel section (everything up to the close of the file's anonymous
+namespace, i.e. all kernels and device helpers, without the ``<<<>>>``
+launch wrappers) is read from the reference tree where it lies and streamed
+through a pipe into g++, preceded by ``ref_shim.h`` / ``ref_launch.h`` (CUDA
+built-in stand-ins, fiber-emulated blocks) and followed by a driver of ours
+(``ref_driver_*.inc``) that exposes extern "C" entry points. No reference
+text is written to disk. Contraction is off (-ffp-contract=off) so the CPU
+build evaluates the reference expressions exactly as written.
+
+Used only in this container, to pin the C++ restatement (lbm_oracle.cpp)
+and to generate the golden fixtures under tests/golden/.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+REFERENCE = Path(os.environ.get("FOILCFD_REFERENCE", "/root/reference"))
+SIM = REFERENCE / "src" / "sim"
+UNITS = {
+    "core": ("lbm_core.cu", "ref_driver_core.inc"),
+    "wall": ("lbm_wallmodel.cu", "ref_driver_wall.inc"),
+    "refine": ("lbm_refine.cu", "ref_driver_refine.inc"),
+}
+FLAGS = ["-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w"]
+
+
+def available() -> bool:
+    return all((SIM / src).exists() for src, _ in UNITS.values()) and (SIM / "wall_model.cpp").exists()
+
+
+def _kernel_section(path: Path) -> str:
+    lines = path.read_text().splitlines(keepends=True)
+    for i, line in enumerate(lines):
+        if line.rstrip() == "} // namespace":
+            return "".join(lines[: i + 1])
+    raise RuntimeError(f"no anonymous-namespace close found in {path}")
+
+
+def _cuda_include() -> str:
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and Path(c, "include", "cuda_runtime_api.h").exists():
+            return str(Path(c, "include"))
+    raise RuntimeError("CUDA headers not found")
+
+
+def build(force: bool = False) -> dict:
+    """Build the three reference CPU libraries; returns {unit: path}."""
+    if not available():
+        raise RuntimeError(f"reference sources not found under {SIM}")
+    OUT.mkdir(parents=True, exist_ok=True)
+    libs = {}
+    for unit, (src, drv) in UNITS.items():
+        so = OUT / f"libref_{unit}.so"
+        libs[unit] = so
+        if so.exists() and not force:
+            continue
+        text = _kernel_section(SIM / src) + "\n" + (HERE / drv).read_text()
+        cmd = ["g++", *FLAGS, "-include", str(HERE / "ref_shim.h"), "-include", str(HERE / "ref_launch.h"),
+               "-I", str(SIM), "-I", _cuda_include(), "-x", "c++", "-", "-o", str(so)]
+        r = subprocess.run(cmd, input=text, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference CPU build of {src} failed:\n{r.stderr[-4000:]}")
+    # The host wall-cell list builder is plain C++: compiled unmodified.
+    so = OUT / "libref_walllist.so"
+    libs["walllist"] = so
+    if force or not so.exists():
+        cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
+               str(SIM / "wall_model.cpp"), str(HERE / "ref_walllist_driver.cpp"),
+               "-I", str(SIM), "-I", _cuda_include(), "-o", str(so)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference wall_model.cpp build failed:\n{r.stderr[-4000:]}")
+    return libs
+
+
+if __name__ == "__main__":
+    for k, v in build(force="--force" in sys.argv).items():
+        print(k, v)

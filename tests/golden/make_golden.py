@@ -1,0 +1,281 @@
+"""Generate the golden vectors of the solver step from the reference itself.
+
+Runs the reference's own kernels, compiled for the CPU from the reference
+tree by ``oracle/ref_build.py`` (``oracle/_ref/``), on small seeded cases and
+stores inputs and outputs under ``tests/golden/*.npz``. It needs the
+reference tree (``FOILCFD_REFERENCE``, default /root/reference) and is run
+by hand in the build container; the fixtures it writes are committed, so
+the tests never need the reference at run time.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import ref_build  # noqa: E402
+from oracle.oracle import CX, CY, CZ, W, equilibrium  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+P = C.c_void_p
+I, F = C.c_int, C.c_float
+
+
+def p(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+def load():
+    libs = ref_build.build()
+    core = C.CDLL(str(libs["core"]))
+    core.ref_collide.argtypes = [I, I, I, P, P, P, F, F, F, F, I, P, P, P, P, P, P, P]
+    core.ref_force.argtypes = [I, I, I, P, P, P, P, P, P]
+    core.ref_init.argtypes = [I, I, I, P, P, F, F, C.c_uint, I]
+    wall = C.CDLL(str(libs["wall"]))
+    wall.ref_wall_update.argtypes = [I, I, I, P, I, P, P, P, P, P, P, P, P, P, P, P, F, F, F, P]
+    refine = C.CDLL(str(libs["refine"]))
+    refine.ref_fill.argtypes = [I, I, I, P, P, P, I, I, I, P, P, I, I, I, F, F, F, I]
+    refine.ref_restrict.argtypes = [I, I, I, P, P, I, I, I, P, P, I, I, I, I, I, F, F, P, P, P, P]
+    wl = C.CDLL(str(libs["walllist"]))
+    wl.ref_build_wall_list.argtypes = [I, I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P]
+    wl.ref_build_wall_list.restype = C.c_longlong
+    return core, wall, refine, wl
+
+
+def open_flags(nx, ny, nz):
+    """Inlet x=0, outlet x=nx-1, slip y faces (tests/lbm_test_util.h:34-54)."""
+    fl = np.zeros((nz, ny, nx), np.uint8)
+    fl[:, 0, :] = 5
+    fl[:, -1, :] = 4
+    fl[:, :, 0] = 2
+    fl[:, :, -1] = 3
+    return fl
+
+
+def perturbed_state(rng, n, u0=0.05, amp=0.01):
+    rho = 1 + amp * rng.standard_normal(n)
+    ux = u0 + amp * rng.standard_normal(n)
+    uy = amp * rng.standard_normal(n)
+    uz = amp * rng.standard_normal(n)
+    f = equilibrium(rho, ux, uy, uz, np.float64)
+    f *= 1 + 1e-3 * rng.standard_normal(f.size)
+    return f.astype(np.float32)
+
+
+def run_collide(core, dims, f, flags, steps, tau, lam, cs, u_in, slip=None):
+    n = int(np.prod(dims))
+    mac = [np.zeros(n, np.float32) for _ in range(4)]
+    sl = slip if slip is not None else [None] * 3
+    for s in range(steps):
+        dst = f.copy()
+        core.ref_collide(*dims, p(f), p(dst), p(flags), tau, lam, cs, u_in, int(s == steps - 1),
+                         *[p(m) for m in mac], *[p(x) for x in sl])
+        f = dst
+    return f, mac
+
+
+def case_collide(core, rng):
+    out = {}
+    dims = (24, 16, 8)
+    n = int(np.prod(dims))
+    fl = open_flags(24, 16, 8)
+    fl[:, 6:10, 8:12] = 1  # square cylinder
+    flags = fl.ravel().copy()
+    f0 = perturbed_state(rng, n)
+    params = dict(tau=0.52, lam=3.0 / 16.0, cs=0.1733, u_in=0.05)
+    f1, m1 = run_collide(core, dims, f0, flags, 1, **params)
+    f20, m20 = run_collide(core, dims, f0, flags, 20, **params)
+    slip = [(0.01 * rng.standard_normal(n)).astype(np.float16).view(np.uint16) for _ in range(3)]
+    f20w, m20w = run_collide(core, dims, f0, flags, 20, slip=slip, **params)
+    force = np.zeros(3, np.float32)
+    core.ref_force(*dims, p(f20), p(flags), None, None, None, p(force))
+    force_w = np.zeros(3, np.float32)
+    core.ref_force(*dims, p(f20w), p(flags), *[p(s) for s in slip], p(force_w))
+    # STL-mode spanwise slip walls.
+    fz = open_flags(24, 16, 8)
+    fz[0, 1:-1, 1:-1] = 6
+    fz[-1, 1:-1, 1:-1] = 7
+    fz[2:6, 6:10, 8:12] = 1
+    flags_z = fz.ravel().copy()
+    f20z, m20z = run_collide(core, dims, f0, flags_z, 20, **params)
+    out.update(dims=np.array(dims), flags=flags, flags_z=flags_z, f0=f0, f1=f1, f20=f20, f20w=f20w, f20z=f20z,
+               slip=np.stack(slip), force20=force, force20w=force_w,
+               m1=np.stack(m1), m20=np.stack(m20), m20w=np.stack(m20w), m20z=np.stack(m20z),
+               params=np.array([params["tau"], params["lam"], params["cs"], params["u_in"]], np.float32))
+    np.savez_compressed(OUT / "collide.npz", **out)
+
+
+def case_taylor_green(core):
+    """Open-domain Taylor-Green (M0 layout, tests/m0_taylor_green.cpp:25-80)
+    at 24x16x8, nu = 0.01 (tau 0.53), LES on, 1000 steps."""
+    dims = (24, 16, 8)
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    k = 2 * np.pi / np.array([nx, ny, nz], dtype=np.float64)
+    u = 0.05 * np.sin(k[0] * x) * np.cos(k[1] * y) * np.cos(k[2] * z)
+    v = -0.05 * np.cos(k[0] * x) * np.sin(k[1] * y) * np.cos(k[2] * z)
+    f0 = equilibrium(np.ones(n), u.ravel(), v.ravel(), np.zeros(n), np.float32)
+    flags = open_flags(*dims).ravel().copy()
+    f1000, m = run_collide(core, dims, f0, flags, 1000, tau=0.53, lam=3.0 / 16.0, cs=0.1733, u_in=1e-3)
+    np.savez_compressed(OUT / "taylor_green.npz", dims=np.array(dims), flags=flags, f0=f0, f1000=f1000,
+                        m1000=np.stack(m), params=np.array([0.53, 3.0 / 16.0, 0.1733, 1e-3], np.float32))
+
+
+def case_init(core):
+    dims = (24, 16, 8)
+    n = int(np.prod(dims))
+    fl = open_flags(*dims)
+    fl[:, 6:10, 8:12] = 1
+    flags = fl.ravel().copy()
+    f = np.zeros(19 * n, np.float32)
+    core.ref_init(*dims, p(f), p(flags), 0.08, 1e-3 * 0.08, 0x5EED, 1)
+    np.savez_compressed(OUT / "init.npz", dims=np.array(dims), flags=flags, f=f,
+                        params=np.array([0.08, 1e-3 * 0.08], np.float32))
+
+
+def plate_case(rng, dims, u_tau=0.004, nu=5e-4):
+    """Solid floor y < 4 with a planted Reichardt-like shear profile."""
+    nx, ny, nz = dims
+    fl = open_flags(nx, ny, nz)
+    fl[:, 1:4, 1:-1] = 1
+    flags = fl.ravel().copy()
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    yw = np.maximum(y - 3.5, 0.0)
+    yp = yw * u_tau / nu
+    uplus = np.log(1 + 0.41 * yp) / 0.41 + 7.8 * (1 - np.exp(-yp / 11) - yp / 11 * np.exp(-yp / 3))
+    u = np.where(fl == 1, 0.0, u_tau * uplus).ravel()
+    u = u + 0.002 * rng.standard_normal(u.size) * (u > 0)
+    w = 0.003 * np.sin(2 * np.pi * z / nz).ravel()
+    f = equilibrium(np.ones(u.size), u, np.zeros(u.size), w, np.float32)
+    return flags, f
+
+
+def case_wall(core, wall, wl, rng):
+    dims = (24, 16, 8)
+    n = int(np.prod(dims))
+    flags, f = plate_case(rng, dims)
+    cap = n
+    arr = dict(cell=np.zeros(cap, np.int64), sample=np.zeros(cap, np.int64), nx=np.zeros(cap, np.float32),
+               ny=np.zeros(cap, np.float32), nz=np.zeros(cap, np.float32), ys=np.zeros(cap, np.float32),
+               mask=np.zeros(cap, np.uint32))
+    stats = np.zeros(3, np.int32)
+    m = wl.ref_build_wall_list(*dims, p(flags), p(flags), 2, p(arr["cell"]), p(arr["sample"]), p(arr["nx"]),
+                               p(arr["ny"]), p(arr["nz"]), p(arr["ys"]), p(arr["mask"]), cap, p(stats))
+    arr = {k: v[:m].copy() for k, v in arr.items()}
+    utau = np.zeros(m, np.float32)
+    slip = [np.zeros(n, np.uint16) for _ in range(3)]
+    nu, cut = np.float32(5e-4), np.float32(1e-3 * 0.05)
+    hist_u, hist_s, hist_st = [], [], []
+    for it in range(3):
+        st = np.zeros(4, np.float32)
+        wall.ref_wall_update(*dims, p(f), m, p(arr["cell"]), p(arr["sample"]), p(arr["nx"]), p(arr["ny"]),
+                             p(arr["nz"]), p(arr["ys"]), p(arr["mask"]), p(utau), *[p(s) for s in slip], nu, cut,
+                             0.25, p(st))
+        hist_u.append(utau.copy())
+        hist_s.append(np.stack(slip).copy())
+        hist_st.append(st)
+    np.savez_compressed(OUT / "wall.npz", dims=np.array(dims), flags=flags, f=f, stats_build=stats,
+                        utau=np.stack(hist_u), slip=np.stack(hist_s), stats=np.stack(hist_st),
+                        params=np.array([nu, cut, 0.25], np.float32), **{"list_" + k: v for k, v in arr.items()})
+
+
+def wall_list_geometries():
+    geoms = {}
+    d = (32, 32, 8)
+    f = np.zeros(d[::-1], np.uint8)
+    f[:, :16, :] = 1
+    geoms["slab"] = (d, f.ravel().copy(), None)
+    d = (64, 64, 8)
+    z, y, x = np.meshgrid(*[np.arange(v) for v in d[::-1]], indexing="ij")
+    geoms["wedge"] = (d, np.where(x + y < 32, 1, 0).astype(np.uint8).ravel(), None)
+    d = (48, 48, 48)
+    z, y, x = np.meshgrid(*[np.arange(v) for v in d[::-1]], indexing="ij")
+    r = np.sqrt((x - 23.5) ** 2 + (y - 23.5) ** 2 + (z - 23.5) ** 2)
+    geoms["sphere"] = (d, np.where(r < 12.0, 1, 0).astype(np.uint8).ravel(), None)
+    # Foil + a "vane" solid only in the active field (VG exclusion).
+    d = (48, 32, 8)
+    z, y, x = np.meshgrid(*[np.arange(v) for v in d[::-1]], indexing="ij")
+    clean = np.where(((x - 24) / 14.0) ** 2 + ((y - 14) / 4.0) ** 2 < 1.0, 1, 0).astype(np.uint8)
+    active = clean.copy()
+    active[(x >= 28) & (x <= 29) & (y >= 18) & (y <= 21)] = 1
+    geoms["vane"] = (d, active.ravel().copy(), clean.ravel().copy())
+    return geoms
+
+
+def case_wall_list(wl):
+    out = {}
+    for name, (d, active, clean) in wall_list_geometries().items():
+        clean = active if clean is None else clean
+        n = int(np.prod(d))
+        for sample in (2, 3):
+            arr = dict(cell=np.zeros(n, np.int64), sample=np.zeros(n, np.int64), nx=np.zeros(n, np.float32),
+                       ny=np.zeros(n, np.float32), nz=np.zeros(n, np.float32), ys=np.zeros(n, np.float32),
+                       mask=np.zeros(n, np.uint32))
+            stats = np.zeros(3, np.int32)
+            m = wl.ref_build_wall_list(*d, p(active), p(clean), sample, p(arr["cell"]), p(arr["sample"]),
+                                       p(arr["nx"]), p(arr["ny"]), p(arr["nz"]), p(arr["ys"]), p(arr["mask"]), n,
+                                       p(stats))
+            for k, v in arr.items():
+                out[f"{name}_{sample}_{k}"] = v[:m].copy()
+            out[f"{name}_{sample}_stats"] = stats
+    np.savez_compressed(OUT / "wall_list.npz", **out)
+
+
+def case_refine(core, refine, rng):
+    cd = (32, 20, 4)
+    cn = int(np.prod(cd))
+    cfl = open_flags(*cd)
+    cflags = cfl.ravel().copy()
+    box = (8, 5, 24, 15)
+    m = 2
+    fd = (m * (box[2] - box[0]), m * (box[3] - box[1]), m * cd[2])
+    fn = int(np.prod(fd))
+    ffl = np.zeros(fd[::-1], np.uint8)
+    ffl[:, :2, :] = 8
+    ffl[:, -2:, :] = 8
+    ffl[:, :, :2] = 8
+    ffl[:, :, -2:] = 8
+    ffl[:, 8:12, 12:16] = 1  # a fine solid block (skipped children)
+    fflags = ffl.ravel().copy()
+    cT0 = perturbed_state(rng, cn)
+    cT1 = perturbed_state(rng, cn)
+    ff0 = perturbed_state(rng, fn)
+    tauC, tauF = np.float32(0.52), np.float32(2 * (0.52 - 0.5) + 0.5)
+    fill_shell = ff0.copy()
+    refine.ref_fill(*cd, p(cT0), p(cT1), p(cflags), *fd, p(fill_shell), p(fflags), box[0], box[1], m, 0.5, tauC,
+                    tauF, 0)
+    fill_full = ff0.copy()
+    refine.ref_fill(*cd, p(cT0), p(cT0), p(cflags), *fd, p(fill_full), p(fflags), box[0], box[1], m, 0.0, tauC,
+                    tauF, 1)
+    fc = cT1.copy()
+    mac = [np.zeros(cn, np.float32) for _ in range(4)]
+    refine.ref_restrict(*fd, p(ff0), p(fflags), *cd, p(fc), p(cflags), *box, m, tauC, tauF, *[p(x) for x in mac])
+    np.savez_compressed(OUT / "refine.npz", cdims=np.array(cd), fdims=np.array(fd), box=np.array(box),
+                        factor=np.array(m), cflags=cflags, fflags=fflags, cT0=cT0, cT1=cT1, ff0=ff0,
+                        fill_shell=fill_shell, fill_full=fill_full, restricted=fc, rmacro=np.stack(mac),
+                        taus=np.array([tauC, tauF], np.float32))
+
+
+def main():
+    core, wall, refine, wl = load()
+    rng = np.random.default_rng(20261203)
+    case_collide(core, rng)
+    case_taylor_green(core)
+    case_init(core)
+    case_wall(core, wall, wl, rng)
+    case_wall_list(wl)
+    case_refine(core, refine, rng)
+    for f in sorted(OUT.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()
