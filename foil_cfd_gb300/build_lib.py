@@ -24,6 +24,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+# Per-file extra flags: the FP32 reference-order kernels and the refinement
+# coupling must not contract multiply-adds (their rounding follows the
+# reference expression tree, so results are bit-identical to it).
+FILE_FLAGS = {"collide_f32.cu": ["--fmad=false"], "refine_kernels.cu": ["--fmad=false"]}
 
 
 def _cuda_home() -> Path:
@@ -46,6 +50,7 @@ def _sources():
 def _digest(files) -> str:
     h = hashlib.sha256()
     h.update(" ".join(NVCC_FLAGS + CXX_FLAGS).encode())
+    h.update(repr(sorted(FILE_FLAGS.items())).encode())
     for f in files:
         h.update(f.name.encode())
         h.update(f.read_bytes())
@@ -73,7 +78,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     jobs = []
     for src in cu:
         obj = BUILD / (src.stem + ".cu.o")
-        jobs.append([nvcc, *NVCC_FLAGS, *inc, "-c", str(src), "-o", str(obj)])
+        jobs.append([nvcc, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *inc, "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = BUILD / (src.stem + ".cpp.o")
         jobs.append(["g++", *CXX_FLAGS, *inc, "-c", str(src), "-o", str(obj)])

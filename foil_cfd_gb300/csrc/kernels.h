@@ -62,6 +62,17 @@ cudaError_t launch_store_to_f32(Storage s, const void* in, float* out,
                                 long long cells, cudaStream_t st);
 cudaError_t launch_fill(float* dst, long long n, float v, cudaStream_t st);
 
+// ---- FP32 reference-order kernels (collide_f32.cu, built with --fmad=false)
+cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint8_t* kind,
+                                   LevelDims d, const CollideParams& p, float* rho,
+                                   float* u, float* v, float* w, SlipField slip,
+                                   cudaStream_t st);
+cudaError_t launch_init_eq_f32(float* f, const std::uint8_t* kind, long long n, float uIn,
+                               cudaStream_t st);
+cudaError_t launch_init_macro_f32(float* f, const std::uint8_t* kind, long long n,
+                                  const float* rho, const float* u, const float* v,
+                                  const float* w, cudaStream_t st);
+
 // ---- force reduction (force_kernels.cu) ------------------------------------
 /// Momentum exchange over a compact wall-link list: entry i is fluid cell
 /// cells[i] with bit q of masks[i] set when the neighbour at +c_q is solid.

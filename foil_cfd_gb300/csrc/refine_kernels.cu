@@ -19,6 +19,10 @@
 // 3-cell edge ramp. The reference recomputes each neighbour's child average
 // inside the filter (19 averages per cell); here pass 1 stores every child
 // average once in scratch and pass 2 filters from scratch.
+//
+// Built with --fmad=false: every expression keeps the reference's rounding,
+// so fill and restriction are bit-identical to the reference kernels (the
+// limiter's 1/sqrt is evaluated as IEEE operations).
 #include "d3q19.cuh"
 #include "kernels.h"
 
@@ -69,7 +73,7 @@ __device__ __forceinline__ void limited_moments(const float (&fi)[kQ], float& rh
     ux = jx * inv; uy = jy * inv; uz = jz * inv;
     const float u2 = ux * ux + uy * uy + uz * uz;
     if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
-        const float sc = kMaxSimSpeed * rsqrtf(u2);
+        const float sc = kMaxSimSpeed * (1.0f / sqrtf(u2));
         ux *= sc; uy *= sc; uz *= sc;
     }
     rho = r;

@@ -389,14 +389,14 @@ cudaError_t launch_collide(Storage s, const void* src, void* dst, const std::uin
     a.writeMacro = (p.writeMacro && rho && u && v && w) ? 1 : 0;
     a.rho = rho; a.u = u; a.v = v; a.w = w;
     a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
-    const bool wm = slip.active();
-    if (s == Storage::F32) {
-        if (wm) collide_dispatch<StoreF32, true>(src, dst, kind, d, a, st);
-        else collide_dispatch<StoreF32, false>(src, dst, kind, d, a, st);
-    } else {
-        if (wm) collide_dispatch<StoreF16, true>(src, dst, kind, d, a, st);
-        else collide_dispatch<StoreF16, false>(src, dst, kind, d, a, st);
-    }
+    // FP32 storage runs the reference-order kernel (bit-identical to the
+    // reference step without FMA contraction); FP16 storage runs the
+    // re-associated pair-sum kernel above.
+    if (s == Storage::F32)
+        return launch_collide_f32_ref(static_cast<const float*>(src), static_cast<float*>(dst), kind, d, p,
+                                      rho, u, v, w, slip, st);
+    if (slip.active()) collide_dispatch<StoreF16, true>(src, dst, kind, d, a, st);
+    else collide_dispatch<StoreF16, false>(src, dst, kind, d, a, st);
     return cudaGetLastError();
 }
 
@@ -405,7 +405,7 @@ cudaError_t launch_init_equilibrium(Storage s, void* f, const std::uint8_t* kind
     const long long n = d.cells();
     if (!f || !kind || n <= 0) return cudaErrorInvalidValue;
     if (s == Storage::F32)
-        init_eq_kernel<StoreF32><<<blocks_for(n), kBlock1D, 0, st>>>(static_cast<float*>(f), kind, n, uInlet);
+        return launch_init_eq_f32(static_cast<float*>(f), kind, n, uInlet, st);
     else
         init_eq_kernel<StoreF16><<<blocks_for(n), kBlock1D, 0, st>>>(static_cast<__half*>(f), kind, n, uInlet);
     return cudaGetLastError();
@@ -437,7 +437,7 @@ cudaError_t launch_init_from_macro(Storage s, void* f, const std::uint8_t* kind,
     const long long n = d.cells();
     if (!f || !kind || n <= 0 || !rho || !u || !v || !w) return cudaErrorInvalidValue;
     if (s == Storage::F32)
-        init_macro_kernel<StoreF32><<<blocks_for(n), kBlock1D, 0, st>>>(static_cast<float*>(f), kind, n, rho, u, v, w);
+        return launch_init_macro_f32(static_cast<float*>(f), kind, n, rho, u, v, w, st);
     else
         init_macro_kernel<StoreF16><<<blocks_for(n), kBlock1D, 0, st>>>(static_cast<__half*>(f), kind, n, rho, u, v, w);
     return cudaGetLastError();

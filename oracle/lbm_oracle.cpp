@@ -646,7 +646,11 @@ void* oracle_tunnel_create(int nx, int ny, int nz, const uint8_t* flags, const f
     const long long n = t->cd.n();
     t->cflags.assign(flags, flags + n);
     t->fc[0].assign(f0, f0 + 19 * n);
-    t->fc[1] = t->fc[0];
+    // The other buffer holds the solver's reset state (equilibrium at u plus
+    // the speck), as after LBMSolver::reset with the ramps off.
+    t->fc[1].assign(19 * n, 0.0f);
+    oracle_init_eq(nx, ny, nz, t->fc[1].data(), flags, u);
+    oracle_speck(nx, ny, nz, t->fc[1].data(), flags, 1e-3f * u, 0x5eedu);
     t->tau = tau; t->u = u; t->smag = smagPre; t->lambda = lambda;
     t->mr.resize(n); t->mu.resize(n); t->mv.resize(n); t->mw.resize(n);
     return t;

@@ -92,12 +92,18 @@ def smag_prefactor(cs: float) -> float:
     return float(np.float32(18.0) * np.float32(1.41421356) * np.float32(cs) * np.float32(cs))
 
 
-def collide(dims, src, flags, tau, lam, smag_pre, u_in, write_macro=False, slip=None):
-    """One reference stream-collide over the whole grid; returns (dst, macro)."""
+def collide(dims, src, flags, tau, lam, smag_pre, u_in, write_macro=False, slip=None, dst=None):
+    """One reference stream-collide over the whole grid; returns (dst, macro).
+
+    ``dst`` is the other buffer of an A/B pair and is written in place; the
+    cells a step does not write (solid, slip, interface) keep its previous
+    contents, exactly as in the solver's ping-pong buffers. Without ``dst`` a
+    copy of ``src`` stands in for it."""
     nx, ny, nz = dims
     n = nx * ny * nz
     dtype = src.dtype
-    dst = src.copy()  # cells the step does not write keep their values
+    if dst is None:
+        dst = src.copy()
     macro = [np.zeros(n, dtype) for _ in range(4)] if write_macro else [None] * 4
     sx = [None] * 3 if slip is None else [np.ascontiguousarray(s) for s in slip]
     fn = lib().oracle_collide_f32 if dtype == np.float32 else lib().oracle_collide_f64
@@ -124,6 +130,14 @@ def init_equilibrium(dims, flags, u_in):
 def speck(dims, f, flags, amp, seed=0x5EED):
     lib().oracle_speck(*dims, _p(f), _p(flags), amp, seed)
     return f
+
+
+def reset_state(dims, flags, u_lat):
+    """LBMSolver::reset with the ramps off (lbm_solver.cpp:893-944):
+    equilibrium at (1, u_lat) -- solids at rest -- plus the speck of
+    amplitude 1e-3 u_lat, seed 0x5eed."""
+    f = init_equilibrium(dims, flags, np.float32(u_lat))
+    return speck(dims, f, flags, np.float32(1e-3) * np.float32(u_lat))
 
 
 def f2h(x: float) -> int:
@@ -212,7 +226,10 @@ class OracleSolver:
         self.tau, self.u_lat, self.lam = tau, u_lat, lam
         self.smag = smag_prefactor(cs)
         self.dtype = dtype
-        self.f = init_equilibrium(self.dims, self.flags, u_lat).astype(dtype)
+        # Both A/B buffers start from the solver's reset state (ramps off):
+        # equilibrium at u_lat plus the spanwise speck.
+        self.f = reset_state(self.dims, self.flags, u_lat).astype(dtype)
+        self.g = self.f.copy()
         self.macro = None
         self.fine = None
         self.wall = None
@@ -221,6 +238,7 @@ class OracleSolver:
         self.steps = 0
 
     def set_state(self, f):
+        """Import into the current buffer only (the solver's import path)."""
         self.f = np.ascontiguousarray(f, self.dtype).copy()
 
     def enable_wall_model(self, wl: WallList):
@@ -236,24 +254,26 @@ class OracleSolver:
         fine = self.fine
         fill_c2f(self.dims, self.f, self.f, self.flags, fd, fine["f"], fine["flags"], box, factor, 0.0,
                  np.float32(tf) / (np.float32(factor) * np.float32(tc)), True)
+        fine["g"] = fine["f"].copy()
 
     def step_n(self, n):
         tau = np.float32(self.tau)
         for i in range(n):
             wm = i == n - 1
             dst, macro = collide(self.dims, self.f, self.flags, tau, self.lam, self.smag, self.u_lat, wm,
-                                 self.slip)
+                                 self.slip, dst=self.g)
             if self.fine is not None:
                 fd, m, box = self.fine["dims"], self.fine["m"], self.fine["box"]
                 tf = np.float32(m) * (tau - np.float32(0.5)) + np.float32(0.5)
                 for k in range(m):
                     fill_c2f(self.dims, self.f, dst, self.flags, fd, self.fine["f"], self.fine["flags"], box, m,
                              np.float32(k) / np.float32(m), tf / (np.float32(m) * tau), False)
-                    self.fine["f"], _ = collide(fd, self.fine["f"], self.fine["flags"], tf, self.lam, self.smag,
-                                                self.u_lat, False, None)
+                    nf, _ = collide(fd, self.fine["f"], self.fine["flags"], tf, self.lam, self.smag,
+                                    self.u_lat, False, None, dst=self.fine["g"])
+                    self.fine["g"], self.fine["f"] = self.fine["f"], nf
                 restrict_f2c(fd, self.fine["f"], self.fine["flags"], self.dims, dst, self.flags, box, m,
                              (np.float32(m) * tau) / tf, macro)
-            self.f = dst
+            self.g, self.f = self.f, dst
             if macro is not None:
                 self.macro = macro
             self.steps += 1

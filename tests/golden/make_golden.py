@@ -69,15 +69,28 @@ def perturbed_state(rng, n, u0=0.05, amp=0.01):
     return f.astype(np.float32)
 
 
+def reset_state(core, dims, flags, u):
+    """The reference solver's buffers after reset() with the ramps off:
+    equilibrium at u plus the speck (1e-3 u, seed 0x5eed)."""
+    f = np.zeros(19 * int(np.prod(dims)), np.float32)
+    core.ref_init(*dims, p(f), p(flags), u, np.float32(1e-3) * np.float32(u), 0x5EED, 1)
+    return f
+
+
 def run_collide(core, dims, f, flags, steps, tau, lam, cs, u_in, slip=None):
+    """`steps` steps on an A/B buffer pair: A = the uploaded state, B = the
+    reset state (uploadF writes the current buffer only), so cells a step
+    never writes carry the same contents the reference solver would have."""
     n = int(np.prod(dims))
     mac = [np.zeros(n, np.float32) for _ in range(4)]
     sl = slip if slip is not None else [None] * 3
+    f = f.copy()
+    other = reset_state(core, dims, flags, u_in)
     for s in range(steps):
-        dst = f.copy()
+        dst = other
         core.ref_collide(*dims, p(f), p(dst), p(flags), tau, lam, cs, u_in, int(s == steps - 1),
                          *[p(m) for m in mac], *[p(x) for x in sl])
-        f = dst
+        f, other = dst, f
     return f, mac
 
 

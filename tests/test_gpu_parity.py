@@ -1,8 +1,15 @@
 """Parity of the CUDA solver step (through the C ABI) with the reference:
 the golden vectors the reference's own kernels produced, and the oracle
-(CPU restatement) on the same inputs. Tolerances are stated per test; the
-bar for the plain FP32 step is <= 1e-6 relative in rho and u (max-norm,
-normalised by the field's max) after 1000 steps."""
+(CPU restatement) on the same inputs.
+
+The FP32 collide and the refinement coupling evaluate the reference's
+expression tree without FMA contraction, so their populations must be
+bit-identical to the reference (golden) and the oracle: the tests assert
+exact equality on every cell a step writes, and also report the north-star
+metric (<= 1e-6 relative in rho and u, max-norm normalised by the field's
+max, after 1000 steps). The wall model (fast __logf/__expf on the device),
+the FP64 force sums (summation order) and FP16 storage carry the tolerances
+stated in their tests."""
 import numpy as np
 import pytest
 
@@ -74,11 +81,11 @@ def test_collide_vs_reference_golden(fc, golden, case, steps, flags_key, slip):
     f = s.export_f32()
     m = written_mask(flags)
     ref = g[case]
-    assert np.abs(f.reshape(19, -1)[:, m] - ref.reshape(19, -1)[:, m]).max() <= 2e-6
+    assert np.array_equal(f.reshape(19, -1)[:, m], ref.reshape(19, -1)[:, m])
     assert_rho_u(f, ref, flags)
     macro = np.stack(s.download_macro())
     mk = {"f1": "m1", "f20": "m20", "f20w": "m20w", "f20z": "m20z"}[case]
-    assert np.abs(macro[:, m] - g[mk][:, m]).max() <= 2e-6
+    assert np.array_equal(macro[:, m], g[mk][:, m])
 
 
 def test_taylor_green_1000_steps_vs_reference(fc, golden):
@@ -89,8 +96,11 @@ def test_taylor_green_1000_steps_vs_reference(fc, golden):
     s = make(fc, dims, g["flags"], tau, u_in, cs)
     s.import_f32(g["f0"])
     assert s.step_n(1000) == 0
-    er, eu = assert_rho_u(s.export_f32(), g["f1000"], g["flags"])
-    print(f"TG 1000 steps vs reference: rho {er:.2e} u {eu:.2e}")
+    f = s.export_f32()
+    er, eu = assert_rho_u(f, g["f1000"], g["flags"])
+    m = written_mask(g["flags"])
+    assert np.array_equal(f.reshape(19, -1)[:, m], g["f1000"].reshape(19, -1)[:, m])
+    print(f"TG 1000 steps vs reference: rho {er:.2e} u {eu:.2e} (bit-identical)")
 
 
 def test_cylinder_1000_steps_vs_oracle(fc, oracle_mod):
@@ -116,8 +126,11 @@ def test_cylinder_1000_steps_vs_oracle(fc, oracle_mod):
     for batch in range(10):
         assert s.step_n(100) == 0
         o.step_n(100)
-    er, eu = assert_rho_u(s.export_f32(), o.f, flags)
-    print(f"cylinder 1000 steps vs oracle: rho {er:.2e} u {eu:.2e}")
+    f = s.export_f32()
+    er, eu = assert_rho_u(f, o.f, flags)
+    m = written_mask(flags)
+    assert np.array_equal(f.reshape(19, -1)[:, m], o.f.reshape(19, -1)[:, m])
+    print(f"cylinder 1000 steps vs oracle: rho {er:.2e} u {eu:.2e} (bit-identical)")
     fg = s.force_raw()
     assert np.allclose(fg, o.last_force, rtol=1e-5, atol=1e-6 * np.abs(o.last_force).max())
 
@@ -145,7 +158,7 @@ def test_periodic_taylor_green_decay(fc, oracle_mod):
     o = oracle_mod.OracleSolver(dims, flags, np.float32(0.53), np.float32(0.0), cs=0.0)
     o.set_state(f0)
     o.step_n(1000)
-    assert_rho_u(s.export_f32(), o.f, flags)
+    assert np.array_equal(s.export_f32(), o.f)
     t = np.arange(1, 11) * 100.0
     rate = -np.polyfit(t, np.log(ke), 1)[0]
     nu = 0.01
@@ -205,7 +218,7 @@ def test_refinement_seed_fill_vs_reference(fc, golden):
     assert info.active == 1 and (info.fine_dims.nx, info.fine_dims.ny, info.fine_dims.nz) == fd
     ff = s.export_fine_f32().reshape(19, -1)
     keep = g["fflags"] != 1
-    assert np.abs(ff[:, keep] - g["fill_full"].reshape(19, -1)[:, keep]).max() <= 2e-6
+    assert np.array_equal(ff[:, keep], g["fill_full"].reshape(19, -1)[:, keep])
 
 
 def test_refined_step_vs_oracle(fc, golden, oracle_mod):
@@ -221,17 +234,15 @@ def test_refined_step_vs_oracle(fc, golden, oracle_mod):
     o = oracle_mod.OracleSolver(cd, g["cflags"], np.float32(tauC), np.float32(0.05))
     o.set_state(g["cT0"])
     o.enable_refinement(box, m, g["fflags"])
-    assert np.abs(s.export_fine_f32() - o.fine["f"]).max() <= 2e-6
+    keep = g["fflags"] != 1
+    assert np.array_equal(s.export_fine_f32().reshape(19, -1)[:, keep], o.fine["f"].reshape(19, -1)[:, keep])
     for _ in range(4):
         assert s.step_n(5) == 0
         o.step_n(5)
-    assert_rho_u(s.export_f32(), o.f, g["cflags"], tol=2e-6)
-    ffl = g["fflags"]
-    r1, u1 = moments(s.export_fine_f32(), ffl.size)
-    r2, u2 = moments(o.fine["f"], ffl.size)
-    mask = ffl == 0
-    assert rel_err(r1, r2, mask) <= 2e-6
-    assert np.abs(u1[:, mask] - u2[:, mask]).max() <= 2e-6 * np.abs(u2[:, mask]).max()
+    m = written_mask(g["cflags"])
+    assert np.array_equal(s.export_f32().reshape(19, -1)[:, m], o.f.reshape(19, -1)[:, m])
+    fm = g["fflags"] == 0
+    assert np.array_equal(s.export_fine_f32().reshape(19, -1)[:, fm], o.fine["f"].reshape(19, -1)[:, fm])
 
 
 def test_fp16_storage_taylor_green_error(fc, oracle_mod):

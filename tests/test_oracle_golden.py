@@ -9,10 +9,13 @@ from conftest import rel_err, written_mask
 
 
 def _collide_n(o, dims, f, flags, steps, p, slip=None):
+    """A/B stepping: the other buffer starts from the solver's reset state."""
     tau, lam, cs, u_in = (np.float32(x) for x in p)
     macro = None
+    other = o.reset_state(dims, flags, u_in)
     for s in range(steps):
-        f, m = o.collide(dims, f, flags, tau, lam, o.smag_prefactor(cs), u_in, s == steps - 1, slip)
+        dst, m = o.collide(dims, f, flags, tau, lam, o.smag_prefactor(cs), u_in, s == steps - 1, slip, dst=other)
+        f, other = dst, f
         macro = m if m is not None else macro
     return f, macro
 
