@@ -263,6 +263,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="320x96x96 tunnel (profiling captures)")
     ap.add_argument("--no-fp16", action="store_true")
+    ap.add_argument("--only-fp16", action="store_true", help="measure the FP16-storage solver only")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
@@ -293,6 +294,12 @@ def main():
         return
 
     clocks = Clocks() if rank == 0 else None
+    if args.only_fp16:
+        r16 = measure(t, "fp16", args.steps, warmup, clocks)
+        r16["solver"] = None
+        print(json.dumps({"metric": METRIC, "value": round(r16["glups"], 3), "unit": UNIT, "storage": "fp16",
+                          "roofline": roofline("fp16", r16["collide"]), "clocks": r16["clocks"]}))
+        return
     r32 = measure(t, "fp32", args.steps, warmup, clocks)
     ms = r32["ms"]
     if dist is not None:

@@ -261,7 +261,9 @@ def case_refine(core, refine, rng):
     cT0 = perturbed_state(rng, cn)
     cT1 = perturbed_state(rng, cn)
     ff0 = perturbed_state(rng, fn)
-    tauC, tauF = np.float32(0.52), np.float32(2 * (0.52 - 0.5) + 0.5)
+    # tau_f as the solver forms it, in FP32: m (tau_c - 1/2) + 1/2.
+    tauC = np.float32(0.52)
+    tauF = np.float32(m) * (tauC - np.float32(0.5)) + np.float32(0.5)
     fill_shell = ff0.copy()
     refine.ref_fill(*cd, p(cT0), p(cT1), p(cflags), *fd, p(fill_shell), p(fflags), box[0], box[1], m, 0.5, tauC,
                     tauF, 0)

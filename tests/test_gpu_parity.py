@@ -135,35 +135,68 @@ def test_cylinder_1000_steps_vs_oracle(fc, oracle_mod):
     assert np.allclose(fg, o.last_force, rtol=1e-5, atol=1e-6 * np.abs(o.last_force).max())
 
 
-def test_periodic_taylor_green_decay(fc, oracle_mod):
-    """Fully periodic TG (new behaviour: the reference cannot wrap x/y), 64^3,
-    nu 0.01, no LES: GPU vs FP32 oracle, and the decay rate vs the analytic
-    exp(-2 nu k^2 t) with k^2 = 3 (2 pi / 64)^2."""
-    N = 64
-    dims = (N, N, N)
+def _tg_field(oracle_mod, N, u0):
     n = N ** 3
     z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
     k = 2 * np.pi / N
-    u = 0.05 * np.sin(k * x) * np.cos(k * y) * np.cos(k * z)
-    v = -0.05 * np.cos(k * x) * np.sin(k * y) * np.cos(k * z)
-    f0 = oracle_mod.equilibrium(np.ones(n), u.ravel(), v.ravel(), np.zeros(n))
+    u = u0 * np.sin(k * x) * np.cos(k * y) * np.cos(k * z)
+    v = -u0 * np.cos(k * x) * np.sin(k * y) * np.cos(k * z)
+    return oracle_mod.equilibrium(np.ones(n), u.ravel(), v.ravel(), np.zeros(n)), k
+
+
+def _ke(f, n):
+    r, uu = moments(f, n)
+    return 0.5 * np.sum(r * (uu ** 2).sum(0))
+
+
+def test_periodic_taylor_green_decay(fc, oracle_mod):
+    """Fully periodic 64^3 Taylor-Green, nu 0.01, no LES (the reference cannot
+    wrap x/y; this is new behaviour). u0 = 0.05: the GPU is bit-identical to
+    the FP32 oracle and its KE decay rate matches the FP64 oracle to 1e-5;
+    at that amplitude (Re ~ 50) nonlinear transfer speeds the decay well past
+    the linear exp(-2 nu k^2 t), so the analytic rate is checked at u0 = 0.002
+    (within 1 %)."""
+    N = 64
+    n = N ** 3
+    dims = (N, N, N)
     flags = np.zeros(n, np.uint8)
+    f0, k = _tg_field(oracle_mod, N, 0.05)
     s = make(fc, dims, flags, 0.53, 0.0, cs=-1.0)
     s.import_f32(f0)
     ke = []
     for b in range(10):
         assert s.step_n(100) == 0
-        r, uu = moments(s.export_f32(), n)
-        ke.append(0.5 * np.sum(r * (uu ** 2).sum(0)))
+        ke.append(_ke(s.export_f32(), n))
     o = oracle_mod.OracleSolver(dims, flags, np.float32(0.53), np.float32(0.0), cs=0.0)
     o.set_state(f0)
     o.step_n(1000)
     assert np.array_equal(s.export_f32(), o.f)
+    f64 = f0.astype(np.float64)
+    g64 = f64.copy()
+    ke64 = []
+    for b in range(10):
+        for _ in range(100):
+            d, _m = oracle_mod.collide(dims, f64, flags, 0.53, 3.0 / 16.0, 0.0, 0.0, dst=g64)
+            f64, g64 = d, f64
+        ke64.append(_ke(f64, n))
     t = np.arange(1, 11) * 100.0
     rate = -np.polyfit(t, np.log(ke), 1)[0]
-    nu = 0.01
-    analytic = 2 * nu * 3 * k * k
-    assert abs(rate / analytic - 1) < 0.02, (rate, analytic)
+    rate64 = -np.polyfit(t, np.log(ke64), 1)[0]
+    analytic = 2 * 0.01 * 3 * k * k
+    print(f"TG u0=0.05: GPU FP32 rate {rate:.6e}, FP64 {rate64:.6e} ({(rate / rate64 - 1):.2e}), "
+          f"linear analytic {analytic:.6e}")
+    assert abs(rate / rate64 - 1) < 1e-5
+    # Linear regime: the analytic decay.
+    f0s, _ = _tg_field(oracle_mod, N, 0.002)
+    s2 = make(fc, dims, flags, 0.53, 0.0, cs=-1.0)
+    s2.import_f32(f0s)
+    kes = []
+    for b in range(10):
+        assert s2.step_n(100) == 0
+        kes.append(_ke(s2.export_f32(), n))
+    rate_s = -np.polyfit(t, np.log(kes), 1)[0]
+    print(f"TG u0=0.002: GPU rate {rate_s:.6e} vs analytic {analytic:.6e} ({(rate_s / analytic - 1):.2e})")
+    assert abs(rate_s / analytic - 1) < 0.01
 
 
 def test_force_vs_oracle_and_reference(fc, golden, oracle_mod):
