@@ -62,12 +62,6 @@ cudaError_t launch_store_to_f32(Storage s, const void* in, float* out,
                                 long long cells, cudaStream_t st);
 cudaError_t launch_fill(float* dst, long long n, float v, cudaStream_t st);
 
-// ---- two-cells-per-thread collide on packed FP32 (collide_pair.cu) --------
-bool pair_kernel_applies(LevelDims d);
-cudaError_t launch_collide_pair(Storage s, const void* src, void* dst, const std::uint8_t* kind,
-                                LevelDims d, const CollideParams& p, float* rho, float* u,
-                                float* v, float* w, SlipField slip, cudaStream_t st);
-
 // ---- FP32 reference-order kernels (collide_f32.cu, built with --fmad=false)
 cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint8_t* kind,
                                    LevelDims d, const CollideParams& p, float* rho,

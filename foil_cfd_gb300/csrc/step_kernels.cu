@@ -389,12 +389,9 @@ cudaError_t launch_collide(Storage s, const void* src, void* dst, const std::uin
     a.writeMacro = (p.writeMacro && rho && u && v && w) ? 1 : 0;
     a.rho = rho; a.u = u; a.v = v; a.w = w;
     a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
-    // Even nx: the two-cells-per-thread packed-FP32 kernel (reference order
-    // for FP32 storage, pair-sum order for FP16). Odd nx: the one-cell
-    // kernels -- FP32 storage in the reference order (bit-identical to the
-    // reference step without FMA contraction), FP16 in the pair-sum order.
-    if (pair_kernel_applies(d))
-        return launch_collide_pair(s, src, dst, kind, d, p, rho, u, v, w, slip, st);
+    // FP32 storage runs the reference-order kernel (bit-identical to the
+    // reference step without FMA contraction); FP16 storage runs the
+    // re-associated pair-sum kernel above.
     if (s == Storage::F32)
         return launch_collide_f32_ref(static_cast<const float*>(src), static_cast<float*>(dst), kind, d, p,
                                       rho, u, v, w, slip, st);
