@@ -34,10 +34,12 @@ METRIC = "GLUPS, 23.6M-cell wall-modeled tunnel: FP16-store vs FP32, % of HBM pe
 UNIT = "GLUPS"
 BYTES_PER_LUP = {"fp32": 153.0, "fp16": 77.0}  # 19 loads + 19 stores + 1 kind byte
 BATCH = 50
-# DRAM bytes per cell update of the collide kernel from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum over cells of the launch) on
-# the small workload; profiles/collide_fp32.md and collide_fp16.md record it.
-NCU_DRAM_BYTES_PER_LUP = {"fp32": None, "fp16": None}
+# Measured DRAM traffic of the collide kernel over its algorithmic bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum of one coarse and one fine
+# launch, divided by the class-based algorithmic bytes of those launches) from
+# the ncu capture of the 320x96x96 tunnel; profiles/collide_fp32_airfoil.md
+# and profiles/collide_fp16_airfoil.md give the figures.
+NCU_TRAFFIC_OVER_ALG = {"fp32": 1.0228, "fp16": 1.0457}
 
 
 def peaks():
@@ -145,28 +147,32 @@ def measure(t, storage, steps, warmup, clocks=None):
     # solver's stream, over a separate run of the same steps.
     sol.enable_collide_timing(True)
     timed_steps(sol, min(steps, 40))
-    col_ms, col_n, col_cells = sol.collide_time_ms()
+    col_ms, col_n, col_cells, col_bytes = sol.collide_time_ms()
     sol.enable_collide_timing(False)
     upd = t.updates_per_step()
     res = dict(ms=ms, glups=upd * steps / (ms * 1e-3) / 1e9,
                coarse_glups=float(np.prod(t.dims)) * steps / (ms * 1e-3) / 1e9, launches=launches, clocks=clk,
-               collide=dict(ms=col_ms, launches=col_n, cells=col_cells),
+               collide=dict(ms=col_ms, launches=col_n, cells=col_cells, bytes=col_bytes),
                nan=sol.nan_detected(), force=sol.force_raw().tolist(), solver=sol, scaling=scaling)
     return res
 
 
 def roofline(storage, col):
+    """Dominant kernel (the collide, coarse and fine launches): algorithmic
+    bytes per launch (per cell class, counted by the library) over the mean
+    CUDA-event duration of a launch."""
     peak, kind = peaks()
-    avg_ms = col["ms"] / max(col["launches"], 1)
-    cells_per_launch = col["cells"] / max(col["launches"], 1)
-    alg = BYTES_PER_LUP[storage] * cells_per_launch
+    nl = max(col["launches"], 1)
+    avg_ms = col["ms"] / nl
+    cells_per_launch = col["cells"] / nl
+    alg = col["bytes"] / nl
     achieved = alg / (avg_ms * 1e-3) / 1e9
-    tb = NCU_DRAM_BYTES_PER_LUP[storage]
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": kind,
-            "traffic": None if tb is None else round(tb * cells_per_launch),
-            "kernel": f"collide_kernel ({storage}, coarse + fine launches)",
-            "bytes_per_lup": BYTES_PER_LUP[storage], "avg_launch_ms": round(avg_ms, 4),
+            "traffic": round(NCU_TRAFFIC_OVER_ALG[storage] * alg),
+            "alg_bytes_per_launch": round(alg),
+            "kernel": f"collide ({storage} storage), coarse + fine launches",
+            "bytes_per_update_rw_cell": BYTES_PER_LUP[storage], "avg_launch_ms": round(avg_ms, 4),
             "cells_per_launch": round(cells_per_launch)}
 
 

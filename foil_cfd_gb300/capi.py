@@ -110,7 +110,7 @@ _SIGS = {
     "fcfd_derive_patch_box": (PatchBox, [C.POINTER(Dims), P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "fcfd_kernel_launches": (C.c_longlong, [P]),
     "fcfd_enable_collide_timing": (C.c_int, [P, C.c_int]),
-    "fcfd_collide_time_ms": (C.c_int, [P, P, P, P]),
+    "fcfd_collide_time_ms": (C.c_int, [P, P, P, P, P]),
     "fcfd_timer_start": (C.c_int, [P]),
     "fcfd_timer_stop": (C.c_int, [P, P]),
     "fcfd_host_alloc": (P, [C.c_size_t]),

@@ -85,6 +85,17 @@ struct Level {
     int linkCount = 0;
     double* dPartials = nullptr;
     WMLevel wm;
+    // Cell classes of the level for the collide's algorithmic byte count:
+    // cells the step reads and writes (fluid, outlets), inlet cells (write
+    // only) and cells it leaves untouched (solid, slip, interface; the kind
+    // byte is still read).
+    long long nReadWrite = 0, nInlet = 0, nUntouched = 0;
+
+    double collideBytes(Storage s) const {
+        const double pop = s == Storage::F32 ? 4.0 : 2.0;
+        return static_cast<double>(nReadWrite) * (2.0 * 19.0 * pop + 1.0)
+             + static_cast<double>(nInlet) * (19.0 * pop + 1.0) + static_cast<double>(nUntouched);
+    }
 
     void free_all() {
         dfree(f[0]); dfree(f[1]); dfree(flags); dfree(kind);
@@ -164,7 +175,7 @@ struct fcfd_solver {
     long long launches = 0;
     bool collideTiming = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> colEv;
-    std::vector<double> colCells;
+    std::vector<double> colCells, colBytes;
     size_t colEvUsed = 0;
     cudaEvent_t tmr0 = nullptr, tmr1 = nullptr;
 
@@ -234,6 +245,13 @@ struct fcfd_solver {
 
     cudaError_t uploadLevelFlags(Level& L, const std::uint8_t* flags) {
         L.hostFlags.assign(flags, flags + L.n);
+        L.nReadWrite = L.nInlet = L.nUntouched = 0;
+        for (long long i = 0; i < L.n; ++i) {
+            const std::uint8_t f = flags[i];
+            if (f == FCFD_FLAG_FLUID || f == FCFD_FLAG_OUTLET || f == FCFD_FLAG_OUTLET_EQ) ++L.nReadWrite;
+            else if (f == FCFD_FLAG_INLET) ++L.nInlet;
+            else ++L.nUntouched;
+        }
         if (auto e = cudaMemcpyAsync(L.flags, flags, static_cast<size_t>(L.n), cudaMemcpyHostToDevice, stream);
             e != cudaSuccess)
             return e;
@@ -367,6 +385,7 @@ struct fcfd_solver {
         for (auto& pr : colEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
         colEv.clear();
         colCells.clear();
+        colBytes.clear();
         for (cudaEvent_t* e : {&tmr0, &tmr1})
             if (*e) { cudaEventDestroy(*e); *e = nullptr; }
         colEvUsed = 0;
@@ -385,10 +404,12 @@ struct fcfd_solver {
                 cudaEventCreate(&b);
                 colEv.emplace_back(a, b);
                 colCells.push_back(0.0);
+                colBytes.push_back(0.0);
             }
             e1 = colEv[colEvUsed].first;
             e2 = colEv[colEvUsed].second;
             colCells[colEvUsed] = static_cast<double>(L.n);
+            colBytes[colEvUsed] = L.collideBytes(storage);
             ++colEvUsed;
             cudaEventRecord(e1, stream);
         }
@@ -1192,18 +1213,21 @@ int fcfd_enable_collide_timing(fcfd_solver* s, int enabled) {
     return 0;
 }
 
-int fcfd_collide_time_ms(fcfd_solver* s, double* total, long long* count, double* cells) {
+int fcfd_collide_time_ms(fcfd_solver* s, double* total, long long* count, double* cells,
+                         double* alg_bytes) {
     if (!s || !total || !count) return cudaErrorInvalidValue;
     if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return e;
-    double t = 0.0, c = 0.0;
+    double t = 0.0, c = 0.0, b = 0.0;
     for (size_t i = 0; i < s->colEvUsed; ++i) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, s->colEv[i].first, s->colEv[i].second) == cudaSuccess) t += ms;
         c += s->colCells[i];
+        b += s->colBytes[i];
     }
     *total = t;
     *count = static_cast<long long>(s->colEvUsed);
     if (cells) *cells = c;
+    if (alg_bytes) *alg_bytes = b;
     s->colEvUsed = 0;
     return 0;
 }

@@ -301,12 +301,14 @@ class LBMSolver:
         self._lib.fcfd_enable_collide_timing(self._h, int(enabled))
 
     def collide_time_ms(self):
-        """(total ms, launches, cells updated) of the timed collide launches."""
+        """(total ms, launches, cells, algorithmic bytes) of the timed
+        collide launches since the last call."""
         t = C.c_double()
         n = C.c_longlong()
         c = C.c_double()
-        self._lib.fcfd_collide_time_ms(self._h, C.byref(t), C.byref(n), C.byref(c))
-        return t.value, n.value, c.value
+        b = C.c_double()
+        self._lib.fcfd_collide_time_ms(self._h, C.byref(t), C.byref(n), C.byref(c), C.byref(b))
+        return t.value, n.value, c.value, b.value
 
     def timer_start(self):
         rc = self._lib.fcfd_timer_start(self._h)

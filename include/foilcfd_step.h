@@ -286,11 +286,13 @@ fcfd_patch_box fcfd_derive_patch_box(const fcfd_dims* dims,
 long long fcfd_kernel_launches(const fcfd_solver* s);
 /* Per-kernel timing on the solver stream with CUDA events: when enabled,
  * every stream-collide launch (both levels) is bracketed by events and
- * fcfd_collide_time_ms returns the total ms, the launch count and the cells
- * those launches updated since the last call. */
+ * fcfd_collide_time_ms returns the total ms, the launch count, the cells
+ * those launches covered and their algorithmic DRAM bytes (per cell class:
+ * read+write cells 2*19 populations + kind byte, inlet cells 19 + 1,
+ * untouched solid/slip/interface cells 1) since the last call. */
 int fcfd_enable_collide_timing(fcfd_solver* s, int enabled);
 int fcfd_collide_time_ms(fcfd_solver* s, double* total_ms, long long* count,
-                         double* cells);
+                         double* cells, double* alg_bytes);
 /* Event pair on the solver stream: start, then stop returns elapsed ms. */
 int fcfd_timer_start(fcfd_solver* s);
 int fcfd_timer_stop(fcfd_solver* s, double* ms);
