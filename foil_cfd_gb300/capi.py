@@ -76,6 +76,7 @@ _SIGS = {
     "fcfd_forces": (C.c_int, [P, C.POINTER(ForceReadout)]),
     "fcfd_force_raw": (C.c_int, [P, P]),
     "fcfd_force_now": (C.c_int, [P, P]),
+    "fcfd_force_links_noalloc": (C.c_int, [P, C.c_longlong, P, P, C.c_int, P, P, P, P, P]),
     "fcfd_macro": (C.c_int, [P, P, P, P, P]),
     "fcfd_download_macro": (C.c_int, [P, P, P, P, P]),
     "fcfd_active_f": (P, [P]),

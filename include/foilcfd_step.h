@@ -180,6 +180,31 @@ int fcfd_forces(fcfd_solver* s, fcfd_force_readout* out);
 int fcfd_force_raw(fcfd_solver* s, double out[3]);
 /* Runs the force reduction now on the current state (no stepping). */
 int fcfd_force_now(fcfd_solver* s, double out[3]);
+
+/* Largest wall-link list fcfd_force_links_noalloc accepts (1,048,576
+ * entries): its scratch is a fixed device array of one FP64 triple per 256
+ * links, 96 KB, held by every GPU that loads the library. */
+#define FCFD_FORCE_NOALLOC_MAX_LINKS (4096 * 256)
+
+/* No counterpart in the reference. The momentum-exchange force of a caller's
+ * FP32 population buffer (unpadded SoA, 19*ncells floats on the device) over
+ * a caller's compact wall-link list (link_cells[i]: fluid cell index,
+ * link_masks[i]: bit q set when the neighbour at +c_q is solid), optionally
+ * with a half-bit slip field (uwx/uwy/uwz, all three or none), summed in FP64
+ * into out[3] (device memory), enqueued on `stream`. For callers that cannot
+ * allocate device memory -- a frame loop with a hard time budget, where
+ * cudaMalloc may synchronise the device, or a host whose memory manager owns
+ * every allocation: it calls no cudaMalloc/cudaFree; its scratch lives in a
+ * static device array. The first call on each device looks that array's
+ * address up (cudaGetSymbolAddress, with the device current); make it before
+ * any stream capture. Calls share the array, so calls that overlap on the GPU
+ * race. Returns cudaErrorInvalidValue (1) when count exceeds
+ * FCFD_FORCE_NOALLOC_MAX_LINKS or an argument is missing. */
+int fcfd_force_links_noalloc(const float* f, long long ncells,
+                             const uint32_t* link_cells,
+                             const uint32_t* link_masks, int count,
+                             const uint16_t* uwx, const uint16_t* uwy,
+                             const uint16_t* uwz, double* out, void* stream);
 /* velocityField() / deviceRho() (lbm_solver.h:423-429): device pointers of
  * the unpadded macroscopic arrays, written on each batch's last step. */
 int fcfd_macro(fcfd_solver* s, const float** rho, const float** u,
