@@ -1,0 +1,544 @@
+// Per-cell building blocks of the stream-collide kernels and the two kernel
+// templates built from them: the one-cell-per-thread kernel and the staged
+// kernel that streams x-rows through shared memory with bulk async copies.
+//
+// Physics follows the reference step (src/sim/lbm_core.cu:213-475): per link
+// the upstream neighbour's flag selects plain streaming, half-way bounce-back
+// (opposite slot of this cell) or specular free slip (mirrored slot of the
+// tangentially displaced cell); inlet cells are written with feq(1, u_in),
+// outlets copy the upstream column; moments with a density floor of 0.05; a
+// |u| <= 0.3 limiter; Smagorinsky tau_eff from the non-equilibrium stress
+// (Hou et al. 1996); TRT with magic parameter Lambda.
+//
+// Two collision bodies, selected by the EXACT template flag:
+//  * collide_exact: the reference kernel's expression tree (lbm_core.cu:
+//    386-467) with zero-coefficient terms skipped (an exact identity). It is
+//    bit-identical to the reference only in a translation unit compiled with
+//    --fmad=false (collide_f32.cu), where no multiply-add is contracted.
+//  * collide_fast: moments, stress and TRT formed from opposite-pair
+//    sums/differences with the equilibrium's second moment in closed form
+//    (rho/3 I + rho u u); fewer instructions, FP32-rounding-level different.
+//
+// This header is included by exactly one translation unit per instantiation
+// set; the kernels live in an anonymous namespace.
+#pragma once
+
+#include "d3q19.cuh"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+namespace fcfd {
+namespace {
+
+struct CollideArgs {
+    int nx, ny, nz;
+    long long n; // cells per direction slice
+    float tau0, lambda, smagPre, uIn;
+    int writeMacro;
+    float *rho, *u, *v, *w;
+    const std::uint16_t *uwx, *uwy, *uwz;
+    int* status; // staged kernel: nonzero when a pipeline wait timed out
+};
+
+// ---- equilibrium in the reference expression order ------------------------
+__device__ __forceinline__ float dot_c(int q, float ux, float uy, float uz) {
+    // (cx ux + cy uy) + cz uz with zero terms dropped and +-1 folded.
+    float d = 0.0f;
+    bool any = false;
+    if (cx(q) != 0) { d = cx(q) > 0 ? ux : -ux; any = true; }
+    if (cy(q) != 0) { const float t = cy(q) > 0 ? uy : -uy; d = any ? d + t : t; any = true; }
+    if (cz(q) != 0) { const float t = cz(q) > 0 ? uz : -uz; d = any ? d + t : t; }
+    return d;
+}
+
+/// Reference equilibrium19 (lbm_core.cu:65-73): (w rho)((1 + cu + cu cu/2) - usq).
+__device__ __forceinline__ void eq19(float rho, float ux, float uy, float uz, float (&feq)[kQ]) {
+    const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+        const float cu = 3.0f * dot_c(q, ux, uy, uz);
+        feq[q] = (wgt(q) * rho) * (1.0f + cu + 0.5f * cu * cu - usq);
+    }
+}
+
+// ---- collision bodies ------------------------------------------------------
+__device__ __forceinline__ void collide_exact(float (&f)[kQ], float tau0, float lambda, float smagPre,
+                                              float& rhoO, float& uxO, float& uyO, float& uzO) {
+    float rho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+        rho += f[q];
+        if (cx(q) != 0) jx = cx(q) > 0 ? jx + f[q] : jx - f[q];
+        if (cy(q) != 0) jy = cy(q) > 0 ? jy + f[q] : jy - f[q];
+        if (cz(q) != 0) jz = cz(q) > 0 ? jz + f[q] : jz - f[q];
+    }
+    rho = fmaxf(rho, kRhoFloor);
+    const float invRho = 1.0f / rho;
+    float ux = jx * invRho, uy = jy * invRho, uz = jz * invRho;
+    const float u2 = ux * ux + uy * uy + uz * uz;
+    if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
+        // 1/sqrt as IEEE operations (the reference's rsqrtf is approximate).
+        const float s = kMaxSimSpeed * (1.0f / sqrtf(u2));
+        ux *= s; uy *= s; uz *= s;
+    }
+    float feq[kQ];
+    eq19(rho, ux, uy, uz, feq);
+    float tauEff = tau0;
+    if (smagPre > 0.0f) {
+        float pxx = 0.0f, pyy = 0.0f, pzz = 0.0f, pxy = 0.0f, pxz = 0.0f, pyz = 0.0f;
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            const float fneq = f[q] - feq[q];
+            if (cx(q) != 0) pxx += fneq;
+            if (cy(q) != 0) pyy += fneq;
+            if (cz(q) != 0) pzz += fneq;
+            if (cx(q) * cy(q) != 0) pxy = cx(q) * cy(q) > 0 ? pxy + fneq : pxy - fneq;
+            if (cx(q) * cz(q) != 0) pxz = cx(q) * cz(q) > 0 ? pxz + fneq : pxz - fneq;
+            if (cy(q) * cz(q) != 0) pyz = cy(q) * cz(q) > 0 ? pyz + fneq : pyz - fneq;
+        }
+        const float qbar = sqrtf(pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
+        tauEff = 0.5f * (tau0 + sqrtf(tau0 * tau0 + smagPre * qbar * invRho));
+    }
+    const float omP = 1.0f / tauEff;
+    const float tauM = 0.5f + lambda / (tauEff - 0.5f);
+    const float omM = 1.0f / tauM;
+    f[0] = f[0] - omP * (f[0] - feq[0]);
+#pragma unroll
+    for (int p = 1; p <= 9; ++p) {
+        const int qa = 2 * p - 1, qb = 2 * p;
+        const float sym = omP * (0.5f * (f[qa] + f[qb]) - 0.5f * (feq[qa] + feq[qb]));
+        const float asym = omM * (0.5f * (f[qa] - f[qb]) - 0.5f * (feq[qa] - feq[qb]));
+        const float fa = f[qa];
+        f[qa] = fa - sym - asym;
+        f[qb] = f[qb] - sym + asym;
+    }
+    rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
+}
+
+__device__ __forceinline__ void collide_fast(float (&f)[kQ], float tau0, float lambda, float smagPre,
+                                             float& rhoO, float& uxO, float& uyO, float& uzO) {
+    float s[10], d[10];
+#pragma unroll
+    for (int p = 1; p <= 9; ++p) {
+        s[p] = f[2 * p - 1] + f[2 * p];
+        d[p] = f[2 * p - 1] - f[2 * p];
+    }
+    // Pair p has velocity c_{2p-1}: p1 (1,0,0) p2 (0,1,0) p3 (0,0,1)
+    // p4 (1,1,0) p5 (1,0,1) p6 (0,1,1) p7 (1,-1,0) p8 (1,0,-1) p9 (0,1,-1).
+    float rho = f[0] + ((s[1] + s[2]) + (s[3] + s[4])) + ((s[5] + s[6]) + (s[7] + s[8])) + s[9];
+    const float jx = (d[1] + d[4]) + (d[5] + d[7]) + d[8];
+    const float jy = (d[2] + d[4]) + (d[6] - d[7]) + d[9];
+    const float jz = (d[3] + d[5]) + (d[6] - d[8]) - d[9];
+    rho = fmaxf(rho, kRhoFloor);
+    const float inv = __frcp_rn(rho);
+    float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+    float u2 = ux * ux + uy * uy + uz * uz;
+    if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
+        const float sc = kMaxSimSpeed * rsqrtf(u2);
+        ux *= sc; uy *= sc; uz *= sc;
+        u2 = ux * ux + uy * uy + uz * uz;
+    }
+    float tauEff = tau0;
+    if (smagPre > 0.0f) {
+        const float pxx = (s[1] + s[4]) + (s[5] + s[7]) + s[8];
+        const float pyy = (s[2] + s[4]) + (s[6] + s[7]) + s[9];
+        const float pzz = (s[3] + s[5]) + (s[6] + s[8]) + s[9];
+        const float r3 = rho * (1.0f / 3.0f);
+        const float rux = rho * ux, ruy = rho * uy;
+        const float nxx = pxx - r3 - rux * ux;
+        const float nyy = pyy - r3 - ruy * uy;
+        const float nzz = pzz - r3 - rho * uz * uz;
+        const float nxy = (s[4] - s[7]) - rux * uy;
+        const float nxz = (s[5] - s[8]) - rux * uz;
+        const float nyz = (s[6] - s[9]) - ruy * uz;
+        const float qbar = sqrtf(nxx * nxx + nyy * nyy + nzz * nzz + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz));
+        tauEff = 0.5f * (tau0 + sqrtf(tau0 * tau0 + smagPre * qbar * inv));
+    }
+    const float omP = __frcp_rn(tauEff);
+    const float omM = __frcp_rn(0.5f + __fdiv_rn(lambda, tauEff - 0.5f));
+    const float base = 1.0f - 1.5f * u2;
+    const float r1 = rho * (1.0f / 18.0f), r2 = rho * (1.0f / 36.0f);
+    f[0] = f[0] - omP * (f[0] - rho * (1.0f / 3.0f) * base);
+#pragma unroll
+    for (int p = 1; p <= 9; ++p) {
+        const int a = 2 * p - 1;
+        const float wr = p <= 3 ? r1 : r2;
+        const float cu = cx(a) * ux + cy(a) * uy + cz(a) * uz;
+        const float es = wr * (base + 4.5f * cu * cu);
+        const float ea = (3.0f * wr) * cu;
+        const float t1 = omP * (0.5f * s[p] - es);
+        const float t2 = omM * (0.5f * d[p] - ea);
+        f[a] = f[a] - t1 - t2;
+        f[a + 1] = f[a + 1] - t1 + t2;
+    }
+    rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ void collide_body(float (&f)[kQ], const CollideArgs& a, float& r, float& ux, float& uy,
+                                             float& uz) {
+    if constexpr (EXACT) collide_exact(f, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
+    else collide_fast(f, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
+}
+
+// ---- per-cell pieces ---------------------------------------------------------
+struct Nbr {
+    unsigned sx[3], sy[3], sz[3];
+};
+
+/// Source coordinates of a pull along each velocity component (x - c, wrapped).
+__device__ __forceinline__ Nbr neighbours(int x, int y, int z, int nx, int ny, int nz) {
+    Nbr b;
+    b.sx[0] = wrap_inc(x, nx); b.sx[1] = x; b.sx[2] = wrap_dec(x, nx);
+    b.sy[0] = wrap_inc(y, ny); b.sy[1] = y; b.sy[2] = wrap_dec(y, ny);
+    b.sz[0] = wrap_inc(z, nz); b.sz[1] = z; b.sz[2] = wrap_dec(z, nz);
+    return b;
+}
+
+/// Boundary (non-fluid) cell: inlet feq(1, u_in), outlets from the upstream
+/// column, everything else untouched (lbm_core.cu:241-283).
+template <class S>
+__device__ __forceinline__ void boundary_cell(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                                              const CollideArgs& a, int flag, unsigned cell, int x, int y, int z) {
+    const long long n = a.n;
+    if (flag == kInlet) {
+        float feq[kQ];
+        eq19(1.0f, a.uIn, 0.0f, 0.0f, feq);
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) S::st(dst + q * n, cell, feq[q], wgt(q));
+        if (a.writeMacro) { a.rho[cell] = 1.0f; a.u[cell] = a.uIn; a.v[cell] = 0.0f; a.w[cell] = 0.0f; }
+    } else if (flag == kOutlet || flag == kOutletEq) {
+        const unsigned up = static_cast<unsigned>(wrap_dec(x, a.nx))
+                          + static_cast<unsigned>(a.nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z);
+        float g[kQ];
+        float r = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            g[q] = S::ld(src + q * n, up, wgt(q));
+            r += g[q];
+            if (cx(q) != 0) jx = cx(q) > 0 ? jx + g[q] : jx - g[q];
+            if (cy(q) != 0) jy = cy(q) > 0 ? jy + g[q] : jy - g[q];
+            if (cz(q) != 0) jz = cz(q) > 0 ? jz + g[q] : jz - g[q];
+        }
+        const float inv = 1.0f / r;
+        const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+        if (flag == kOutletEq) {
+            eq19(1.0f, ux, uy, uz, g);   // equilibrium outflow feq(1, u_upstream)
+            r = 1.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) S::st(dst + q * n, cell, g[q], wgt(q));
+        if (a.writeMacro) { a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz; }
+    } else if (a.writeMacro) {
+        a.rho[cell] = 1.0f; a.u[cell] = 0.0f; a.v[cell] = 0.0f; a.w[cell] = 0.0f;
+    }
+}
+
+/// Bulk fluid cell: 19 plain pulls from global memory.
+template <class S>
+__device__ __forceinline__ void gather_bulk(const typename S::T* __restrict__ src, const CollideArgs& a,
+                                            const Nbr& b, float (&f)[kQ]) {
+    const unsigned unx = a.nx, uny = a.ny;
+#pragma unroll
+    for (int q = 0; q < kQ; ++q)
+        f[q] = S::ld(src + q * a.n, b.sx[1 + cx(q)] + unx * (b.sy[1 + cy(q)] + uny * b.sz[1 + cz(q)]), wgt(q));
+}
+
+/// Near-wall fluid cell: the upstream flag picks the (slot, cell) pair per
+/// link; the wall-model Ladd term 6 w_q (c_q . u_w) on solid links.
+template <class S, bool WM>
+__device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ src,
+                                            const std::uint8_t* __restrict__ kind, const CollideArgs& a,
+                                            const Nbr& b, unsigned cell, int y, int z, float (&f)[kQ]) {
+    const unsigned unx = a.nx, uny = a.ny;
+    const long long n = a.n;
+    float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
+    bool uwLoaded = false;
+    f[0] = S::ld(src, cell, wgt(0));
+#pragma unroll
+    for (int q = 1; q < kQ; ++q) {
+        const unsigned X = b.sx[1 + cx(q)], Y = b.sy[1 + cy(q)], Z = b.sz[1 + cz(q)];
+        const unsigned pn = X + unx * (Y + uny * Z);
+        const int nf = kind[pn] & kFlagMask;
+        const bool solid = nf == kSolid;
+        const bool slipY = is_slip_y(nf);
+        const bool slipZ = is_slip_z(nf);
+        const unsigned pY = X + unx * (static_cast<unsigned>(y) + uny * Z);
+        const unsigned pZ = X + unx * (Y + uny * static_cast<unsigned>(z));
+        const int qs = solid ? opp(q) : (slipY ? mir_y(q) : (slipZ ? mir_z(q) : q));
+        const unsigned cs = solid ? cell : (slipY ? pY : (slipZ ? pZ : pn));
+        float fq = S::ld(src + static_cast<long long>(qs) * n, cs, wgt(q));
+        if constexpr (WM) {
+            if (solid) {
+                if (!uwLoaded) {
+                    uwx = __half2float(__ushort_as_half(a.uwx[cell]));
+                    uwy = __half2float(__ushort_as_half(a.uwy[cell]));
+                    uwz = __half2float(__ushort_as_half(a.uwz[cell]));
+                    uwLoaded = true;
+                }
+                fq += (6.0f * wgt(q)) * dot_c(q, uwx, uwy, uwz);
+            }
+        }
+        f[q] = fq;
+    }
+}
+
+template <class S, bool EXACT>
+__device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, const CollideArgs& a, unsigned cell,
+                                            float (&f)[kQ]) {
+    float r, ux, uy, uz;
+    collide_body<EXACT>(f, a, r, ux, uy, uz);
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) S::st(dst + q * a.n, cell, f[q], wgt(q));
+    if (a.writeMacro) { a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz; }
+}
+
+// ---- one cell per thread -----------------------------------------------------
+constexpr int kCellBlockX = 128;
+
+template <class S, bool WM, bool EXACT>
+__global__ void __launch_bounds__(kCellBlockX)
+collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                    const std::uint8_t* __restrict__ kind, CollideArgs a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= a.nx) return;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const unsigned cell = static_cast<unsigned>(x)
+                        + static_cast<unsigned>(a.nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z);
+    const std::uint8_t k = kind[cell];
+    const int flag = k & kFlagMask;
+    if (flag != kFluid) {
+        boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
+        return;
+    }
+    const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
+    float f[kQ];
+    if (!(k & kNearWall)) gather_bulk<S>(src, a, b, f);
+    else gather_wall<S, WM>(src, kind, a, b, cell, y, z, f);
+    finish_cell<S, EXACT>(dst, a, cell, f);
+}
+
+// ---- staged: x-rows through shared memory with bulk async copies -------------
+// A persistent CTA walks rows r = blockIdx.x + k * gridDim.x (r = y + ny z).
+// For every row it needs, per direction q, the full source row (y - c_y,
+// z - c_z) of slice q; one cp.async.bulk per direction brings it into a
+// shared-memory stage and signals the stage's mbarrier (complete_tx). With
+// `stages` stages the copies of the next rows are in flight while the current
+// row is computed, so the bytes in flight no longer depend on resident warps.
+// Bulk fluid cells read their 19 pulls from the stage (x - c_x wraps inside
+// the row); wall-adjacent and boundary cells use the global-memory paths.
+// Requires rows of a multiple of 16 bytes (bulk-copy alignment).
+constexpr int kStagedThreads = 320;
+constexpr long long kWaitLimit = 1LL << 22; // try_wait polls before a timeout
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(std::uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(std::uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+/// Bounded wait on a stage barrier; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, unsigned parity) {
+    for (long long i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dstSmem, const void* srcGlobal, unsigned bytes, std::uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dstSmem)),
+        "l"(srcGlobal), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <class S>
+__device__ __forceinline__ void issue_row(const typename S::T* __restrict__ src, typename S::T* stage,
+                                          std::uint64_t* bar, long long row, const CollideArgs& a) {
+    using T = typename S::T;
+    const int y = static_cast<int>(row % a.ny), z = static_cast<int>(row / a.ny);
+    const unsigned rowBytes = static_cast<unsigned>(a.nx) * sizeof(T);
+    mbar_expect_tx(bar, rowBytes * kQ);
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+        int ys = y - cy(q), zs = z - cz(q);
+        ys = ys < 0 ? ys + a.ny : (ys >= a.ny ? ys - a.ny : ys);
+        zs = zs < 0 ? zs + a.nz : (zs >= a.nz ? zs - a.nz : zs);
+        const T* g = src + q * a.n + static_cast<long long>(a.nx) * (ys + static_cast<long long>(a.ny) * zs);
+        bulk_g2s(stage + q * a.nx, g, rowBytes, bar);
+    }
+}
+
+template <class S, bool WM, bool EXACT>
+__global__ void __launch_bounds__(kStagedThreads)
+collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                      const std::uint8_t* __restrict__ kind, CollideArgs a, int stages) {
+    using T = typename S::T;
+    extern __shared__ __align__(128) unsigned char smem[];
+    std::uint64_t* bars = reinterpret_cast<std::uint64_t*>(smem);
+    T* buf = reinterpret_cast<T*>(smem + 128);
+    const long long rows = static_cast<long long>(a.ny) * a.nz;
+    const long long G = gridDim.x;
+    const int nx = a.nx;
+    const size_t stageElems = static_cast<size_t>(kQ) * nx;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int s = 0; s < stages; ++s) {
+            const long long r = blockIdx.x + s * G;
+            if (r < rows) issue_row<S>(src, buf + s * stageElems, &bars[s], r, a);
+        }
+    }
+    __syncthreads();
+
+    for (long long k = 0;; ++k) {
+        const long long r = blockIdx.x + k * G;
+        if (r >= rows) break;
+        const int s = static_cast<int>(k % stages);
+        // Bounded wait, decided for the whole block at once.
+        const int landed = __syncthreads_and(mbar_wait(&bars[s], static_cast<unsigned>((k / stages) & 1)) ? 1 : 0);
+        if (!landed) {
+            // Copies did not land within the limit: report, let the copies
+            // still in flight for this CTA finish (bounded), and stop.
+            if (threadIdx.x == 0) {
+                atomicExch(a.status, 1);
+                for (long long j = k; j < k + stages; ++j)
+                    if (blockIdx.x + j * G < rows)
+                        (void)mbar_wait(&bars[j % stages], static_cast<unsigned>((j / stages) & 1));
+            }
+            break;
+        }
+        const T* st = buf + s * stageElems;
+        const int y = static_cast<int>(r % a.ny), z = static_cast<int>(r / a.ny);
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+            const unsigned cell = static_cast<unsigned>(x) + static_cast<unsigned>(nx) * static_cast<unsigned>(r);
+            const std::uint8_t kb = __ldg(kind + cell);
+            const int flag = kb & kFlagMask;
+            if (flag != kFluid) {
+                boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
+                continue;
+            }
+            float f[kQ];
+            if (!(kb & kNearWall)) {
+                const int xs[3] = {wrap_inc(x, nx), x, wrap_dec(x, nx)};
+#pragma unroll
+                for (int q = 0; q < kQ; ++q) f[q] = S::lds(st + q * nx, xs[1 + cx(q)], wgt(q));
+            } else {
+                const Nbr b = neighbours(x, y, z, nx, a.ny, a.nz);
+                gather_wall<S, WM>(src, kind, a, b, cell, y, z, f);
+            }
+            finish_cell<S, EXACT>(dst, a, cell, f);
+        }
+        __syncthreads(); // every thread is done reading stage s
+        const long long rn = r + stages * G;
+        if (threadIdx.x == 0 && rn < rows) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_row<S>(src, buf + s * stageElems, &bars[s], rn, a);
+        }
+    }
+}
+
+// ---- launch ------------------------------------------------------------------
+struct StagedPlan {
+    int stages = 0;
+    size_t smem = 0;
+};
+
+template <class S>
+StagedPlan staged_plan(LevelDims d) {
+    StagedPlan p;
+    const size_t rowBytes = static_cast<size_t>(d.nx) * sizeof(typename S::T);
+    if (rowBytes % 16 != 0 || d.nx < 8) return p;
+    const size_t stageBytes = rowBytes * kQ;
+    // Two CTAs per SM when they fit (<= 113 KB each), else one (<= 227 KB).
+    for (size_t budget : {size_t(113 * 1024), size_t(227 * 1024)}) {
+        const long long st = static_cast<long long>((budget - 128) / stageBytes);
+        if (st >= 2) {
+            p.stages = static_cast<int>(st > 4 ? 4 : st);
+            p.smem = 128 + stageBytes * static_cast<size_t>(p.stages);
+            return p;
+        }
+    }
+    return p;
+}
+
+inline int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <class S, bool EXACT>
+cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t* kind, LevelDims d,
+                                const CollideParams& p, float* rho, float* u, float* v, float* w, SlipField slip,
+                                cudaStream_t st) {
+    using T = typename S::T;
+    CollideArgs a;
+    a.nx = d.nx; a.ny = d.ny; a.nz = d.nz; a.n = d.cells();
+    a.tau0 = p.tau; a.lambda = p.magicLambda; a.smagPre = p.smagPrefactor; a.uIn = p.uInlet;
+    a.writeMacro = (p.writeMacro && rho && u && v && w) ? 1 : 0;
+    a.rho = rho; a.u = u; a.v = v; a.w = w;
+    a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
+    a.status = p.status;
+    const T* src = static_cast<const T*>(srcv);
+    T* dst = static_cast<T*>(dstv);
+    const bool wm = slip.active();
+    const StagedPlan plan = staged_plan<S>(d);
+    const bool staged = p.status && plan.stages >= 2 && p.kernel != 1;
+    if (staged) {
+        auto kern = wm ? collide_staged_kernel<S, true, EXACT> : collide_staged_kernel<S, false, EXACT>;
+        // Attribute and occupancy are queried once per (kernel, smem size).
+        struct Entry { const void* k; size_t smem; int perSm; };
+        static Entry cache[8] = {};
+        int perSm = 0;
+        for (const Entry& c : cache)
+            if (c.k == reinterpret_cast<const void*>(kern) && c.smem == plan.smem) perSm = c.perSm;
+        if (perSm == 0) {
+            if (auto e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              static_cast<int>(plan.smem));
+                e != cudaSuccess)
+                return e;
+            if (auto e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kStagedThreads, plan.smem);
+                e != cudaSuccess)
+                return e;
+            if (perSm < 1) perSm = 1;
+            for (Entry& c : cache)
+                if (c.k == nullptr) { c = Entry{reinterpret_cast<const void*>(kern), plan.smem, perSm}; break; }
+        }
+        const long long rows = static_cast<long long>(d.ny) * d.nz;
+        long long grid = static_cast<long long>(sm_count()) * perSm;
+        if (grid > rows) grid = rows;
+        kern<<<static_cast<unsigned>(grid), kStagedThreads, plan.smem, st>>>(src, dst, kind, a, plan.stages);
+        return cudaGetLastError();
+    }
+    const int bx = d.nx >= kCellBlockX ? kCellBlockX : ((d.nx + 31) / 32) * 32;
+    const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),
+                    static_cast<unsigned>(d.nz));
+    if (wm) collide_cell_kernel<S, true, EXACT><<<grid, bx, 0, st>>>(src, dst, kind, a);
+    else collide_cell_kernel<S, false, EXACT><<<grid, bx, 0, st>>>(src, dst, kind, a);
+    return cudaGetLastError();
+}
+
+} // namespace
+} // namespace fcfd

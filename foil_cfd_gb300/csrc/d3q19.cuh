@@ -117,6 +117,8 @@ struct StoreF32 {
     __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float) {
         p[i] = v;
     }
+    /// Load from a shared-memory stage.
+    __device__ __forceinline__ static float lds(const T* p, int i, float) { return p[i]; }
 };
 struct StoreF16 {
     using T = __half;
@@ -127,6 +129,7 @@ struct StoreF16 {
     __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float w) {
         p[i] = __float2half_rn(v - w);
     }
+    __device__ __forceinline__ static float lds(const T* p, int i, float w) { return w + __half2float(p[i]); }
 };
 
 // ---- helpers ---------------------------------------------------------------

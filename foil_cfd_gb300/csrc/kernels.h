@@ -28,6 +28,8 @@ struct CollideParams {
     float smagPrefactor = 0.0f; ///< 18*sqrt(2)*Cs^2; 0 disables LES.
     float uInlet = 0.08f;
     int writeMacro = 0;
+    int* status = nullptr;  ///< Device int set nonzero if a staged copy wait timed out.
+    int kernel = 0;         ///< 0 automatic, 1 one-cell kernel, 2 staged kernel.
 };
 
 /// Half-bit slip field of a level (WallSlipView, lbm_core.cuh:201-208).
@@ -67,6 +69,8 @@ cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint
                                    LevelDims d, const CollideParams& p, float* rho,
                                    float* u, float* v, float* w, SlipField slip,
                                    cudaStream_t st);
+/// Whether the staged kernel serves a level (16-byte rows, >= 2 stages fit).
+bool staged_applies(LevelDims d, Storage s);
 cudaError_t launch_init_eq_f32(float* f, const std::uint8_t* kind, long long n, float uIn,
                                cudaStream_t st);
 cudaError_t launch_init_macro_f32(float* f, const std::uint8_t* kind, long long n,

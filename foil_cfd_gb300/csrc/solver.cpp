@@ -124,6 +124,7 @@ struct fcfd_solver {
     Storage storage = Storage::F32;
     float lesCs = kDefaultCs;
     float lambda = kDefaultLambda;
+    int collideKernel = 0;
     bool initialized = false;
 
     // ---- levels ----
@@ -145,7 +146,8 @@ struct fcfd_solver {
     double* dForce = nullptr;
     double* hForce = nullptr;
     int* dNan = nullptr;
-    int* hNan = nullptr;
+    int* hNan = nullptr;      // [0] watchdog verdict, [1] staged-copy status
+    int* dStatus = nullptr;
     cudaEvent_t evT0 = nullptr, evT1 = nullptr, evForce = nullptr, evNan = nullptr;
 
     // ---- state ----
@@ -226,7 +228,8 @@ struct fcfd_solver {
             forcePending = false;
         }
         if (nanPending && eventDone(evNan)) {
-            if (*hNan != 0) { nanLatched = true; nanKind = *hNan; }
+            if (hNan[0] != 0) { nanLatched = true; nanKind = hNan[0]; }
+            if (hNan[1] != 0) { nanLatched = true; nanKind = 9; }
             nanPending = false;
         }
     }
@@ -377,7 +380,7 @@ struct fcfd_solver {
         if (stream) cudaStreamSynchronize(stream);
         freeFine();
         coarse.free_all();
-        dfree(rho); dfree(u); dfree(v); dfree(w); dfree(dForce); dfree(dNan);
+        dfree(rho); dfree(u); dfree(v); dfree(w); dfree(dForce); dfree(dNan); dfree(dStatus);
         if (hForce) { cudaFreeHost(hForce); hForce = nullptr; }
         if (hNan) { cudaFreeHost(hNan); hNan = nullptr; }
         for (cudaEvent_t* e : {&evT0, &evT1, &evForce, &evNan})
@@ -447,6 +450,8 @@ struct fcfd_solver {
             p.smagPrefactor = smagPre();
             p.uInlet = effU();
             p.writeMacro = (i == n - 1) ? 1 : 0;
+            p.status = dStatus;
+            p.kernel = collideKernel;
             if (auto e = collide(coarse, p, rho, u, v, w); e != cudaSuccess) return e;
             if (fineActive) {
                 const int m = factor;
@@ -487,6 +492,7 @@ struct fcfd_solver {
                     launch_watchdog(storage, fine.f[fine.src], fine.d, dNan, steps * 977, 2, stream);
                 }
                 cudaMemcpyAsync(hNan, dNan, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                cudaMemcpyAsync(hNan + 1, dStatus, sizeof(int), cudaMemcpyDeviceToHost, stream);
                 cudaEventRecord(evNan, stream);
                 nanPending = true;
             }
@@ -528,6 +534,7 @@ struct fcfd_solver {
         nanKind = 0;
         sinceWatchdog = 0;
         cudaMemsetAsync(dNan, 0, sizeof(int), stream);
+        cudaMemsetAsync(dStatus, 0, sizeof(int), stream);
         const float initU = rampEnabled ? 0.0f : scaling.u_lat;
         for (int i = 0; i < 2; ++i) {
             launches += 2;
@@ -676,10 +683,12 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
     s->storage = Storage::F32;
     s->lesCs = kDefaultCs;
     s->lambda = kDefaultLambda;
+    s->collideKernel = 0;
     if (opts) {
         s->storage = opts->storage == FCFD_STORE_FP16 ? Storage::F16 : Storage::F32;
         if (opts->les_cs != 0.0f) s->lesCs = opts->les_cs;
         if (opts->magic_lambda > 0.0f) s->lambda = opts->magic_lambda;
+        s->collideKernel = (opts->collide_kernel >= 0 && opts->collide_kernel <= 2) ? opts->collide_kernel : 0;
     }
     auto fail = [&](const char* what, cudaError_t e) {
         set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));
@@ -693,14 +702,17 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
         if (auto e = dalloc(p, cells * 4); e != cudaSuccess) return fail("macroscopic allocation failed", e);
     if (auto e = dalloc(&s->dForce, 3 * sizeof(double)); e != cudaSuccess) return fail("force slot allocation failed", e);
     if (auto e = dalloc(&s->dNan, sizeof(int)); e != cudaSuccess) return fail("watchdog allocation failed", e);
+    if (auto e = dalloc(&s->dStatus, sizeof(int)); e != cudaSuccess) return fail("status allocation failed", e);
+    if (auto e = cudaMemsetAsync(s->dStatus, 0, sizeof(int), s->stream); e != cudaSuccess)
+        return fail("status allocation failed", e);
     if (auto e = cudaMallocHost(&s->hForce, 3 * sizeof(double)); e != cudaSuccess) return fail("pinned allocation failed", e);
-    if (auto e = cudaMallocHost(&s->hNan, sizeof(int)); e != cudaSuccess) return fail("pinned allocation failed", e);
+    if (auto e = cudaMallocHost(&s->hNan, 2 * sizeof(int)); e != cudaSuccess) return fail("pinned allocation failed", e);
     for (auto pr : {std::pair<cudaEvent_t*, unsigned>{&s->evT0, 0u}, {&s->evT1, 0u},
                     {&s->evForce, static_cast<unsigned>(cudaEventDisableTiming)},
                     {&s->evNan, static_cast<unsigned>(cudaEventDisableTiming)}})
         if (auto e = cudaEventCreateWithFlags(pr.first, pr.second); e != cudaSuccess)
             return fail("event creation failed", e);
-    *s->hNan = 0;
+    s->hNan[0] = s->hNan[1] = 0;
     s->launches += 1;
     launch_fill(s->rho, d.cells(), 1.0f, s->stream);
     cudaMemsetAsync(s->u, 0, cells * 4, s->stream);

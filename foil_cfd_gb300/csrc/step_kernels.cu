@@ -1,236 +1,19 @@
-// Fused D3Q19 stream-collide (pull scheme, TRT + Smagorinsky, optional iMEM
-// moving-wall term) and the small per-level kernels around it: cell-kind
-// classification, equilibrium / speck / macroscopic initialisation, the NaN
-// watchdog and FP32 <-> storage conversion.
-//
-// Physics follows the reference step (src/sim/lbm_core.cu:213-475): per link
-// the upstream neighbour's flag selects plain streaming, half-way bounce-back
-// (opposite slot of this cell), or specular free slip (mirrored slot of the
-// tangentially displaced cell); moments with a density floor of 0.05; a
-// velocity limiter at |u| = 0.3; Smagorinsky tau_eff from the non-equilibrium
-// stress (Hou et al. 1996); TRT with magic parameter Lambda.
+// Per-level kernels around the stream-collide: cell-kind classification,
+// equilibrium / speck / macroscopic initialisation, the NaN watchdog, FP32 <->
+// storage conversion, and the FP16-storage stream-collide (the pair-sum
+// collision body of collide_common.cuh with fused multiply-adds; the FP32
+// storage collide lives in collide_f32.cu, compiled without contraction).
 //
 // GB300 layout choices (not in the reference): the buffers are unpadded SoA
 // and all three axes wrap periodically in the index math, so there is no
 // ghost-plane refresh pass; a per-cell kind byte marks the fluid cells that
-// touch a wall, so bulk cells stream without reading 18 neighbour flags; the
-// collision works on opposite-pair sums/differences, with the equilibrium's
-// second moment in closed form (rho/3 I + rho u u) instead of 19 fneq terms.
-#include "d3q19.cuh"
-#include "kernels.h"
-
-#include <cuda_runtime.h>
+// touch a wall, so bulk cells stream without reading 18 neighbour flags.
+#include "collide_common.cuh"
 
 namespace fcfd {
 namespace {
 
-constexpr int kCollideBlockX = 128;
 constexpr int kBlock1D = 256;
-
-struct CollideArgs {
-    int nx, ny, nz;
-    long long n; // cells per direction slice
-    float tau0, lambda, smagPre, uIn;
-    int writeMacro;
-    float* rho;
-    float* u;
-    float* v;
-    float* w;
-    const std::uint16_t* uwx;
-    const std::uint16_t* uwy;
-    const std::uint16_t* uwz;
-};
-
-/// TRT + Smagorinsky collision of one cell, in place on f[19].
-/// Pairs (a, a+1) for odd a carry opposite velocities, so with
-/// s = f_a + f_b and d = f_a - f_b the moments, the momentum-flux tensor and
-/// the TRT update are all formed from 9 sums and 9 differences.
-__device__ __forceinline__ void collide_trt(float (&f)[kQ], float tau0,
-                                            float lambda, float smagPre,
-                                            float& rhoOut, float& uxOut,
-                                            float& uyOut, float& uzOut) {
-    float s[10], d[10];
-#pragma unroll
-    for (int p = 1; p <= 9; ++p) {
-        s[p] = f[2 * p - 1] + f[2 * p];
-        d[p] = f[2 * p - 1] - f[2 * p];
-    }
-    // Pair p has velocity c_{2p-1}: p1 (1,0,0) p2 (0,1,0) p3 (0,0,1)
-    // p4 (1,1,0) p5 (1,0,1) p6 (0,1,1) p7 (1,-1,0) p8 (1,0,-1) p9 (0,1,-1).
-    float rho = f[0] + ((s[1] + s[2]) + (s[3] + s[4])) + ((s[5] + s[6]) + (s[7] + s[8])) + s[9];
-    const float jx = (d[1] + d[4]) + (d[5] + d[7]) + d[8];
-    const float jy = (d[2] + d[4]) + (d[6] - d[7]) + d[9];
-    const float jz = (d[3] + d[5]) + (d[6] - d[8]) - d[9];
-    const float pxx = (s[1] + s[4]) + (s[5] + s[7]) + s[8];
-    const float pyy = (s[2] + s[4]) + (s[6] + s[7]) + s[9];
-    const float pzz = (s[3] + s[5]) + (s[6] + s[8]) + s[9];
-    const float pxy = s[4] - s[7];
-    const float pxz = s[5] - s[8];
-    const float pyz = s[6] - s[9];
-
-    rho = fmaxf(rho, kRhoFloor); // also scrubs a NaN density (IEEE fmax)
-    const float inv = __frcp_rn(rho);
-    float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-    float u2 = ux * ux + uy * uy + uz * uz;
-    if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
-        const float sc = kMaxSimSpeed * rsqrtf(u2);
-        ux *= sc; uy *= sc; uz *= sc;
-        u2 = ux * ux + uy * uy + uz * uz;
-    }
-
-    float tauEff = tau0;
-    if (smagPre > 0.0f) {
-        // Non-equilibrium stress: Pi(f) - (rho/3 I + rho u u).
-        const float r3 = rho * (1.0f / 3.0f);
-        const float rux = rho * ux, ruy = rho * uy;
-        const float nxx = pxx - r3 - rux * ux;
-        const float nyy = pyy - r3 - ruy * uy;
-        const float nzz = pzz - r3 - rho * uz * uz;
-        const float nxy = pxy - rux * uy;
-        const float nxz = pxz - rux * uz;
-        const float nyz = pyz - ruy * uz;
-        const float qbar = sqrtf(nxx * nxx + nyy * nyy + nzz * nzz
-                                 + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz));
-        tauEff = 0.5f * (tau0 + sqrtf(tau0 * tau0 + smagPre * qbar * inv));
-    }
-    const float omP = __frcp_rn(tauEff);
-    const float tauM = 0.5f + __fdiv_rn(lambda, tauEff - 0.5f);
-    const float omM = __frcp_rn(tauM);
-
-    const float base = 1.0f - 1.5f * u2;
-    const float r0 = rho * (1.0f / 3.0f);
-    const float r1 = rho * (1.0f / 18.0f);
-    const float r2 = rho * (1.0f / 36.0f);
-    f[0] = f[0] - omP * (f[0] - r0 * base);
-#pragma unroll
-    for (int p = 1; p <= 9; ++p) {
-        const int a = 2 * p - 1;
-        const float wr = (p <= 3) ? r1 : r2;
-        const float cu = cx(a) * ux + cy(a) * uy + cz(a) * uz;
-        const float es = wr * (base + 4.5f * cu * cu);
-        const float ea = (3.0f * wr) * cu;
-        const float t1 = omP * (0.5f * s[p] - es);
-        const float t2 = omM * (0.5f * d[p] - ea);
-        f[a] = f[a] - t1 - t2;
-        f[a + 1] = f[a + 1] - t1 + t2;
-    }
-    rhoOut = rho; uxOut = ux; uyOut = uy; uzOut = uz;
-}
-
-template <class S, bool WM>
-__global__ void __launch_bounds__(kCollideBlockX)
-collide_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
-               const std::uint8_t* __restrict__ kind, CollideArgs a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= a.nx) return;
-    const int y = blockIdx.y, z = blockIdx.z;
-    const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const long long n = a.n;
-    const unsigned cell = static_cast<unsigned>(x)
-        + static_cast<unsigned>(nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(ny) * z);
-    const std::uint8_t k = kind[cell];
-    const int flag = k & kFlagMask;
-
-    const int xm = wrap_dec(x, nx), xp = wrap_inc(x, nx);
-    // Source coordinate of a pull along velocity component c: x - c.
-    const unsigned sx[3] = {static_cast<unsigned>(xp), static_cast<unsigned>(x),
-                            static_cast<unsigned>(xm)};
-    const unsigned sy[3] = {static_cast<unsigned>(wrap_inc(y, ny)), static_cast<unsigned>(y),
-                            static_cast<unsigned>(wrap_dec(y, ny))};
-    const unsigned sz[3] = {static_cast<unsigned>(wrap_inc(z, nz)), static_cast<unsigned>(z),
-                            static_cast<unsigned>(wrap_dec(z, nz))};
-    const unsigned unx = static_cast<unsigned>(nx), uny = static_cast<unsigned>(ny);
-
-    if (flag != kFluid) {
-        // ---- boundary cells (reference lbm_core.cu:241-283) ----
-        if (flag == kInlet) {
-            const float usq = 1.5f * (a.uIn * a.uIn);
-#pragma unroll
-            for (int q = 0; q < kQ; ++q)
-                S::st(dst + q * n, cell, feq_q(q, 1.0f, a.uIn, 0.0f, 0.0f, usq), wgt(q));
-            if (a.writeMacro) {
-                a.rho[cell] = 1.0f; a.u[cell] = a.uIn; a.v[cell] = 0.0f; a.w[cell] = 0.0f;
-            }
-        } else if (flag == kOutlet || flag == kOutletEq) {
-            const unsigned up = static_cast<unsigned>(xm) + unx * (static_cast<unsigned>(y) + uny * z);
-            float g[kQ];
-            float r = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
-#pragma unroll
-            for (int q = 0; q < kQ; ++q) {
-                g[q] = S::ld(src + q * n, up, wgt(q));
-                r += g[q];
-                jx += cx(q) * g[q]; jy += cy(q) * g[q]; jz += cz(q) * g[q];
-            }
-            const float inv = 1.0f / r;
-            float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-            if (flag == kOutletEq) {
-                // Equilibrium outflow: feq(1, u_upstream).
-                const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
-#pragma unroll
-                for (int q = 0; q < kQ; ++q) g[q] = feq_q(q, 1.0f, ux, uy, uz, usq);
-                r = 1.0f;
-            }
-#pragma unroll
-            for (int q = 0; q < kQ; ++q) S::st(dst + q * n, cell, g[q], wgt(q));
-            if (a.writeMacro) {
-                a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz;
-            }
-        } else if (a.writeMacro) {
-            a.rho[cell] = 1.0f; a.u[cell] = 0.0f; a.v[cell] = 0.0f; a.w[cell] = 0.0f;
-        }
-        return;
-    }
-
-    float f[kQ];
-    if (!(k & kNearWall)) {
-        // Bulk cell: every pull streams from the upstream neighbour.
-#pragma unroll
-        for (int q = 0; q < kQ; ++q) {
-            const unsigned src_idx = sx[1 + cx(q)] + unx * (sy[1 + cy(q)] + uny * sz[1 + cz(q)]);
-            f[q] = S::ld(src + q * n, src_idx, wgt(q));
-        }
-    } else {
-        // Near-wall cell: the upstream flag picks the (slot, cell) pair.
-        float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
-        bool uwLoaded = false;
-        f[0] = S::ld(src, cell, wgt(0));
-#pragma unroll
-        for (int q = 1; q < kQ; ++q) {
-            const unsigned X = sx[1 + cx(q)], Y = sy[1 + cy(q)], Z = sz[1 + cz(q)];
-            const unsigned pn = X + unx * (Y + uny * Z);
-            const int nf = kind[pn] & kFlagMask;
-            const bool solid = nf == kSolid;
-            const bool slipY = is_slip_y(nf);
-            const bool slipZ = is_slip_z(nf);
-            const unsigned pY = X + unx * (static_cast<unsigned>(y) + uny * Z);
-            const unsigned pZ = X + unx * (Y + uny * static_cast<unsigned>(z));
-            const int qs = solid ? opp(q) : (slipY ? mir_y(q) : (slipZ ? mir_z(q) : q));
-            const unsigned cs = solid ? cell : (slipY ? pY : (slipZ ? pZ : pn));
-            float fq = S::ld(src + static_cast<long long>(qs) * n, cs, wgt(q));
-            if constexpr (WM) {
-                // Ladd moving-wall term 6 w_q (c_q . u_w) on solid links.
-                if (solid) {
-                    if (!uwLoaded) {
-                        uwx = __half2float(__ushort_as_half(a.uwx[cell]));
-                        uwy = __half2float(__ushort_as_half(a.uwy[cell]));
-                        uwz = __half2float(__ushort_as_half(a.uwz[cell]));
-                        uwLoaded = true;
-                    }
-                    fq += 6.0f * wgt(q) * (cx(q) * uwx + cy(q) * uwy + cz(q) * uwz);
-                }
-            }
-            f[q] = fq;
-        }
-    }
-
-    float rho, ux, uy, uz;
-    collide_trt(f, a.tau0, a.lambda, a.smagPre, rho, ux, uy, uz);
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) S::st(dst + q * n, cell, f[q], wgt(q));
-    if (a.writeMacro) {
-        a.rho[cell] = rho; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz;
-    }
-}
 
 /// kind = flag | kNearWall for fluid cells with a solid/slip pull neighbour.
 __global__ void classify_kernel(const std::uint8_t* __restrict__ flags,
@@ -362,14 +145,6 @@ inline dim3 plane_grid(const LevelDims& d, int bx) {
                 static_cast<unsigned>(d.nz));
 }
 
-template <class S, bool WM>
-void collide_dispatch(const void* src, void* dst, const std::uint8_t* kind, LevelDims d,
-                      const CollideArgs& args, cudaStream_t st) {
-    const int bx = d.nx >= kCollideBlockX ? kCollideBlockX : ((d.nx + 31) / 32) * 32;
-    collide_kernel<S, WM><<<plane_grid(d, bx), bx, 0, st>>>(
-        static_cast<const typename S::T*>(src), static_cast<typename S::T*>(dst), kind, args);
-}
-
 } // namespace
 
 cudaError_t launch_classify(const std::uint8_t* flags, std::uint8_t* kind, LevelDims d,
@@ -379,25 +154,17 @@ cudaError_t launch_classify(const std::uint8_t* flags, std::uint8_t* kind, Level
     return cudaGetLastError();
 }
 
-cudaError_t launch_collide(Storage s, const void* src, void* dst, const std::uint8_t* kind,
-                           LevelDims d, const CollideParams& p, float* rho, float* u, float* v,
-                           float* w, SlipField slip, cudaStream_t st) {
+cudaError_t launch_collide(Storage s, const void* src, void* dst, const std::uint8_t* kind, LevelDims d,
+                           const CollideParams& p, float* rho, float* u, float* v, float* w, SlipField slip,
+                           cudaStream_t st) {
     if (!src || !dst || !kind || d.cells() <= 0) return cudaErrorInvalidValue;
-    CollideArgs a;
-    a.nx = d.nx; a.ny = d.ny; a.nz = d.nz; a.n = d.cells();
-    a.tau0 = p.tau; a.lambda = p.magicLambda; a.smagPre = p.smagPrefactor; a.uIn = p.uInlet;
-    a.writeMacro = (p.writeMacro && rho && u && v && w) ? 1 : 0;
-    a.rho = rho; a.u = u; a.v = v; a.w = w;
-    a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
-    // FP32 storage runs the reference-order kernel (bit-identical to the
+    // FP32 storage runs the reference-order kernels (bit-identical to the
     // reference step without FMA contraction); FP16 storage runs the
-    // re-associated pair-sum kernel above.
+    // pair-sum collision. Both pick the staged kernel when rows fit it.
     if (s == Storage::F32)
         return launch_collide_f32_ref(static_cast<const float*>(src), static_cast<float*>(dst), kind, d, p,
                                       rho, u, v, w, slip, st);
-    if (slip.active()) collide_dispatch<StoreF16, true>(src, dst, kind, d, a, st);
-    else collide_dispatch<StoreF16, false>(src, dst, kind, d, a, st);
-    return cudaGetLastError();
+    return launch_collide_impl<StoreF16, false>(src, dst, kind, d, p, rho, u, v, w, slip, st);
 }
 
 cudaError_t launch_init_equilibrium(Storage s, void* f, const std::uint8_t* kind, LevelDims d,

@@ -96,11 +96,14 @@ class LBMSolver:
 
     # ---- lifecycle -------------------------------------------------------
     def init(self, dims, scaling: capi.Scaling, flags: np.ndarray, stream=None, storage: str = "fp32",
-             les_cs: float | None = None, magic_lambda: float | None = None) -> None:
+             les_cs: float | None = None, magic_lambda: float | None = None, kernel: str = "auto") -> None:
+        """kernel: "auto", "cell" (one cell per thread) or "staged" (rows
+        streamed through shared memory by bulk async copies)."""
         flags = np.ascontiguousarray(flags, np.uint8)
         d = capi.Dims(*dims)
         opt = capi.Options(STORE[storage], 0.0 if les_cs is None else (les_cs if les_cs > 0 else -1.0),
-                           0.0 if magic_lambda is None else magic_lambda, 0)
+                           0.0 if magic_lambda is None else magic_lambda, 0,
+                           {"auto": 0, "cell": 1, "staged": 2}[kernel])
         err = C.create_string_buffer(512)
         rc = self._lib.fcfd_init(self._h, C.byref(d), C.byref(scaling), ptr(flags), flags.size, stream,
                                  C.byref(opt), err, 512)

@@ -81,6 +81,11 @@ def airfoil_tunnel(nx=640, ny=192, nz=192, chord=256, aoa=6.0, digits="0012", ma
     if patch:
         m = int(round(margin_chord * chord))
         box = derive_patch_box(dims, flags, m, m, m, m, 3)
+        # Widen the box to a multiple of 4 coarse cells so fine rows are
+        # 16-byte multiples in both storage precisions (bulk-copy staging).
+        extra = (-(box.x1 - box.x0)) % 4
+        grow_right = min(extra, nx - 3 - box.x1)
+        box = Box(box.x0 - (extra - grow_right), box.y0, box.x1 + grow_right, box.y1)
         t.box = box
         fd = t.fine_dims
         ff = np.zeros(int(np.prod(fd)), np.uint8)

@@ -79,6 +79,8 @@ typedef struct fcfd_options {
     float les_cs;       /* Smagorinsky constant                          */
     float magic_lambda; /* TRT magic parameter                           */
     int use_graphs;     /* 1: replay steady-state batches as CUDA graphs */
+    int collide_kernel; /* 0 automatic, 1 one cell per thread, 2 staged
+                           rows (bulk async copies into shared memory) */
 } fcfd_options;
 
 /* Refinement patch in coarse cells, [x0,x1) x [y0,y1) x [0,nz)
@@ -229,7 +231,10 @@ int fcfd_restore_from_macro(fcfd_solver* s, const float* rho, const float* u,
                             const float* v, const float* w);
 /* perfStats (lbm_solver.cpp:1696-1716). */
 int fcfd_perf_stats(const fcfd_solver* s, fcfd_perf* out);
-/* nanDetected / nanDiagnosis (lbm_solver.h:401-404); trip kind in [0, 4]. */
+/* nanDetected / nanDiagnosis (lbm_solver.h:401-404). Kind 1/2: NaN or
+ * velocity runaway on the coarse grid, 3/4 on the fine grid (the reference's
+ * codes), 9: a staged collide's copy wait timed out (the step's results are
+ * incomplete; the solver pauses like on a watchdog trip). */
 int fcfd_nan_detected(fcfd_solver* s);
 int fcfd_nan_kind(fcfd_solver* s);
 

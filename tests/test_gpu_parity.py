@@ -26,9 +26,9 @@ def fc(built_lib):
     return fc
 
 
-def make(fc, dims, flags, tau, u_lat, cs=0.1733, storage="fp32"):
+def make(fc, dims, flags, tau, u_lat, cs=0.1733, storage="fp32", kernel="auto"):
     s = fc.LBMSolver()
-    s.init(dims, fc.scaling_direct(tau, u_lat), flags, storage=storage, les_cs=cs)
+    s.init(dims, fc.scaling_direct(tau, u_lat), flags, storage=storage, les_cs=cs, kernel=kernel)
     s.set_startup_ramp_enabled(False)
     s.reset()
     return s
@@ -54,15 +54,18 @@ def assert_rho_u(f_gpu, f_ref, flags, tol=RHO_U_TOL):
     return er, eu
 
 
+@pytest.mark.parametrize("kernel", ["cell", "staged"])
 @pytest.mark.parametrize("case,steps,flags_key,slip", [
     ("f1", 1, "flags", False), ("f20", 20, "flags", False), ("f20w", 20, "flags", True),
     ("f20z", 20, "flags_z", False)])
-def test_collide_vs_reference_golden(fc, golden, case, steps, flags_key, slip):
+def test_collide_vs_reference_golden(fc, golden, case, steps, flags_key, slip, kernel):
+    """Both collide variants (one cell per thread; rows staged through shared
+    memory by bulk async copies) against the reference's golden vectors."""
     g = golden("collide")
     dims = tuple(int(x) for x in g["dims"])
     tau, lam, cs, u_in = (float(x) for x in g["params"])
     flags = g[flags_key]
-    s = make(fc, dims, flags, tau, u_in, cs)
+    s = make(fc, dims, flags, tau, u_in, cs, kernel=kernel)
     if slip:
         # A wall list must exist for the slip field to be read; install the
         # golden slip field as the level's state.
@@ -308,6 +311,28 @@ def test_fp16_storage_taylor_green_error(fc, oracle_mod):
     r64 = -np.polyfit(t, np.log(ke64), 1)[0]
     print(f"FP16 TG decay rate {r16:.6e} vs FP64 {r64:.6e} ({(r16 / r64 - 1) * 100:.3f} %)")
     assert abs(r16 / r64 - 1) < 5e-3
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_staged_equals_cell_kernel(fc, oracle_mod, storage):
+    """The staged kernel computes the same populations, bit for bit, as the
+    one-cell kernel (same collision body; loads from shared memory instead of
+    global memory) on a wall-modelled airfoil tunnel with a patch."""
+    from foil_cfd_gb300 import tunnels
+    t = tunnels.airfoil_tunnel(nx=160, ny=48, nz=16, chord=64)
+    out = {}
+    for kernel in ("cell", "staged"):
+        s = fc.LBMSolver()
+        s.init(t.dims, fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat), t.flags, storage=storage,
+               les_cs=0.1, kernel=kernel)
+        s.set_wall_model_enabled(True)
+        s.set_startup_ramp_enabled(False)
+        s.reset()
+        s.init_refinement(t.box, 2, t.fine_flags)
+        assert s.step_n(30) == 0
+        out[kernel] = (s.export_f32(), s.export_fine_f32(), s.force_raw())
+    for a, b in zip(out["cell"], out["staged"]):
+        assert np.array_equal(a, b)
 
 
 def test_watchdog_verdicts(fc, oracle_mod):
