@@ -508,17 +508,29 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     const bool staged = p.status && plan.stages >= 2 && p.kernel != 1;
     if (staged) {
         auto kern = wm ? collide_staged_kernel<S, true, EXACT> : collide_staged_kernel<S, false, EXACT>;
-        // Attribute and occupancy are queried once per (kernel, smem size).
+        // The dynamic shared-memory limit is a per-kernel attribute: raise it
+        // once to the device's opt-in maximum (levels of one solver use
+        // different stage sizes); occupancy is cached per (kernel, size).
+        static const void* raised[4] = {};
+        bool isRaised = false;
+        for (const void* k : raised) isRaised |= (k == reinterpret_cast<const void*>(kern));
+        if (!isRaised) {
+            int dev = 0, optin = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            if (static_cast<size_t>(optin) < plan.smem) return cudaErrorInvalidValue;
+            if (auto e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                e != cudaSuccess)
+                return e;
+            for (const void*& k : raised)
+                if (!k) { k = reinterpret_cast<const void*>(kern); break; }
+        }
         struct Entry { const void* k; size_t smem; int perSm; };
         static Entry cache[8] = {};
         int perSm = 0;
         for (const Entry& c : cache)
             if (c.k == reinterpret_cast<const void*>(kern) && c.smem == plan.smem) perSm = c.perSm;
         if (perSm == 0) {
-            if (auto e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(plan.smem));
-                e != cudaSuccess)
-                return e;
             if (auto e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kStagedThreads, plan.smem);
                 e != cudaSuccess)
                 return e;
