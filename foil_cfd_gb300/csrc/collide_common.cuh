@@ -322,14 +322,20 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
 // ---- staged: x-rows through shared memory with bulk async copies -------------
 // A persistent CTA walks rows r = blockIdx.x + k * gridDim.x (r = y + ny z).
 // For every row it needs, per direction q, the full source row (y - c_y,
-// z - c_z) of slice q; one cp.async.bulk per direction brings it into a
-// shared-memory stage and signals the stage's mbarrier (complete_tx). With
-// `stages` stages the copies of the next rows are in flight while the current
-// row is computed, so the bytes in flight no longer depend on resident warps.
-// Bulk fluid cells read their 19 pulls from the stage (x - c_x wraps inside
-// the row); wall-adjacent and boundary cells use the global-memory paths.
-// Requires rows of a multiple of 16 bytes (bulk-copy alignment).
-constexpr int kStagedThreads = 320;
+// z - c_z) of slice q, plus the row's kind bytes. A producer warp brings them
+// into a ring of shared-memory stages with one cp.async.bulk per row piece,
+// each completing on the stage's "full" mbarrier (complete_tx); consumer
+// warps wait on "full", compute their cells of the row, and release the stage
+// on its "empty" mbarrier (one arrive per warp). There is no block-wide
+// barrier per row: warps drift by up to the ring depth, and the bytes in
+// flight are set by the ring, not by resident warps. Bulk fluid cells read
+// their 19 pulls from the stage (x - c_x wraps inside the row); wall-adjacent
+// and boundary cells use the global-memory paths. Requires rows of a
+// multiple of 16 bytes. Every wait is bounded: on a timeout the kernel sets
+// *status, lets its copies in flight land (bounded) and returns.
+constexpr int kConsumerWarps = 15;
+constexpr int kStagedThreads = (kConsumerWarps + 1) * 32;
+constexpr int kMaxStages = 8;
 constexpr long long kWaitLimit = 1LL << 22; // try_wait polls before a timeout
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
@@ -342,6 +348,9 @@ __device__ __forceinline__ void mbar_expect_tx(std::uint64_t* bar, unsigned byte
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -353,7 +362,7 @@ __device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parit
         : "memory");
     return ok != 0;
 }
-/// Bounded wait on a stage barrier; false when the limit ran out.
+/// Bounded wait on a barrier phase; false when the limit ran out.
 __device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, unsigned parity) {
     for (long long i = 0; i < kWaitLimit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
@@ -367,68 +376,111 @@ __device__ __forceinline__ void bulk_g2s(void* dstSmem, const void* srcGlobal, u
         : "memory");
 }
 
+/// Shared-memory layout of the ring.
+struct StageLayout {
+    unsigned kindBytes;  // per stage, 16-byte multiple (row bytes + alignment prefix)
+    unsigned popBytes;   // per stage: 19 rows
+    __host__ __device__ static unsigned header() { return 256; }
+};
+
 template <class S>
-__device__ __forceinline__ void issue_row(const typename S::T* __restrict__ src, typename S::T* stage,
-                                          std::uint64_t* bar, long long row, const CollideArgs& a) {
+__host__ __device__ inline StageLayout stage_layout(int nx) {
+    StageLayout l;
+    l.kindBytes = static_cast<unsigned>(((nx + 15 + 15) / 16) * 16);
+    l.popBytes = static_cast<unsigned>(kQ) * static_cast<unsigned>(nx) * sizeof(typename S::T);
+    return l;
+}
+
+template <class S>
+__device__ __forceinline__ void issue_row(const typename S::T* __restrict__ src,
+                                          const std::uint8_t* __restrict__ kind, unsigned char* kstage,
+                                          typename S::T* pstage, std::uint64_t* bar, long long row,
+                                          const CollideArgs& a, unsigned kindBytes) {
     using T = typename S::T;
     const int y = static_cast<int>(row % a.ny), z = static_cast<int>(row / a.ny);
     const unsigned rowBytes = static_cast<unsigned>(a.nx) * sizeof(T);
-    mbar_expect_tx(bar, rowBytes * kQ);
+    // Kind row: copy from the 16-byte boundary at or below its start.
+    const long long kstart = row * static_cast<long long>(a.nx);
+    const long long kal = kstart & ~15LL;
+    const unsigned kb = static_cast<unsigned>(((kstart - kal + a.nx + 15) / 16) * 16);
+    mbar_expect_tx(bar, rowBytes * kQ + kb);
+    bulk_g2s(kstage, kind + kal, kb, bar);
 #pragma unroll
     for (int q = 0; q < kQ; ++q) {
         int ys = y - cy(q), zs = z - cz(q);
         ys = ys < 0 ? ys + a.ny : (ys >= a.ny ? ys - a.ny : ys);
         zs = zs < 0 ? zs + a.nz : (zs >= a.nz ? zs - a.nz : zs);
         const T* g = src + q * a.n + static_cast<long long>(a.nx) * (ys + static_cast<long long>(a.ny) * zs);
-        bulk_g2s(stage + q * a.nx, g, rowBytes, bar);
+        bulk_g2s(pstage + q * a.nx, g, rowBytes, bar);
     }
+    (void)kindBytes;
 }
 
 template <class S, bool WM, bool EXACT>
-__global__ void __launch_bounds__(kStagedThreads)
+__global__ void __launch_bounds__(kStagedThreads, 1)
 collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                       const std::uint8_t* __restrict__ kind, CollideArgs a, int stages) {
     using T = typename S::T;
     extern __shared__ __align__(128) unsigned char smem[];
-    std::uint64_t* bars = reinterpret_cast<std::uint64_t*>(smem);
-    T* buf = reinterpret_cast<T*>(smem + 128);
+    std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem);
+    std::uint64_t* empty = full + kMaxStages;
+    const StageLayout L = stage_layout<S>(a.nx);
+    unsigned char* kring = smem + StageLayout::header();
+    T* pring = reinterpret_cast<T*>(kring + static_cast<size_t>(L.kindBytes) * stages);
     const long long rows = static_cast<long long>(a.ny) * a.nz;
     const long long G = gridDim.x;
     const int nx = a.nx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t stageElems = static_cast<size_t>(kQ) * nx;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < stages; ++s) mbar_init(&bars[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         for (int s = 0; s < stages; ++s) {
-            const long long r = blockIdx.x + s * G;
-            if (r < rows) issue_row<S>(src, buf + s * stageElems, &bars[s], r, a);
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
         }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
+    if (warp == kConsumerWarps) {
+        // ---- producer warp: one lane issues every copy ----
+        if (lane == 0) {
+            long long k = 0;
+            for (;; ++k) {
+                const long long r = blockIdx.x + k * G;
+                if (r >= rows) break;
+                const int s = static_cast<int>(k % stages);
+                if (k >= stages && !mbar_wait(&empty[s], static_cast<unsigned>(((k / stages) - 1) & 1))) {
+                    atomicExch(a.status, 1);
+                    break;
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_row<S>(src, kind, kring + static_cast<size_t>(L.kindBytes) * s, pring + stageElems * s,
+                             &full[s], r, a, L.kindBytes);
+            }
+            // Let every copy this CTA issued land before the CTA can exit.
+            for (long long j = k - stages; j < k; ++j)
+                if (j >= 0) (void)mbar_wait(&full[j % stages], static_cast<unsigned>((j / stages) & 1));
+        }
+        return;
+    }
+
+    // ---- consumer warps ----
     for (long long k = 0;; ++k) {
         const long long r = blockIdx.x + k * G;
         if (r >= rows) break;
         const int s = static_cast<int>(k % stages);
-        // Bounded wait, decided for the whole block at once.
-        const int landed = __syncthreads_and(mbar_wait(&bars[s], static_cast<unsigned>((k / stages) & 1)) ? 1 : 0);
-        if (!landed) {
-            // Copies did not land within the limit: report, let the copies
-            // still in flight for this CTA finish (bounded), and stop.
-            if (threadIdx.x == 0) {
-                atomicExch(a.status, 1);
-                for (long long j = k; j < k + stages; ++j)
-                    if (blockIdx.x + j * G < rows)
-                        (void)mbar_wait(&bars[j % stages], static_cast<unsigned>((j / stages) & 1));
-            }
+        if (!mbar_wait(&full[s], static_cast<unsigned>((k / stages) & 1))) {
+            atomicExch(a.status, 1);
             break;
         }
-        const T* st = buf + s * stageElems;
+        const T* st = pring + stageElems * s;
+        const long long kstart = r * static_cast<long long>(nx);
+        const std::uint8_t* krow = kring + static_cast<size_t>(L.kindBytes) * s + (kstart & 15);
         const int y = static_cast<int>(r % a.ny), z = static_cast<int>(r / a.ny);
-        for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+        for (int x = warp * 32 + lane; x < nx; x += kConsumerWarps * 32) {
             const unsigned cell = static_cast<unsigned>(x) + static_cast<unsigned>(nx) * static_cast<unsigned>(r);
-            const std::uint8_t kb = __ldg(kind + cell);
+            const std::uint8_t kb = krow[x];
             const int flag = kb & kFlagMask;
             if (flag != kFluid) {
                 boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
@@ -445,12 +497,8 @@ collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __re
             }
             finish_cell<S, EXACT>(dst, a, cell, f);
         }
-        __syncthreads(); // every thread is done reading stage s
-        const long long rn = r + stages * G;
-        if (threadIdx.x == 0 && rn < rows) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_row<S>(src, buf + s * stageElems, &bars[s], rn, a);
-        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
     }
 }
 
@@ -465,16 +513,14 @@ StagedPlan staged_plan(LevelDims d) {
     StagedPlan p;
     const size_t rowBytes = static_cast<size_t>(d.nx) * sizeof(typename S::T);
     if (rowBytes % 16 != 0 || d.nx < 8) return p;
-    const size_t stageBytes = rowBytes * kQ;
-    // Two CTAs per SM when they fit (<= 113 KB each), else one (<= 227 KB).
-    for (size_t budget : {size_t(113 * 1024), size_t(227 * 1024)}) {
-        const long long st = static_cast<long long>((budget - 128) / stageBytes);
-        if (st >= 2) {
-            p.stages = static_cast<int>(st > 4 ? 4 : st);
-            p.smem = 128 + stageBytes * static_cast<size_t>(p.stages);
-            return p;
-        }
-    }
+    const StageLayout L = stage_layout<S>(d.nx);
+    const size_t stageBytes = static_cast<size_t>(L.kindBytes) + L.popBytes;
+    // One CTA per SM with as deep a ring as 227 KB allows (2..8 stages).
+    const size_t budget = 227 * 1024 - StageLayout::header();
+    const long long st = static_cast<long long>(budget / stageBytes);
+    if (st < 2) return p;
+    p.stages = static_cast<int>(st > kMaxStages ? kMaxStages : st);
+    p.smem = StageLayout::header() + stageBytes * static_cast<size_t>(p.stages);
     return p;
 }
 

@@ -242,7 +242,9 @@ struct fcfd_solver {
         for (void*& p : L.f)
             if (auto e = cudaMalloc(&p, fb); e != cudaSuccess) return e;
         if (auto e = dalloc(&L.flags, static_cast<size_t>(L.n)); e != cudaSuccess) return e;
-        if (auto e = dalloc(&L.kind, static_cast<size_t>(L.n)); e != cudaSuccess) return e;
+        // Kind bytes are fetched in 16-byte-aligned row copies that may run
+        // up to 31 bytes past the last row: pad the allocation.
+        if (auto e = dalloc(&L.kind, static_cast<size_t>(L.n) + 64); e != cudaSuccess) return e;
         return cudaSuccess;
     }
 
