@@ -466,6 +466,10 @@ collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __re
     }
 
     // ---- consumer warps ----
+    // Row k is cut into 32-cell chunks; chunk j goes to warp
+    // (j + k * nchunks) mod W, so the assignment rotates from row to row and
+    // every warp does the same work over a few rows.
+    const int nchunks = (nx + 31) / 32;
     for (long long k = 0;; ++k) {
         const long long r = blockIdx.x + k * G;
         if (r >= rows) break;
@@ -474,13 +478,19 @@ collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __re
             atomicExch(a.status, 1);
             break;
         }
-        const T* st = pring + stageElems * s;
+        const unsigned sbase = smem_addr(pring + stageElems * s);
         const long long kstart = r * static_cast<long long>(nx);
-        const std::uint8_t* krow = kring + static_cast<size_t>(L.kindBytes) * s + (kstart & 15);
+        const unsigned kbase = smem_addr(kring + static_cast<size_t>(L.kindBytes) * s) + static_cast<unsigned>(kstart & 15);
         const int y = static_cast<int>(r % a.ny), z = static_cast<int>(r / a.ny);
-        for (int x = warp * 32 + lane; x < nx; x += kConsumerWarps * 32) {
+        const int j0 = static_cast<int>(((warp - (k * nchunks) % kConsumerWarps) % kConsumerWarps + kConsumerWarps)
+                                        % kConsumerWarps);
+        for (int j = j0; j < nchunks; j += kConsumerWarps) {
+            const int x = j * 32 + lane;
+            if (x >= nx) continue;
             const unsigned cell = static_cast<unsigned>(x) + static_cast<unsigned>(nx) * static_cast<unsigned>(r);
-            const std::uint8_t kb = krow[x];
+            unsigned short kb16;
+            asm volatile("ld.shared.u8 %0, [%1];" : "=h"(kb16) : "r"(kbase + static_cast<unsigned>(x)));
+            const std::uint8_t kb = static_cast<std::uint8_t>(kb16);
             const int flag = kb & kFlagMask;
             if (flag != kFluid) {
                 boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
@@ -489,8 +499,9 @@ collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __re
             float f[kQ];
             if (!(kb & kNearWall)) {
                 const int xs[3] = {wrap_inc(x, nx), x, wrap_dec(x, nx)};
+                const unsigned rowBytes = static_cast<unsigned>(nx) * sizeof(T);
 #pragma unroll
-                for (int q = 0; q < kQ; ++q) f[q] = S::lds(st + q * nx, xs[1 + cx(q)], wgt(q));
+                for (int q = 0; q < kQ; ++q) f[q] = S::lds(sbase + q * rowBytes, xs[1 + cx(q)], wgt(q));
             } else {
                 const Nbr b = neighbours(x, y, z, nx, a.ny, a.nz);
                 gather_wall<S, WM>(src, kind, a, b, cell, y, z, f);

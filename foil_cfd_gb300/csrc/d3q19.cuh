@@ -117,8 +117,12 @@ struct StoreF32 {
     __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float) {
         p[i] = v;
     }
-    /// Load from a shared-memory stage.
-    __device__ __forceinline__ static float lds(const T* p, int i, float) { return p[i]; }
+    /// Load element i of a shared-memory row at shared address `row`.
+    __device__ __forceinline__ static float lds(unsigned row, int i, float) {
+        float v;
+        asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(row + 4u * static_cast<unsigned>(i)));
+        return v;
+    }
 };
 struct StoreF16 {
     using T = __half;
@@ -129,7 +133,11 @@ struct StoreF16 {
     __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float w) {
         p[i] = __float2half_rn(v - w);
     }
-    __device__ __forceinline__ static float lds(const T* p, int i, float w) { return w + __half2float(p[i]); }
+    __device__ __forceinline__ static float lds(unsigned row, int i, float w) {
+        unsigned short h;
+        asm volatile("ld.shared.u16 %0, [%1];" : "=h"(h) : "r"(row + 2u * static_cast<unsigned>(i)));
+        return w + __half2float(__ushort_as_half(h));
+    }
 };
 
 // ---- helpers ---------------------------------------------------------------
