@@ -336,7 +336,7 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
 constexpr int kConsumerWarps = 15;
 constexpr int kStagedThreads = (kConsumerWarps + 1) * 32;
 constexpr int kMaxStages = 8;
-constexpr long long kWaitLimit = 1LL << 22; // try_wait polls before a timeout
+constexpr long long kWaitLimit = 1LL << 18; // try_wait polls (each may sleep ~20 us) before a timeout
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -352,13 +352,15 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parity) {
+    // The suspend-time hint (ns) lets a waiting warp sleep until the phase
+    // completes instead of re-polling and taking issue slots.
     unsigned ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(20000u)
         : "memory");
     return ok != 0;
 }
@@ -417,7 +419,7 @@ __device__ __forceinline__ void issue_row(const typename S::T* __restrict__ src,
 }
 
 template <class S, bool WM, bool EXACT>
-__global__ void __launch_bounds__(kStagedThreads, 1)
+__global__ void __launch_bounds__(kStagedThreads, 2)
 collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                       const std::uint8_t* __restrict__ kind, CollideArgs a, int stages) {
     using T = typename S::T;
@@ -526,8 +528,9 @@ StagedPlan staged_plan(LevelDims d) {
     if (rowBytes % 16 != 0 || d.nx < 8) return p;
     const StageLayout L = stage_layout<S>(d.nx);
     const size_t stageBytes = static_cast<size_t>(L.kindBytes) + L.popBytes;
-    // One CTA per SM with as deep a ring as 227 KB allows (2..8 stages).
-    const size_t budget = 227 * 1024 - StageLayout::header();
+    // Two CTAs per SM (113 KB each), each with as deep a ring as fits
+    // (2..8 stages).
+    const size_t budget = 113 * 1024 - StageLayout::header();
     const long long st = static_cast<long long>(budget / stageBytes);
     if (st < 2) return p;
     p.stages = static_cast<int>(st > kMaxStages ? kMaxStages : st);
