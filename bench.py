@@ -57,11 +57,14 @@ def workload(small: bool):
     return tunnels.airfoil_tunnel()
 
 
+COLLIDE_KERNEL = "auto"
+
+
 def make_solver(t, storage: str):
     import foil_cfd_gb300 as fc
     s = fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat)
     sol = fc.LBMSolver()
-    sol.init(t.dims, s, t.flags, storage=storage, les_cs=0.1)
+    sol.init(t.dims, s, t.flags, storage=storage, les_cs=0.1, kernel=COLLIDE_KERNEL)
     sol.set_wall_model_enabled(True)
     sol.set_startup_ramp_enabled(False)
     sol.reset()
@@ -271,7 +274,11 @@ def main():
     ap.add_argument("--no-fp16", action="store_true")
     ap.add_argument("--only-fp16", action="store_true", help="measure the FP16-storage solver only")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
+                    help="collide kernel variant")
     args = ap.parse_args()
+    global COLLIDE_KERNEL
+    COLLIDE_KERNEL = args.kernel
     warmup = max(args.warmup, 3)
     dist, rank, ws = dist_setup()
     t = workload(args.small)

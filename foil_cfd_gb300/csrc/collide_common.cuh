@@ -565,7 +565,11 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     T* dst = static_cast<T*>(dstv);
     const bool wm = slip.active();
     const StagedPlan plan = staged_plan<S>(d);
-    const bool staged = p.status && plan.stages >= 2 && p.kernel != 1;
+    // Automatic selection takes the one-cell kernel: on a GB300 the staged
+    // ring measured slower (1.43-1.57 ms vs 0.89 ms per FP32 collide launch
+    // on the 640x192x192 airfoil tunnel), its consumer warps being issue-bound
+    // on shared-memory reads and ring bookkeeping.
+    const bool staged = p.status && plan.stages >= 2 && p.kernel == 2;
     if (staged) {
         auto kern = wm ? collide_staged_kernel<S, true, EXACT> : collide_staged_kernel<S, false, EXACT>;
         // The dynamic shared-memory limit is a per-kernel attribute: raise it

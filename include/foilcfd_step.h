@@ -79,8 +79,9 @@ typedef struct fcfd_options {
     float les_cs;       /* Smagorinsky constant                          */
     float magic_lambda; /* TRT magic parameter                           */
     int use_graphs;     /* 1: replay steady-state batches as CUDA graphs */
-    int collide_kernel; /* 0 automatic, 1 one cell per thread, 2 staged
-                           rows (bulk async copies into shared memory) */
+    int collide_kernel; /* 0 automatic (= 1), 1 one cell per thread,
+                           2 staged rows (bulk async copies into shared
+                           memory; slower on GB300, kept selectable) */
 } fcfd_options;
 
 /* Refinement patch in coarse cells, [x0,x1) x [y0,y1) x [0,nz)
