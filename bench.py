@@ -215,6 +215,75 @@ def e2e(t, res, steps):
             "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps)}
 
 
+def wall_seed_leg(sol, t, epochs=150, n_harvest=2_000_000, n_synth=1_000_000, batch=2048, lr_max=3e-3):
+    """Learned u_tau seed: harvested (NACA 0012 tunnels at 0-12 deg, coarse +
+    patch wall cells) and synthetic samples, labelled by FP64 Newton, trained
+    on the GPU; then, on this tunnel's own wall cells (held out: another
+    resolution and angle), the seed's error against the FP64 Newton judge and
+    the wall-update time of each u_tau solve."""
+    import torch
+    from foil_cfd_gb300 import wallnet as wn
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ut, ys, nu, tau = wn.training_set(n_harvest, n_synth, seed=0)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    net, hist = wn.train_wallnet(ut, ys, nu, tau, epochs=epochs, batch=batch, lr_max=lr_max, seed=0)
+    t_train = time.perf_counter() - t0
+    out = {"network": "3-32-32-1 tanh, BF16 weights, FP32 accumulate; inputs log u_par, log y, log nu",
+           "samples": {"harvested": n_harvest, "synthetic": n_synth, "seconds": round(t_data, 2)},
+           "train": {"epochs": epochs, "batch": batch, "lr_max": lr_max, "seconds": round(t_train, 2),
+                     "final_loss": float(hist[-1])}}
+    import foil_cfd_gb300 as fc
+    sc = fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat)
+    for level, name in ((0, "coarse"), (1, "fine")):
+        cnt = sol.wall_count(level)
+        if cnt <= 0:
+            continue
+        nu_l = (sc.tau - 0.5) / 3.0 * (1 if level == 0 else t.factor)
+        ub = torch.empty(cnt, device="cuda")
+        yb = torch.empty(cnt, device="cuda")
+        sol.wall_harvest(level, ub.data_ptr(), yb.data_ptr(), cnt)
+        keep = ub > 0
+        u_, y_ = ub[keep].contiguous(), yb[keep].contiguous()
+        n_ = torch.full_like(u_, nu_l)
+        judge, sj = wn.utau_solve(wn.NEWTON64, u_, y_, n_)
+        lrn, sl = wn.utau_solve(wn.LEARNED, u_, y_, n_, net=net)
+        ref6, _ = wn.utau_solve(wn.REFERENCE, u_, y_, n_)
+        seed = net.predict(u_, y_, n_)
+        _, sn = wn.utau_solve(wn.NEWTON64_NET, u_, y_, n_, net=net)
+        j = judge.double()
+
+        def err(x):
+            e = ((x.double() - j).abs() / j).cpu().numpy()
+            return {"max": float(e.max()), "median": float(np.median(e)), "p99": float(np.percentile(e, 99))}
+
+        lev = {"wall_cells": int(cnt), "active": int(u_.numel()),
+               "seed_error_vs_fp64_newton": err(seed), "learned_error_vs_fp64_newton": err(lrn),
+               "reference_6iter_fresh_seed_error": err(ref6),
+               "fallback_frac": round(sl["fallbacks"] / max(sl["solved"], 1), 5),
+               "fp64_newton_iters_per_cell": {"reference_seed": round(sj["newton_iterations"] / max(sj["solved"], 1), 3),
+                                              "network_seed": round(sn["newton_iterations"] / max(sn["solved"], 1), 3)}}
+        utau0, slip0 = sol.export_wall_state(level)
+        times = {}
+        for method, key in ((wn.REFERENCE, "reference_fp32_6iter"), (wn.NEWTON64, "full_newton_fp64"),
+                            (wn.LEARNED, "learned")):
+            sol.import_wall_state(level, utau0, slip0)
+            sol.set_wall_solver(method, net if method == wn.LEARNED else None)
+            sol.wall_update_timed(level, 3)
+            sol.import_wall_state(level, utau0, slip0)
+            ms, st = sol.wall_update_timed(level, 20)
+            times[key] = round(ms, 5)
+        sol.import_wall_state(level, utau0, slip0)
+        sol.set_wall_solver(wn.REFERENCE)
+        lev["wall_update_ms"] = times
+        lev["speedup_learned_vs_full_newton"] = round(times["full_newton_fp64"] / times["learned"], 2)
+        out[name] = lev
+    net.close()
+    return out
+
+
 def cpu_host():
     try:
         model = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -274,6 +343,7 @@ def main():
     ap.add_argument("--no-fp16", action="store_true")
     ap.add_argument("--only-fp16", action="store_true", help="measure the FP16-storage solver only")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-wallnet", action="store_true", help="skip the learned wall-seed leg")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
     args = ap.parse_args()
@@ -329,6 +399,8 @@ def main():
             "gpu_launches": int(r32["launches"]), "clocks": r32["clocks"],
             "force_lattice": r32["force"], "nan": bool(r32["nan"])}
     line["e2e"] = e2e(t, r32, args.steps)
+    if not args.no_wallnet and ws == 1:
+        line["wall_seed"] = wall_seed_leg(r32["solver"], t)
     r32["solver"] = None
     del r32
     if not args.no_fp16:

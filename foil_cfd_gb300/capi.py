@@ -1,4 +1,5 @@
-"""ctypes binding of include/foilcfd_step.h (the solver step's C ABI).
+"""ctypes binding of include/foilcfd_step.h (the solver step's C ABI) and
+include/foilcfd_wallnet.h (the learned u_tau seed).
 
 Loading fails loudly when the compiled library is missing: there is no CPU
 fallback for the solver step. Build it with ``foil_cfd_gb300.build_lib``
@@ -51,6 +52,20 @@ class Perf(C.Structure):
 class RefineInfo(C.Structure):
     _fields_ = [("active", C.c_int), ("factor", C.c_int), ("box", PatchBox), ("fine_dims", Dims),
                 ("forces_from_fine", C.c_int), ("vram_bytes", C.c_double)]
+
+
+class WallNetNorm(C.Structure):
+    _fields_ = [("in_mean", C.c_float * 3), ("in_std", C.c_float * 3), ("out_mean", C.c_float),
+                ("out_std", C.c_float)]
+
+
+class TrainOpts(C.Structure):
+    _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr_max", C.c_float), ("warmup_frac", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float), ("seed", C.c_ulonglong)]
+
+
+class UtauStats(C.Structure):
+    _fields_ = [("solved", C.c_int), ("fallbacks", C.c_int), ("newton_iterations", C.c_longlong)]
 
 
 P = C.c_void_p
@@ -117,13 +132,27 @@ _SIGS = {
     "fcfd_host_alloc": (P, [C.c_size_t]),
     "fcfd_host_free": (None, [P]),
     "fcfd_version": (C.c_char_p, []),
+    # include/foilcfd_wallnet.h
+    "fcfd_wallnet_create": (P, []),
+    "fcfd_wallnet_destroy": (None, [P]),
+    "fcfd_wallnet_init_params": (C.c_int, [P, C.c_ulonglong]),
+    "fcfd_wallnet_set_params": (C.c_int, [P, P, C.POINTER(WallNetNorm)]),
+    "fcfd_wallnet_get_params": (C.c_int, [P, P, P, C.POINTER(WallNetNorm)]),
+    "fcfd_wallnet_fit_norm": (C.c_int, [P, P, P, P, P, C.c_int, P]),
+    "fcfd_wallnet_gradient": (C.c_int, [P, P, P, P, P, C.c_int, C.POINTER(C.c_double), P, P]),
+    "fcfd_wallnet_train": (C.c_int, [P, P, P, P, P, C.c_int, C.POINTER(TrainOpts), P, P]),
+    "fcfd_wallnet_predict": (C.c_int, [P, P, P, P, P, C.c_int, P]),
+    "fcfd_utau_solve": (C.c_int, [C.c_int, P, P, P, P, P, P, C.c_int, C.POINTER(UtauStats), P]),
+    "fcfd_set_wall_solver": (C.c_int, [P, C.c_int, P]),
+    "fcfd_wall_harvest": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(C.c_int)]),
+    "fcfd_wall_update_timed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(UtauStats)]),
 }
 
 _lib = None
 
 
 def declared_symbols():
-    """Every function name include/foilcfd_step.h declares."""
+    """Every function name the headers in include/ declare."""
     return list(_SIGS)
 
 

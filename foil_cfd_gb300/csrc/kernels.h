@@ -7,6 +7,10 @@
 #include <cstdint>
 #include <cuda_runtime_api.h>
 
+#include "wallnet_types.h"
+
+struct fcfd_wallnet;
+
 #ifdef __CUDACC__
 #define FCFD_HD __host__ __device__
 #else
@@ -107,12 +111,26 @@ struct WallStatsDev {
     int maxYplusBits;
     int activeCells;
     int clampedCells;
+    int fallbackCells;            // learned u_tau solve: FP64 fallbacks
+    int pad;
+    unsigned long long newtonIters; // FP64 Newton iterations summed
 };
+/// u_tau solve of a wall update: the FCFD_UTAU_* values of
+/// include/foilcfd_wallnet.h (0 reference, 1 FP64 Newton, 2 learned).
+/// `net` is the device view of a learned seed (BF16 weights + normalisation),
+/// required by the learned method.
 cudaError_t launch_wall_update(Storage s, const void* f, long long cells,
                                WallListDev list, std::uint16_t* uwx,
                                std::uint16_t* uwy, std::uint16_t* uwz,
                                float nuLat, float utCutoff, float emaAlpha,
-                               WallStatsDev* stats, cudaStream_t st);
+                               WallStatsDev* stats, cudaStream_t st,
+                               int method = 0, const wallnet::NetDev* net = nullptr);
+/// Device view (BF16 weights + normalisation) of a learned seed network.
+wallnet::NetDev wallnet_view(const fcfd_wallnet* net);
+/// Sampled tangential speed (0 below the cut-off) and sample distance of
+/// every wall-list entry.
+cudaError_t launch_wall_harvest(Storage s, const void* f, long long cells, WallListDev list,
+                                float utCutoff, float* utOut, float* ysOut, cudaStream_t st);
 
 // ---- refinement (refine_kernels.cu) ----------------------------------------
 struct RefineGeom {

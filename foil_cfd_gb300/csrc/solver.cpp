@@ -8,6 +8,7 @@
 // 200 steps. Buffers are unpadded (periodic wrap lives in the kernels), so
 // there is no ghost-plane refresh anywhere in the loop.
 #include "../../include/foilcfd_step.h"
+#include "../../include/foilcfd_wallnet.h"
 #include "host_geom.h"
 #include "kernels.h"
 
@@ -172,6 +173,9 @@ struct fcfd_solver {
     int nanKind = 0;
     bool wmEnabled = false;
     bool zSlipWalls = false;
+    int wallMethod = 0;                 // FCFD_UTAU_* solve of the wall updates
+    std::uint16_t* dNetW = nullptr;     // learned seed: solver-owned BF16 weights
+    wallnet::NetDev netView{};
 
     // ---- diagnostics ----
     long long launches = 0;
@@ -383,6 +387,9 @@ struct fcfd_solver {
         freeFine();
         coarse.free_all();
         dfree(rho); dfree(u); dfree(v); dfree(w); dfree(dForce); dfree(dNan); dfree(dStatus);
+        dfree(dNetW);
+        wallMethod = 0;
+        netView = wallnet::NetDev{};
         if (hForce) { cudaFreeHost(hForce); hForce = nullptr; }
         if (hNan) { cudaFreeHost(hNan); hNan = nullptr; }
         for (cudaEvent_t* e : {&evT0, &evT1, &evForce, &evNan})
@@ -435,7 +442,8 @@ struct fcfd_solver {
         if (!L.wm.active) return cudaSuccess;
         ++launches;
         return launch_wall_update(storage, L.f[L.src], L.n, L.wm.list(), L.wm.dUwx, L.wm.dUwy,
-                                  L.wm.dUwz, nu, 1e-3f * scaling.u_lat, kWallEma, L.wm.dStats, stream);
+                                  L.wm.dUwz, nu, 1e-3f * scaling.u_lat, kWallEma, L.wm.dStats, stream,
+                                  wallMethod, &netView);
     }
 
     int stepN(int n) {
@@ -1030,7 +1038,8 @@ int fcfd_wall_update_now(fcfd_solver* s, int level, float nu, float cut) {
     if (!L || !L->wm.active) return cudaErrorInvalidValue;
     ++s->launches;
     if (auto e = launch_wall_update(s->storage, L->f[L->src], L->n, L->wm.list(), L->wm.dUwx, L->wm.dUwy,
-                                    L->wm.dUwz, nu, cut, kWallEma, L->wm.dStats, s->stream);
+                                    L->wm.dUwz, nu, cut, kWallEma, L->wm.dStats, s->stream, s->wallMethod,
+                                    &s->netView);
         e != cudaSuccess)
         return e;
     return cudaStreamSynchronize(s->stream);
@@ -1280,3 +1289,66 @@ void fcfd_host_free(void* p) {
 const char* fcfd_version(void) { return "foilcfd-gb300 0.1 (sm_103a)"; }
 
 } // extern "C"
+
+// ---- learned u_tau seed: solver side (include/foilcfd_wallnet.h) ----------
+
+int fcfd_set_wall_solver(fcfd_solver* s, int method, const fcfd_wallnet* net) {
+    if (!s || !s->initialized) return cudaErrorNotReady;
+    if (method != FCFD_UTAU_REFERENCE && method != FCFD_UTAU_NEWTON64 && method != FCFD_UTAU_LEARNED)
+        return cudaErrorInvalidValue;
+    if (method == FCFD_UTAU_LEARNED) {
+        if (!net) return cudaErrorInvalidValue;
+        const wallnet::NetDev v = wallnet_view(net);
+        if (!v.w) return cudaErrorInvalidValue;
+        if (!s->dNetW)
+            if (auto e = dalloc(&s->dNetW, wallnet::kParams * 2); e != cudaSuccess) return e;
+        if (auto e = cudaMemcpyAsync(s->dNetW, v.w, wallnet::kParams * 2, cudaMemcpyDeviceToDevice, s->stream);
+            e != cudaSuccess)
+            return e;
+        s->netView.w = s->dNetW;
+        s->netView.norm = v.norm;
+    }
+    s->wallMethod = method;
+    return cudaStreamSynchronize(s->stream);
+}
+
+int fcfd_wall_harvest(fcfd_solver* s, int level, float* ut, float* ys, int capacity, int* count) {
+    Level* L = level_of(s, level);
+    if (!L || !L->wm.active || !ut || !ys || capacity < L->wm.count) return cudaErrorInvalidValue;
+    if (auto e = launch_wall_harvest(s->storage, L->f[L->src], L->n, L->wm.list(), 1e-3f * s->scaling.u_lat, ut,
+                                     ys, s->stream);
+        e != cudaSuccess)
+        return e;
+    if (count) *count = L->wm.count;
+    return cudaStreamSynchronize(s->stream);
+}
+
+int fcfd_wall_update_timed(fcfd_solver* s, int level, int reps, float* ms, fcfd_utau_stats* stats) {
+    Level* L = level_of(s, level);
+    if (!L || !L->wm.active || reps <= 0) return cudaErrorInvalidValue;
+    const float tc = s->effTau();
+    const float tau = level == 0 ? tc : fcfd_solver::fineTau(tc, s->factor);
+    const float nu = (tau - 0.5f) / 3.0f;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s->stream);
+    cudaError_t e = cudaSuccess;
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = s->wallUpdate(*L, nu);
+    cudaEventRecord(b, s->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float t = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) return e;
+    if (ms) *ms = t / static_cast<float>(reps);
+    if (stats) {
+        WallStatsDev st{};
+        if (auto e2 = cudaMemcpy(&st, L->wm.dStats, sizeof st, cudaMemcpyDeviceToHost); e2 != cudaSuccess) return e2;
+        stats->solved = st.activeCells;
+        stats->fallbacks = st.fallbackCells;
+        stats->newton_iterations = static_cast<long long>(st.newtonIters);
+    }
+    return 0;
+}

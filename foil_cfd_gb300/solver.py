@@ -257,6 +257,30 @@ class LBMSolver:
         if rc:
             raise SolverError(f"wall update failed ({rc})")
 
+    def set_wall_solver(self, method: int, net=None):
+        """u_tau solve of the wall updates: 0 the reference's, 1 full FP64
+        Newton, 2 the learned seed (net: a foil_cfd_gb300.wallnet.WallNet)."""
+        rc = self._lib.fcfd_set_wall_solver(self._h, int(method), None if net is None else net.handle)
+        if rc:
+            raise SolverError(f"wall solver selection failed ({rc})")
+
+    def wall_harvest(self, level: int, ut_ptr: int, ys_ptr: int, capacity: int) -> int:
+        """(u_par, y) of each wall entry into device buffers; returns the count."""
+        cnt = C.c_int()
+        rc = self._lib.fcfd_wall_harvest(self._h, level, ut_ptr, ys_ptr, capacity, C.byref(cnt))
+        if rc:
+            raise SolverError(f"wall harvest failed ({rc})")
+        return cnt.value
+
+    def wall_update_timed(self, level: int, reps: int):
+        """(mean ms per wall update, stats) of `reps` back-to-back updates."""
+        ms = C.c_float()
+        st = capi.UtauStats()
+        rc = self._lib.fcfd_wall_update_timed(self._h, level, reps, C.byref(ms), C.byref(st))
+        if rc:
+            raise SolverError(f"timed wall update failed ({rc})")
+        return ms.value, {"solved": st.solved, "fallbacks": st.fallbacks, "newton_iterations": st.newton_iterations}
+
     # ---- refinement ------------------------------------------------------
     def init_refinement(self, box: Box, factor: int, fine_flags) -> None:
         ff = np.ascontiguousarray(fine_flags, np.uint8)
