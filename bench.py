@@ -284,6 +284,67 @@ def wall_seed_leg(sol, t, epochs=150, n_harvest=2_000_000, n_synth=1_000_000, ba
     return out
 
 
+def polar_leg(steps=10000, seq_steps=2000, trial_steps=10):
+    """Batched polar: 24 NACA 4-digit tunnels of uneven size in one launch per
+    step (FP16 storage, graph-replayed chunks, autotuned shape) from a uniform
+    start; against 24 sequential single-tunnel FP32 runs (the drop-in)."""
+    import foil_cfd_gb300 as fc
+    from foil_cfd_gb300 import batch
+    tunnels = batch.polar_tunnels()
+    upd = float(sum(t.cells for t in tunnels))
+    out = {"tunnels": len(tunnels), "cells": int(upd), "steps": steps,
+           "sections": "NACA 0012/2412/4412, -4..16 deg by 2.5 (first 24), chord 96-192 cells, 2.5 x 1.5 chords, "
+                       "span 16 periodic"}
+    res = {}
+    for storage in ("fp16", "fp32"):
+        b = batch.BatchSolver()
+        b.init(tunnels, storage=storage, les_cs=0.1, force_every=100)
+        chosen, ms_tune, table = b.autotune(trial_steps)
+        b.reset()
+        n = steps if storage == "fp16" else min(steps, seq_steps)
+        b.synchronize()
+        l0 = b.kernel_launches()
+        t0 = time.perf_counter()
+        assert b.step_n(n, use_graphs=True) == 0
+        b.synchronize()
+        wall = time.perf_counter() - t0
+        res[storage] = {"glups": round(upd * n / wall / 1e9, 3), "wall_s": round(wall, 3), "steps": n,
+                        "device_ms_per_step": round(b.last_ms() / n, 4), "autotuned_shape": list(chosen),
+                        "shapes_timed": len(table), "launches_per_step": round((b.kernel_launches() - l0) / n, 3),
+                        "tuning_ms_per_step": {"/".join(map(str, c)): round(m, 4) for c, m in table}}
+        if storage == "fp16":
+            cl, cd = b.coefficients(0.5)
+            out["polar"] = [{"section": t.digits, "aoa": t.aoa, "chord": t.chord, "cl": round(float(a), 4),
+                             "cd": round(float(c), 5)} for t, a, c in zip(tunnels, cl, cd)]
+        b.close()
+    out["batched_fp16"] = res["fp16"]
+    out["batched_fp32"] = res["fp32"]
+    # 24 sequential plain FP32 runs (one solver per tunnel, its own launches).
+    seq = 0.0
+    for t in tunnels:
+        s = fc.LBMSolver()
+        s.init(t.dims, fc.scaling_direct(t.tau, t.u_lat, t.chord), t.flags, storage="fp32", les_cs=0.1)
+        s.set_startup_ramp_enabled(False)
+        s.reset()
+        s.synchronize()
+        t0 = time.perf_counter()
+        left = seq_steps
+        while left > 0:
+            k = min(BATCH, left)
+            assert s.step_n(k) == 0
+            left -= k
+        s.synchronize()
+        seq += time.perf_counter() - t0
+        del s
+    out["sequential_fp32"] = {"glups": round(upd * seq_steps / seq / 1e9, 3), "wall_s": round(seq, 3),
+                              "steps": seq_steps,
+                              "wall_s_projected_full_polar": round(seq * steps / seq_steps, 2)}
+    out["polar_wall_s_batched_fp16"] = res["fp16"]["wall_s"] * steps / res["fp16"]["steps"]
+    out["speedup_batched_fp16_vs_sequential_fp32"] = round(out["sequential_fp32"]["wall_s_projected_full_polar"]
+                                                          / out["polar_wall_s_batched_fp16"], 2)
+    return out
+
+
 def cpu_host():
     try:
         model = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -344,6 +405,8 @@ def main():
     ap.add_argument("--only-fp16", action="store_true", help="measure the FP16-storage solver only")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wallnet", action="store_true", help="skip the learned wall-seed leg")
+    ap.add_argument("--no-polar", action="store_true", help="skip the batched-polar leg")
+    ap.add_argument("--polar-steps", type=int, default=10000)
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
     args = ap.parse_args()
@@ -402,6 +465,8 @@ def main():
     if not args.no_wallnet and ws == 1:
         line["wall_seed"] = wall_seed_leg(r32["solver"], t)
     r32["solver"] = None
+    if not args.no_polar and ws == 1:
+        line["batched_polar"] = polar_leg(args.polar_steps)
     del r32
     if not args.no_fp16:
         r16 = measure(t, "fp16", args.steps, warmup, None)

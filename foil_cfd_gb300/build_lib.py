@@ -27,7 +27,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
 # Per-file extra flags: the FP32 reference-order kernels and the refinement
 # coupling must not contract multiply-adds (their rounding follows the
 # reference expression tree, so results are bit-identical to it).
-FILE_FLAGS = {"collide_f32.cu": ["--fmad=false"], "refine_kernels.cu": ["--fmad=false"]}
+FILE_FLAGS = {"collide_f32.cu": ["--fmad=false"], "refine_kernels.cu": ["--fmad=false"], "batch_f32.cu": ["--fmad=false"]}
 
 
 def _cuda_home() -> Path:

@@ -1,5 +1,6 @@
-"""ctypes binding of include/foilcfd_step.h (the solver step's C ABI) and
-include/foilcfd_wallnet.h (the learned u_tau seed).
+"""ctypes binding of include/foilcfd_step.h (the solver step's C ABI),
+include/foilcfd_wallnet.h (the learned u_tau seed) and
+include/foilcfd_batch.h (the batched multi-tunnel step).
 
 Loading fails loudly when the compiled library is missing: there is no CPU
 fallback for the solver step. Build it with ``foil_cfd_gb300.build_lib``
@@ -66,6 +67,15 @@ class TrainOpts(C.Structure):
 
 class UtauStats(C.Structure):
     _fields_ = [("solved", C.c_int), ("fallbacks", C.c_int), ("newton_iterations", C.c_longlong)]
+
+
+class BatchTunnel(C.Structure):
+    _fields_ = [("dims", Dims), ("flags", C.c_void_p), ("tau", C.c_float), ("u_lat", C.c_float),
+                ("chord_cells", C.c_int)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("block", C.c_int), ("rows", C.c_int), ("ctas_per_sm", C.c_int), ("group_mb", C.c_int)]
 
 
 P = C.c_void_p
@@ -146,6 +156,27 @@ _SIGS = {
     "fcfd_set_wall_solver": (C.c_int, [P, C.c_int, P]),
     "fcfd_wall_harvest": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(C.c_int)]),
     "fcfd_wall_update_timed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(UtauStats)]),
+    # include/foilcfd_batch.h
+    "fcfd_batch_create": (P, []),
+    "fcfd_batch_destroy": (None, [P]),
+    "fcfd_batch_init": (C.c_int, [P, C.POINTER(BatchTunnel), C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, P,
+                                  C.c_char_p, C.c_size_t]),
+    "fcfd_batch_reset": (C.c_int, [P]),
+    "fcfd_batch_set_config": (C.c_int, [P, C.POINTER(BatchConfig)]),
+    "fcfd_batch_get_config": (C.c_int, [P, C.POINTER(BatchConfig)]),
+    "fcfd_batch_autotune": (C.c_int, [P, C.c_int, C.POINTER(BatchConfig), C.POINTER(C.c_float),
+                                      C.POINTER(BatchConfig), C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
+    "fcfd_batch_step_n": (C.c_int, [P, C.c_int, C.c_int]),
+    "fcfd_batch_synchronize": (C.c_int, [P]),
+    "fcfd_batch_step_count": (C.c_longlong, [P]),
+    "fcfd_batch_updates_per_step": (C.c_longlong, [P]),
+    "fcfd_batch_kernel_launches": (C.c_longlong, [P]),
+    "fcfd_batch_force_samples": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "fcfd_batch_force_history": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_int)]),
+    "fcfd_batch_forces_now": (C.c_int, [P, P]),
+    "fcfd_batch_export_f32": (C.c_int, [P, C.c_int, P, C.c_size_t]),
+    "fcfd_batch_import_f32": (C.c_int, [P, C.c_int, P, C.c_size_t]),
+    "fcfd_batch_last_ms": (C.c_int, [P, C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -1,0 +1,536 @@
+// Host side of the batched multi-tunnel step (include/foilcfd_batch.h): the
+// device arena of all tunnels, the work-item table of the current launch
+// shape, graph capture of step chunks with their force samples, and the
+// launch-shape autotuner.
+//
+// Per tunnel the set-up follows the single-tunnel solver: flags -> kind
+// bytes (launch_classify), compact force-link list (build_force_links),
+// uniform-flow reset feq(1, u) + the reference's speck perturbation
+// (src/sim/lbm_solver.cpp:49, 896-935) on both buffers.
+#include "../../include/foilcfd_batch.h"
+#include "host_geom.h"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+using namespace fcfd;
+
+namespace {
+
+constexpr float kSpeckAmplitudeFrac = 1e-3f;  // reference speck: 1e-3 u_lat
+constexpr unsigned kSpeckSeed = 0x5eedu;
+constexpr int kHistCapacity = 4096;            // force samples kept (ring)
+
+void set_err(char* err, size_t len, const char* m) {
+    if (err && len) std::snprintf(err, len, "%s", m);
+}
+
+struct Tunnel {
+    LevelDims d;
+    long long n = 0;
+    void* f[2] = {nullptr, nullptr};
+    std::uint8_t* flags = nullptr;
+    std::uint8_t* kind = nullptr;
+    std::uint32_t* linkCells = nullptr;
+    std::uint32_t* linkMasks = nullptr;
+    int linkCount = 0;
+    float tau = 0.6f, uLat = 0.0f;
+    int chord = 1;
+};
+
+} // namespace
+
+struct fcfd_batch {
+    std::vector<Tunnel> t;
+    Storage storage = Storage::F16;
+    float lesCs = 0.1f, lambda = 3.0f / 16.0f;
+    int forceEvery = 100;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;  // stream capture needs a non-legacy stream
+    bool initialized = false;
+
+    fcfd_batch_config cfg{128, 1, 0, 0};
+    BatchTable table{};
+    long long nItems = 0;
+    struct Group {
+        long long itemBegin = 0, itemEnd = 0;
+    };
+    std::vector<Group> groups;
+    int parity = 0;
+    long long steps = 0;
+    long long launches = 0;
+    int sms = 0;
+
+    double* dPartials = nullptr;
+    double* dForceCur = nullptr;
+    double* dHist = nullptr;
+    int* dHistCount = nullptr;
+
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double lastMs = 0.0;
+
+    int ntun() const { return static_cast<int>(t.size()); }
+    float smagPre() const { return lesCs > 0.0f ? 18.0f * 1.41421356f * lesCs * lesCs : 0.0f; }
+
+    void dropGraphs() {
+        for (auto& g : graph)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+
+    void freeAll() {
+        if (stream) cudaStreamSynchronize(stream);
+        dropGraphs();
+        for (Tunnel& x : t) {
+            cudaFree(x.f[0]); cudaFree(x.f[1]); cudaFree(x.flags); cudaFree(x.kind);
+            cudaFree(x.linkCells); cudaFree(x.linkMasks);
+        }
+        t.clear();
+        cudaFree(dPartials); cudaFree(dForceCur); cudaFree(dHist); cudaFree(dHistCount);
+        dPartials = dForceCur = dHist = nullptr; dHistCount = nullptr;
+        if (ev0) { cudaEventDestroy(ev0); ev0 = nullptr; }
+        if (ev1) { cudaEventDestroy(ev1); ev1 = nullptr; }
+        if (ownStream && stream) cudaStreamDestroy(stream);
+        if (ownStream) stream = nullptr;
+        ownStream = false;
+        initialized = false;
+    }
+
+    BatchShape shape() const {
+        BatchShape s;
+        s.block = cfg.block;
+        s.rows = cfg.rows;
+        s.grid = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm * sms : 0;
+        return s;
+    }
+
+    int occupancy(const fcfd_batch_config& c) const {
+        BatchShape s{c.block, c.rows, 0};
+        return storage == Storage::F32 ? batch_occupancy_f32(s) : batch_occupancy_f16(s);
+    }
+
+    size_t tunnelBytes(const Tunnel& x) const {
+        return static_cast<size_t>(x.n) * (2 * 19 * (storage == Storage::F32 ? 4 : 2) + 1);
+    }
+
+    /// Work-item table and tunnel groups for the current configuration.
+    cudaError_t uploadTable() {
+        table = BatchTable{};
+        table.ntun = ntun();
+        table.lambda = lambda;
+        table.smagPre = smagPre();
+        groups.clear();
+        const size_t limit = static_cast<size_t>(std::max(cfg.group_mb, 0)) << 20;
+        size_t groupBytes = 0;
+        long long item = 0;
+        for (size_t i = 0; i < t.size(); ++i) {
+            const Tunnel& x = t[i];
+            BatchTunnelParam& d = table.t[i];
+            d.f[0] = x.f[0]; d.f[1] = x.f[1];
+            d.kind = x.kind;
+            d.n = x.n;
+            d.nx = x.d.nx; d.ny = x.d.ny; d.nz = x.d.nz;
+            d.xChunks = 1;  // a work item spans whole rows
+            d.tau = x.tau; d.uIn = x.uLat;
+            table.begins[i] = static_cast<unsigned>(item);
+            const size_t bytes = tunnelBytes(x);
+            if (groups.empty() || (limit > 0 && groupBytes + bytes > limit)) {
+                groups.push_back(Group{item, item});
+                groupBytes = 0;
+            }
+            const long long rowGroups = (static_cast<long long>(x.d.ny) * x.d.nz + cfg.rows - 1) / cfg.rows;
+            item += static_cast<long long>(d.xChunks) * rowGroups;
+            groups.back().itemEnd = item;
+            groupBytes += bytes;
+        }
+        if (limit == 0) groups.assign(1, Group{0, item});
+        nItems = item;
+        return item < (1LL << 31) ? cudaSuccess : cudaErrorInvalidValue;
+    }
+
+    cudaError_t collideRange(long long ib, long long ie, int par) {
+        ++launches;
+        const BatchShape s = shape();
+        const unsigned b0 = static_cast<unsigned>(ib), cnt = static_cast<unsigned>(ie - ib);
+        return storage == Storage::F32 ? launch_batch_collide_f32(table, b0, cnt, par, s, stream)
+                                       : launch_batch_collide_f16(table, b0, cnt, par, s, stream);
+    }
+
+    /// One step of every tunnel (all items in one launch).
+    cudaError_t collideOnce() {
+        const cudaError_t e = collideRange(0, nItems, parity);
+        parity ^= 1;
+        return e;
+    }
+
+    /// Force of every tunnel at the current state -> dForceCur.
+    cudaError_t forcesNow() {
+        for (int i = 0; i < ntun(); ++i) {
+            const Tunnel& x = t[i];
+            launches += 2;
+            if (auto e = launch_force(storage, x.f[parity], x.n, x.linkCells, x.linkMasks, x.linkCount, SlipField{},
+                                      dPartials, dForceCur + 3 * i, stream);
+                e != cudaSuccess)
+                return e;
+        }
+        return cudaSuccess;
+    }
+
+    cudaError_t forceSample() {
+        if (auto e = forcesNow(); e != cudaSuccess) return e;
+        ++launches;
+        return launch_force_append(dForceCur, 3 * ntun(), dHist, kHistCapacity, dHistCount, stream);
+    }
+
+    /// One step launched directly (+ the force sample on the cadence).
+    cudaError_t stepDirect() {
+        if (auto e = collideOnce(); e != cudaSuccess) return e;
+        ++steps;
+        if (steps % forceEvery == 0) return forceSample();
+        return cudaSuccess;
+    }
+
+    /// Graph of forceEvery steps + one force sample, from parity p: all
+    /// tunnels per launch, or group after group (each group all its steps).
+    cudaError_t captureChunk(int p) {
+        const int keepParity = parity;
+        const long long keepLaunches = launches;
+        parity = p;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { parity = keepParity; return e; }
+        if (cfg.group_mb <= 0) {
+            for (int s = 0; s < forceEvery && e == cudaSuccess; ++s) e = collideOnce();
+        } else {
+            for (const Group& gr : groups)
+                for (int s = 0; s < forceEvery && e == cudaSuccess; ++s)
+                    e = collideRange(gr.itemBegin, gr.itemEnd, p ^ (s & 1));
+            parity = p;  // forceEvery is even
+        }
+        if (e == cudaSuccess) e = forceSample();
+        cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+        parity = keepParity;
+        launches = keepLaunches;
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&graph[p], g, 0);
+        if (g) cudaGraphDestroy(g);
+        return e;
+    }
+
+    /// Launches per replayed chunk (collides + force kernels + append).
+    long long chunkLaunches() const {
+        const long long collides = cfg.group_mb > 0 ? static_cast<long long>(groups.size()) * forceEvery : forceEvery;
+        return collides + 2LL * ntun() + 1;
+    }
+
+    cudaError_t stepN(int n, bool useGraphs) {
+        cudaEventRecord(ev0, stream);
+        cudaError_t e = cudaSuccess;
+        while (n > 0 && e == cudaSuccess) {
+            if (useGraphs && steps % forceEvery == 0 && n >= forceEvery) {
+                if (!graph[parity]) e = captureChunk(parity);
+                if (e != cudaSuccess) break;
+                e = cudaGraphLaunch(graph[parity], stream);
+                steps += forceEvery;
+                launches += chunkLaunches();
+                n -= forceEvery;  // forceEvery is even: parity unchanged
+            } else {
+                e = stepDirect();
+                --n;
+            }
+        }
+        cudaEventRecord(ev1, stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+        lastMs = ms;
+        return e;
+    }
+
+    cudaError_t reset() {
+        steps = 0;
+        parity = 0;
+        for (Tunnel& x : t)
+            for (int i = 0; i < 2; ++i) {
+                launches += 2;
+                if (auto e = launch_init_equilibrium(storage, x.f[i], x.kind, x.d, x.uLat, stream); e != cudaSuccess)
+                    return e;
+                if (auto e = launch_speck(storage, x.f[i], x.kind, x.d, kSpeckAmplitudeFrac * x.uLat, kSpeckSeed,
+                                          stream);
+                    e != cudaSuccess)
+                    return e;
+            }
+        if (auto e = cudaMemsetAsync(dHistCount, 0, sizeof(int), stream); e != cudaSuccess) return e;
+        return cudaStreamSynchronize(stream);
+    }
+};
+
+extern "C" {
+
+fcfd_batch* fcfd_batch_create(void) { return new fcfd_batch(); }
+
+void fcfd_batch_destroy(fcfd_batch* b) {
+    if (!b) return;
+    b->freeAll();
+    delete b;
+}
+
+int fcfd_batch_init(fcfd_batch* b, const fcfd_batch_tunnel* tunnels, int count, int storage, float lesCs,
+                    float magicLambda, int forceEvery, void* stream, char* err, size_t errlen) {
+    if (!b || !tunnels || count <= 0 || count > FCFD_BATCH_MAX_TUNNELS) {
+        set_err(err, errlen, "need 1..64 tunnels");
+        return cudaErrorInvalidValue;
+    }
+    if (storage != FCFD_STORE_FP32 && storage != FCFD_STORE_FP16) {
+        set_err(err, errlen, "unknown storage");
+        return cudaErrorInvalidValue;
+    }
+    if (forceEvery < 2 || forceEvery % 2 != 0) {
+        set_err(err, errlen, "force_every must be even and >= 2");
+        return cudaErrorInvalidValue;
+    }
+    b->freeAll();
+    b->storage = storage == FCFD_STORE_FP32 ? Storage::F32 : Storage::F16;
+    b->lesCs = lesCs;
+    b->lambda = magicLambda > 0.0f ? magicLambda : 3.0f / 16.0f;
+    b->forceEvery = forceEvery;
+    b->stream = static_cast<cudaStream_t>(stream);
+    if (!b->stream) {
+        if (auto e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking); e != cudaSuccess) {
+            set_err(err, errlen, cudaGetErrorString(e));
+            return e;
+        }
+        b->ownStream = true;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t esz = b->storage == Storage::F32 ? 4 : 2;
+    int maxLinks = 0;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < count && e == cudaSuccess; ++i) {
+        const fcfd_batch_tunnel& in = tunnels[i];
+        Tunnel x;
+        x.d = LevelDims{in.dims.nx, in.dims.ny, in.dims.nz};
+        x.n = x.d.cells();
+        if (x.d.nx < 3 || x.d.ny < 3 || x.d.nz < 1 || !in.flags || x.n >= (1LL << 31) / 19) {
+            set_err(err, errlen, "bad tunnel dims or flags");
+            b->freeAll();
+            return cudaErrorInvalidValue;
+        }
+        x.tau = in.tau;
+        x.uLat = in.u_lat;
+        x.chord = std::max(1, in.chord_cells);
+        b->t.push_back(x);
+        Tunnel& y = b->t.back();
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMalloc(&y.f[k], static_cast<size_t>(y.n) * 19 * esz);
+        if (e == cudaSuccess) e = cudaMalloc(&y.flags, static_cast<size_t>(y.n));
+        if (e == cudaSuccess) e = cudaMalloc(&y.kind, static_cast<size_t>(y.n) + 64);
+        if (e == cudaSuccess) e = cudaMemcpy(y.flags, in.flags, static_cast<size_t>(y.n), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_classify(y.flags, y.kind, y.d, b->stream);
+        std::vector<std::uint32_t> cells, masks;
+        if (e == cudaSuccess) build_force_links(y.d, in.flags, cells, masks);
+        y.linkCount = static_cast<int>(cells.size());
+        maxLinks = std::max(maxLinks, y.linkCount);
+        if (e == cudaSuccess) e = cudaMalloc(&y.linkCells, std::max<size_t>(4, cells.size() * 4));
+        if (e == cudaSuccess) e = cudaMalloc(&y.linkMasks, std::max<size_t>(4, masks.size() * 4));
+        if (e == cudaSuccess && !cells.empty()) {
+            e = cudaMemcpy(y.linkCells, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(y.linkMasks, masks.data(), masks.size() * 4, cudaMemcpyHostToDevice);
+        }
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->dPartials, std::max(1, force_blocks(maxLinks)) * 3 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dForceCur, 3 * count * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dHist, static_cast<size_t>(kHistCapacity) * 3 * count * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dHistCount, sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e == cudaSuccess) e = b->uploadTable();
+    if (e == cudaSuccess) e = b->reset();
+    if (e != cudaSuccess) {
+        set_err(err, errlen, cudaGetErrorString(e));
+        b->freeAll();
+        return e;
+    }
+    b->initialized = true;
+    return 0;
+}
+
+int fcfd_batch_reset(fcfd_batch* b) {
+    if (!b || !b->initialized) return cudaErrorNotReady;
+    return b->reset();
+}
+
+int fcfd_batch_set_config(fcfd_batch* b, const fcfd_batch_config* c) {
+    if (!b || !b->initialized || !c) return cudaErrorInvalidValue;
+    const int occ = b->occupancy(*c);
+    if (occ <= 0 || c->ctas_per_sm < 0 || c->ctas_per_sm > occ || c->group_mb < 0) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(b->stream); e != cudaSuccess) return e;
+    b->cfg = *c;
+    b->dropGraphs();
+    return b->uploadTable();
+}
+
+int fcfd_batch_get_config(const fcfd_batch* b, fcfd_batch_config* c) {
+    if (!b || !c) return cudaErrorInvalidValue;
+    *c = b->cfg;
+    return 0;
+}
+
+int fcfd_batch_autotune(fcfd_batch* b, int trialSteps, fcfd_batch_config* chosen, float* msOut,
+                        fcfd_batch_config* cands, float* msEach, int maxCands, int* nCands) {
+    if (!b || !b->initialized || trialSteps <= 0) return cudaErrorInvalidValue;
+    int written = 0;
+    auto record = [&](const fcfd_batch_config& c, float ms) {
+        if (cands && msEach && written < maxCands) {
+            cands[written] = c;
+            msEach[written] = ms;
+            ++written;
+        }
+    };
+    // Stage 1: launch shapes, all tunnels per launch, direct steps.
+    std::vector<fcfd_batch_config> list;
+    for (int block : {64, 128, 256})
+        for (int rows : {1, 2, 4}) {
+            fcfd_batch_config c{block, rows, 0, 0};
+            const int occ = b->occupancy(c);
+            if (occ <= 0) continue;
+            list.push_back(c);  // one block per work item
+            for (int k : {1, 2, 4, 8, 16})
+                if (k <= occ) list.push_back(fcfd_batch_config{block, rows, k, 0});
+            if (occ > 16) list.push_back(fcfd_batch_config{block, rows, occ, 0});
+        }
+    float best = 1e30f;
+    fcfd_batch_config bestCfg = b->cfg;
+    for (const fcfd_batch_config& c : list) {
+        if (auto e = fcfd_batch_set_config(b, &c); e != 0) return e;
+        // One untimed step (first-launch costs), then the timed trial.
+        if (auto e = b->stepN(1, false); e != cudaSuccess) return e;
+        if (auto e = b->stepN(trialSteps, false); e != cudaSuccess) return e;
+        const float ms = static_cast<float>(b->lastMs) / static_cast<float>(trialSteps);
+        record(c, ms);
+        if (ms < best) {
+            best = ms;
+            bestCfg = c;
+        }
+    }
+    // Stage 2: tunnel grouping with the best shape, one graph chunk each.
+    const int fe = b->forceEvery;
+    if (const long long r = b->steps % fe; r != 0)
+        if (auto e = b->stepN(static_cast<int>(fe - r), false); e != cudaSuccess) return e;
+    const fcfd_batch_config shape = bestCfg;
+    best = 1e30f;
+    for (int mb : {0, 48, 96, 192}) {
+        fcfd_batch_config c = shape;
+        c.group_mb = mb;
+        if (auto e = fcfd_batch_set_config(b, &c); e != 0) return e;
+        if (auto e = b->stepN(fe, true); e != cudaSuccess) return e;  // capture + first replay
+        if (auto e = b->stepN(fe, true); e != cudaSuccess) return e;
+        const float ms = static_cast<float>(b->lastMs) / static_cast<float>(fe);
+        record(c, ms);
+        if (ms < best) {
+            best = ms;
+            bestCfg = c;
+        }
+    }
+    if (nCands) *nCands = written;
+    if (auto e = fcfd_batch_set_config(b, &bestCfg); e != 0) return e;
+    if (chosen) *chosen = bestCfg;
+    if (msOut) *msOut = best;
+    return 0;
+}
+
+int fcfd_batch_step_n(fcfd_batch* b, int n, int useGraphs) {
+    if (!b || !b->initialized) return cudaErrorNotReady;
+    if (n <= 0) return 0;
+    return b->stepN(n, useGraphs != 0);
+}
+
+int fcfd_batch_synchronize(fcfd_batch* b) {
+    if (!b) return cudaErrorInvalidValue;
+    return cudaStreamSynchronize(b->stream);
+}
+
+long long fcfd_batch_step_count(const fcfd_batch* b) { return b ? b->steps : 0; }
+
+long long fcfd_batch_updates_per_step(const fcfd_batch* b) {
+    long long u = 0;
+    if (b)
+        for (const Tunnel& x : b->t) u += x.n;
+    return u;
+}
+
+long long fcfd_batch_kernel_launches(const fcfd_batch* b) { return b ? b->launches : 0; }
+
+int fcfd_batch_force_samples(fcfd_batch* b, int* total) {
+    if (!b || !b->initialized || !total) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(b->stream); e != cudaSuccess) return e;
+    return cudaMemcpy(total, b->dHistCount, sizeof(int), cudaMemcpyDeviceToHost);
+}
+
+int fcfd_batch_force_history(fcfd_batch* b, double* out, int maxSamples, int* written) {
+    if (!b || !b->initialized || !out || maxSamples <= 0) return cudaErrorInvalidValue;
+    int total = 0;
+    if (auto e = fcfd_batch_force_samples(b, &total); e != 0) return e;
+    const int avail = std::min(total, kHistCapacity);
+    const int take = std::min(avail, maxSamples);
+    const size_t per = 3 * static_cast<size_t>(b->ntun());
+    for (int k = 0; k < take; ++k) {
+        const int idx = (total - take + k) % kHistCapacity;
+        if (auto e = cudaMemcpy(out + k * per, b->dHist + idx * per, per * sizeof(double), cudaMemcpyDeviceToHost);
+            e != cudaSuccess)
+            return e;
+    }
+    if (written) *written = take;
+    return 0;
+}
+
+int fcfd_batch_forces_now(fcfd_batch* b, double* out) {
+    if (!b || !b->initialized || !out) return cudaErrorInvalidValue;
+    if (auto e = b->forcesNow(); e != cudaSuccess) return e;
+    if (auto e = cudaStreamSynchronize(b->stream); e != cudaSuccess) return e;
+    return cudaMemcpy(out, b->dForceCur, 3 * b->ntun() * sizeof(double), cudaMemcpyDeviceToHost);
+}
+
+int fcfd_batch_export_f32(fcfd_batch* b, int tunnel, float* f, size_t n) {
+    if (!b || !b->initialized || !f || tunnel < 0 || tunnel >= b->ntun()) return cudaErrorInvalidValue;
+    const Tunnel& x = b->t[tunnel];
+    if (n != static_cast<size_t>(x.n) * 19) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(b->stream); e != cudaSuccess) return e;
+    if (b->storage == Storage::F32) return cudaMemcpy(f, x.f[b->parity], n * 4, cudaMemcpyDeviceToHost);
+    float* stage = nullptr;
+    if (auto e = cudaMalloc(&stage, n * 4); e != cudaSuccess) return e;
+    cudaError_t e = launch_store_to_f32(b->storage, x.f[b->parity], stage, x.n, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(f, stage, n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(stage);
+    return e;
+}
+
+int fcfd_batch_import_f32(fcfd_batch* b, int tunnel, const float* f, size_t n) {
+    if (!b || !b->initialized || !f || tunnel < 0 || tunnel >= b->ntun()) return cudaErrorInvalidValue;
+    const Tunnel& x = b->t[tunnel];
+    if (n != static_cast<size_t>(x.n) * 19) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(b->stream); e != cudaSuccess) return e;
+    if (b->storage == Storage::F32) return cudaMemcpy(x.f[b->parity], f, n * 4, cudaMemcpyHostToDevice);
+    float* stage = nullptr;
+    if (auto e = cudaMalloc(&stage, n * 4); e != cudaSuccess) return e;
+    cudaError_t e = cudaMemcpy(stage, f, n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_f32_to_store(b->storage, stage, x.f[b->parity], x.n, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(stage);
+    return e;
+}
+
+int fcfd_batch_last_ms(const fcfd_batch* b, double* ms) {
+    if (!b || !ms) return cudaErrorInvalidValue;
+    *ms = b->lastMs;
+    return 0;
+}
+
+} // extern "C"

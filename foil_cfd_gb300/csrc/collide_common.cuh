@@ -294,16 +294,12 @@ __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, con
     if (a.writeMacro) { a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz; }
 }
 
-// ---- one cell per thread -----------------------------------------------------
-constexpr int kCellBlockX = 128;
-
+/// One full cell update at (x, y, z): boundary cells by flag, fluid cells
+/// by their 19 pulls (bulk or near-wall path) and the collision.
 template <class S, bool WM, bool EXACT>
-__global__ void __launch_bounds__(kCellBlockX)
-collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
-                    const std::uint8_t* __restrict__ kind, CollideArgs a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= a.nx) return;
-    const int y = blockIdx.y, z = blockIdx.z;
+__device__ __forceinline__ void collide_one(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                                            const std::uint8_t* __restrict__ kind, const CollideArgs& a, int x, int y,
+                                            int z) {
     const unsigned cell = static_cast<unsigned>(x)
                         + static_cast<unsigned>(a.nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z);
     const std::uint8_t k = kind[cell];
@@ -317,6 +313,18 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
     if (!(k & kNearWall)) gather_bulk<S>(src, a, b, f);
     else gather_wall<S, WM>(src, kind, a, b, cell, y, z, f);
     finish_cell<S, EXACT>(dst, a, cell, f);
+}
+
+// ---- one cell per thread -----------------------------------------------------
+constexpr int kCellBlockX = 128;
+
+template <class S, bool WM, bool EXACT>
+__global__ void __launch_bounds__(kCellBlockX)
+collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                    const std::uint8_t* __restrict__ kind, CollideArgs a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= a.nx) return;
+    collide_one<S, WM, EXACT>(src, dst, kind, a, x, blockIdx.y, blockIdx.z);
 }
 
 // ---- staged: x-rows through shared memory with bulk async copies -------------

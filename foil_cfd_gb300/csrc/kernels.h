@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cuda_runtime_api.h>
 
+#include "batch_types.h"
 #include "wallnet_types.h"
 
 struct fcfd_wallnet;
@@ -131,6 +132,20 @@ wallnet::NetDev wallnet_view(const fcfd_wallnet* net);
 /// every wall-list entry.
 cudaError_t launch_wall_harvest(Storage s, const void* f, long long cells, WallListDev list,
                                 float utCutoff, float* utOut, float* ysOut, cudaStream_t st);
+
+// ---- batched multi-tunnel step (batch_f32.cu, batch_f16.cu) ---------------
+/// One step of the tunnels owning work items [itemBase, itemBase + nItems):
+/// src = f[parity], dst = f[parity ^ 1]. The table goes by value into the
+/// kernel's parameters. Shapes: block 64/128/256, rows 1/2/4; grid 0 = one
+/// block per work item.
+cudaError_t launch_batch_collide_f32(const BatchTable& tab, unsigned itemBase, unsigned nItems, int parity,
+                                     BatchShape sh, cudaStream_t st);
+cudaError_t launch_batch_collide_f16(const BatchTable& tab, unsigned itemBase, unsigned nItems, int parity,
+                                     BatchShape sh, cudaStream_t st);
+/// Resident blocks per SM of a batched collide shape (0: unknown shape).
+int batch_occupancy_f32(BatchShape sh);
+int batch_occupancy_f16(BatchShape sh);
+cudaError_t launch_force_append(const double* cur, int n3, double* hist, int cap, int* count, cudaStream_t st);
 
 // ---- refinement (refine_kernels.cu) ----------------------------------------
 struct RefineGeom {
