@@ -145,6 +145,8 @@ def measure(t, storage, steps, warmup, clocks=None):
         clocks.start()
     ms = timed_steps(sol, steps)
     clk = clocks.stop() if clocks else None
+    if sol.nan_detected():
+        raise RuntimeError("the solver latched its watchdog inside the timed steps: no valid timing")
     launches = sol.kernel_launches() - l0
     # Dominant kernel: every collide launch bracketed by events, on the
     # solver's stream, over a separate run of the same steps.
@@ -152,6 +154,8 @@ def measure(t, storage, steps, warmup, clocks=None):
     timed_steps(sol, min(steps, 40))
     col_ms, col_n, col_cells, col_bytes = sol.collide_time_ms()
     sol.enable_collide_timing(False)
+    if sol.nan_detected():
+        raise RuntimeError("the solver latched its watchdog inside the collide timing: no valid timing")
     upd = t.updates_per_step()
     res = dict(ms=ms, glups=upd * steps / (ms * 1e-3) / 1e9,
                coarse_glups=float(np.prod(t.dims)) * steps / (ms * 1e-3) / 1e9, launches=launches, clocks=clk,
@@ -206,6 +210,8 @@ def e2e(t, res, steps):
     assert sol.download_macro_into(*[m.array for m in macro]) == 0
     force = sol.force_raw()
     dt = time.perf_counter() - t0
+    if sol.nan_detected():
+        raise RuntimeError("the solver latched its watchdog inside the e2e steps: no valid timing")
     h2d = fcoarse.array.nbytes + (ffine.array.nbytes if ffine is not None else 0)
     d2h = sum(m.array.nbytes for m in macro) + force.nbytes
     for a in [fcoarse, ffine, *macro]:
@@ -284,7 +290,7 @@ def wall_seed_leg(sol, t, epochs=150, n_harvest=2_000_000, n_synth=1_000_000, ba
     return out
 
 
-def polar_leg(steps=10000, seq_steps=2000, trial_steps=10):
+def polar_leg(steps=10000, seq_steps=2000, trial_steps=10, fixed=None):
     """Batched polar: 24 NACA 4-digit tunnels of uneven size in one launch per
     step (FP16 storage, graph-replayed chunks, autotuned shape) from a uniform
     start; against 24 sequential single-tunnel FP32 runs (the drop-in)."""
@@ -294,12 +300,16 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10):
     upd = float(sum(t.cells for t in tunnels))
     out = {"tunnels": len(tunnels), "cells": int(upd), "steps": steps,
            "sections": "NACA 0012/2412/4412, -4..16 deg by 2.5 (first 24), chord 96-192 cells, 2.5 x 1.5 chords, "
-                       "span 16 periodic"}
+                       "span 16 periodic, Re 1000 on the chord, uniform-flow start"}
     res = {}
     for storage in ("fp16", "fp32"):
         b = batch.BatchSolver()
         b.init(tunnels, storage=storage, les_cs=0.1, force_every=100)
-        chosen, ms_tune, table = b.autotune(trial_steps)
+        if fixed is None:
+            chosen, ms_tune, table = b.autotune(trial_steps)
+        else:
+            b.set_config(*fixed)
+            chosen, table = tuple(fixed), []
         b.reset()
         n = steps if storage == "fp16" else min(steps, seq_steps)
         b.synchronize()
@@ -312,15 +322,19 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10):
                         "device_ms_per_step": round(b.last_ms() / n, 4), "autotuned_shape": list(chosen),
                         "shapes_timed": len(table), "launches_per_step": round((b.kernel_launches() - l0) / n, 3),
                         "tuning_ms_per_step": {"/".join(map(str, c)): round(m, 4) for c, m in table}}
+        speed, bad = b.health()
+        res[storage]["diverged_tunnels"] = int(((speed >= 0.285) | (bad > 0)).sum())
         if storage == "fp16":
             cl, cd = b.coefficients(0.5)
             out["polar"] = [{"section": t.digits, "aoa": t.aoa, "chord": t.chord, "cl": round(float(a), 4),
-                             "cd": round(float(c), 5)} for t, a, c in zip(tunnels, cl, cd)]
+                             "cd": round(float(c), 5), "max_speed": round(float(v), 4), "diverged": bool(v >= 0.285 or k)}
+                            for t, a, c, v, k in zip(tunnels, cl, cd, speed, bad)]
         b.close()
     out["batched_fp16"] = res["fp16"]
     out["batched_fp32"] = res["fp32"]
     # 24 sequential plain FP32 runs (one solver per tunnel, its own launches).
     seq = 0.0
+    latched = 0
     for t in tunnels:
         s = fc.LBMSolver()
         s.init(t.dims, fc.scaling_direct(t.tau, t.u_lat, t.chord), t.flags, storage="fp32", les_cs=0.1)
@@ -335,13 +349,197 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10):
             left -= k
         s.synchronize()
         seq += time.perf_counter() - t0
+        latched += int(s.nan_detected())
         del s
     out["sequential_fp32"] = {"glups": round(upd * seq_steps / seq / 1e9, 3), "wall_s": round(seq, 3),
-                              "steps": seq_steps,
+                              "steps": seq_steps, "watchdog_latched_runs": latched,
                               "wall_s_projected_full_polar": round(seq * steps / seq_steps, 2)}
     out["polar_wall_s_batched_fp16"] = res["fp16"]["wall_s"] * steps / res["fp16"]["steps"]
     out["speedup_batched_fp16_vs_sequential_fp32"] = round(out["sequential_fp32"]["wall_s_projected_full_polar"]
                                                           / out["polar_wall_s_batched_fp16"], 2)
+    return out
+
+
+def _gpu_tunnel(dims, flags, tau, u_lat, storage, cs=0.1, chord=64, ramp=False):
+    import foil_cfd_gb300 as fc
+    s = fc.LBMSolver()
+    s.init(dims, fc.scaling_direct(tau, u_lat, chord), flags, storage=storage, les_cs=cs)
+    s.set_startup_ramp_enabled(ramp)
+    s.reset()
+    return s
+
+
+def _force_series(step_fn, force_fn, steps, every):
+    out = []
+    for _ in range(steps // every):
+        step_fn(every)
+        out.append(np.asarray(force_fn(), np.float64).copy())
+    return np.array(out)
+
+
+def _coefficients(series, u, length, span, last=0.5):
+    k = max(1, int(len(series) * last))
+    q = 0.5 * u * u * length * span
+    return float(series[-k:, 0].mean() / q), float(series[-k:, 1].mean() / q)
+
+
+def _strouhal(series, every, u, d, last=0.5):
+    """Shedding frequency from the zero crossings of the lift over the last
+    part of the record."""
+    k = max(4, int(len(series) * last))
+    cl = series[-k:, 1] - series[-k:, 1].mean()
+    t = np.arange(len(cl)) * every
+    s = np.signbit(cl)
+    idx = np.nonzero(s[1:] != s[:-1])[0]
+    if len(idx) < 3:
+        return None
+    # linear interpolation of each crossing
+    tc = t[idx] + every * cl[idx] / (cl[idx] - cl[idx + 1])
+    period = 2.0 * (tc[-1] - tc[0]) / (len(tc) - 1)
+    return float(d / (period * u))
+
+
+def precision_leg():
+    """Storage precision: FP32 (the drop-in) and FP16 deviation storage
+    against each other at the metric's sizes, and against the FP64 oracle
+    (the reference's step restated in double) at sizes the CPU finishes."""
+    from oracle import oracle
+    from foil_cfd_gb300 import tunnels
+    oracle.build()
+    out = {}
+    # Taylor-Green, 64^3 periodic, u0 0.05, nu 0.01, no LES, 1000 steps.
+    N = 64
+    n = N ** 3
+    z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    kw = 2 * np.pi / N
+    u0 = 0.05 * np.sin(kw * x) * np.cos(kw * y) * np.cos(kw * z)
+    v0 = -0.05 * np.cos(kw * x) * np.sin(kw * y) * np.cos(kw * z)
+    f0 = oracle.equilibrium(np.ones(n), u0.ravel(), v0.ravel(), np.zeros(n))
+    flags = np.zeros(n, np.uint8)
+
+    def ke(f):
+        f = f.reshape(19, n).astype(np.float64)
+        r = f.sum(0)
+        j = np.stack([oracle.CX @ f, oracle.CY @ f, oracle.CZ @ f])
+        return 0.5 * float(np.sum((j * j).sum(0) / r))
+
+    rates = {}
+    t = np.arange(1, 11) * 100.0
+    for st in ("fp32", "fp16"):
+        s = _gpu_tunnel((N, N, N), flags, 0.53, 0.0, st, cs=-1.0)
+        s.import_f32(f0)
+        e = []
+        for _ in range(10):
+            assert s.step_n(100) == 0
+            e.append(ke(s.export_f32()))
+        rates[st] = -np.polyfit(t, np.log(e), 1)[0]
+    f64 = f0.astype(np.float64)
+    g64 = f64.copy()
+    e64 = []
+    for _ in range(10):
+        for _ in range(100):
+            d, _m = oracle.collide((N, N, N), f64, flags, 0.53, 3.0 / 16.0, 0.0, 0.0, dst=g64)
+            f64, g64 = d, f64
+        e64.append(ke(f64))
+    r64 = -np.polyfit(t, np.log(e64), 1)[0]
+    out["taylor_green_64_decay_rate"] = {"fp64_oracle": r64, "fp32": float(rates["fp32"]), "fp16": float(rates["fp16"]),
+                                         "fp32_rel_err": float(rates["fp32"] / r64 - 1),
+                                         "fp16_rel_err": float(rates["fp16"] / r64 - 1)}
+
+    # Square cylinder, config 2 sizes on the GPU (FP16 vs FP32), 40k steps,
+    # free-slip channel walls so the force is the body's, startup ramp. At
+    # config 2's Re 1000 (tau 0.5058) the step trips the speed watchdog in
+    # both precisions (recorded below); Cd and St compare at Re 150, the
+    # reference's own cylinder-test Reynolds number, as time statistics of
+    # the last half (vortex shedding).
+    cyl = tunnels.square_cylinder(outlet_eq=True, walls="slip")
+    res = {}
+    for st in ("fp32", "fp16"):
+        s = _gpu_tunnel(cyl.dims, cyl.flags, 0.5 + 3 * 0.08 * 24 / 1000.0, 0.08, st, chord=24, ramp=True)
+        latch = None
+        for k in range(40):
+            assert s.step_n(500) == 0
+            if s.nan_detected():
+                latch = (k + 1) * 500
+                break
+        res[f"re1000_{st}_watchdog_latched_by_step"] = latch
+    for st in ("fp32", "fp16"):
+        s = _gpu_tunnel(cyl.dims, cyl.flags, 0.5 + 3 * 0.08 * 24 / 150.0, 0.08, st, chord=24, ramp=True)
+        ser = _force_series(lambda k: s.step_n(k), s.force_now, 40000, 50)
+        cd, cl = _coefficients(ser, 0.08, 24, cyl.dims[2])
+        res[st] = {"cd": cd, "cl_mean": cl, "st": _strouhal(ser, 50, 0.08, 24), "diverged": s.nan_detected()}
+    out["cylinder_384x128x64_re150_40k"] = {
+        **res, "cd_fp16_vs_fp32": res["fp16"]["cd"] / res["fp32"]["cd"] - 1,
+        "st_fp16_vs_fp32": (res["fp16"]["st"] / res["fp32"]["st"] - 1) if res["fp16"]["st"] and res["fp32"]["st"]
+        else None}
+    # Laminar (steady) cylinder against the FP64 oracle: 192x64x8, side 12,
+    # Re 40, 4000 steps; the same smooth trajectory in every precision.
+    small = tunnels.square_cylinder(192, 64, 8, side=12, cx=48, outlet_eq=True, walls="slip")
+    tau_s = 0.5 + 3 * 0.08 * 12 / 40.0
+    red = {}
+    for st in ("fp32", "fp16"):
+        s = _gpu_tunnel(small.dims, small.flags, tau_s, 0.08, st)
+        red[st] = _coefficients(_force_series(lambda k: s.step_n(k), s.force_now, 4000, 50), 0.08, 12, 8, 0.1)[0]
+        assert not s.nan_detected()
+    o = oracle.OracleSolver(small.dims, small.flags, tau_s, 0.08, cs=0.1, dtype=np.float64)
+    red["fp64_oracle"] = _coefficients(_force_series(o.step_n, lambda: o.last_force, 4000, 50), 0.08, 12, 8,
+                                       0.1)[0]
+    out["cylinder_192x64x8_re40_4000_cd"] = {**red, "fp32_rel_err": red["fp32"] / red["fp64_oracle"] - 1,
+                                             "fp16_rel_err": red["fp16"] / red["fp64_oracle"] - 1}
+
+    # Airfoil, the metric's tunnel (wall model, 2:1 patch), FP16 vs FP32,
+    # from a uniform start. At the specified tau 0.5005 (fine
+    # level 0.501) the step trips the speed watchdog within a few hundred
+    # steps in both precisions (recorded); Cl/Cd compare at tau 0.55
+    # (Re ~1.2e3 on the chord), where the tunnel runs; the flow there is a
+    # stable limit cycle (Cl period ~1800 steps) that FP16 follows with a
+    # slightly different period, so Cl/Cd compare as averages over the last
+    # 40 % of 10,000 steps (about two cycles).
+    import foil_cfd_gb300 as fc
+    t3 = tunnels.airfoil_tunnel()
+    air = {}
+    for st in ("fp32", "fp16"):
+        sol, sc = make_solver(t3, st)
+        latch = None
+        for k in range(50):
+            assert sol.step_n(100) == 0
+            if sol.nan_detected():
+                latch = (k + 1) * 100
+                break
+        air[f"tau0.5005_{st}_watchdog_latched_by_step"] = latch
+        del sol
+    for st in ("fp32", "fp16"):
+        sol = fc.LBMSolver()
+        sol.init(t3.dims, fc.scaling_direct(0.55, t3.u_lat, t3.chord_cells), t3.flags, storage=st, les_cs=0.1)
+        sol.set_wall_model_enabled(True)
+        sol.set_startup_ramp_enabled(False)
+        sol.reset()
+        sol.init_refinement(t3.box, t3.factor, t3.fine_flags)
+        ser = _force_series(lambda k: sol.step_n(k), sol.force_raw, 10000, 50)
+        fd = t3.fine_dims  # the patch carries the surface: fine-level force
+        cd, cl = _coefficients(ser, t3.u_lat, t3.factor * t3.chord_cells, fd[2], last=0.4)
+        air[st] = {"cl": cl, "cd": cd, "diverged": sol.nan_detected()}
+        del sol
+    out["airfoil_640x192x192_10000"] = {**air, "cl_fp16_vs_fp32": air["fp16"]["cl"] / air["fp32"]["cl"] - 1,
+                                       "cd_fp16_vs_fp32": air["fp16"]["cd"] / air["fp32"]["cd"] - 1}
+    # Steady airfoil against the FP64 oracle (no wall model / patch: the
+    # oracle's FP64 path is the plain step), 160x64x8, chord 48, Re 100,
+    # 4000 steps (at Re 500 the section sheds and FP32 and FP64 trajectories
+    # part after ~500 steps, so no precision shows there).
+    ta = tunnels.airfoil_tunnel(160, 64, 8, chord=48, patch=False)
+    tau_a = 0.5 + 3 * 0.08 * 48 / 100.0
+    ra = {}
+    for st in ("fp32", "fp16"):
+        s = _gpu_tunnel(ta.dims, ta.flags, tau_a, 0.08, st)
+        cd, cl = _coefficients(_force_series(lambda k: s.step_n(k), s.force_now, 4000, 50), 0.08, 48, 8, 0.1)
+        assert not s.nan_detected()
+        ra[st] = {"cl": cl, "cd": cd}
+    o = oracle.OracleSolver(ta.dims, ta.flags, tau_a, 0.08, cs=0.1, dtype=np.float64)
+    cd, cl = _coefficients(_force_series(o.step_n, lambda: o.last_force, 4000, 50), 0.08, 48, 8, 0.1)
+    ra["fp64_oracle"] = {"cl": cl, "cd": cd}
+    out["airfoil_160x64x8_re100_4000_no_wall_model"] = {
+        **ra, **{f"{k}_{st}_rel_err": ra[st][k] / ra["fp64_oracle"][k] - 1 for st in ("fp32", "fp16")
+                 for k in ("cl", "cd")}}
     return out
 
 
@@ -407,6 +605,11 @@ def main():
     ap.add_argument("--no-wallnet", action="store_true", help="skip the learned wall-seed leg")
     ap.add_argument("--no-polar", action="store_true", help="skip the batched-polar leg")
     ap.add_argument("--polar-steps", type=int, default=10000)
+    ap.add_argument("--precision", action="store_true",
+                    help="add the FP32/FP16/FP64 precision study (cylinder, airfoil, Taylor-Green)")
+    ap.add_argument("--only-precision", action="store_true", help="run only the precision study")
+    ap.add_argument("--only-polar", action="store_true", help="run only the batched-polar leg")
+    ap.add_argument("--polar-config", default="", help="block,rows,ctas_per_sm,group_mb: skip the autotuner")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
     args = ap.parse_args()
@@ -439,6 +642,16 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.only_precision:
+        if rank == 0:
+            print(json.dumps({"precision": precision_leg()}))
+        return
+    if args.only_polar:
+        if rank == 0:
+            fixed = tuple(int(v) for v in args.polar_config.split(",")) if args.polar_config else None
+            print(json.dumps({"batched_polar": polar_leg(args.polar_steps, fixed=fixed)}))
+        return
+
     clocks = Clocks() if rank == 0 else None
     if args.only_fp16:
         r16 = measure(t, "fp16", args.steps, warmup, clocks)
@@ -467,6 +680,8 @@ def main():
     r32["solver"] = None
     if not args.no_polar and ws == 1:
         line["batched_polar"] = polar_leg(args.polar_steps)
+    if args.precision and ws == 1:
+        line["precision"] = precision_leg()
     del r32
     if not args.no_fp16:
         r16 = measure(t, "fp16", args.steps, warmup, None)

@@ -2,7 +2,7 @@
 polar built on it: NACA 4-digit sections (camber 0/2/4 % at 40 % chord, 12 %
 thick) at -4..16 deg in 2.5 deg steps, first 24 (camber, angle) pairs, chord
 resolution drawn uniformly from 96-192 cells, domain 2.5 x 1.5 chords, span
-16 cells periodic, equilibrium outflow.
+16 cells periodic, equilibrium outflow, Reynolds number 1000 on the chord.
 """
 from __future__ import annotations
 
@@ -12,7 +12,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import capi
-from .solver import STORE, SolverError, boundary_flags, compute_scaling, naca4, voxelize_airfoil
+from .solver import STORE, SolverError, boundary_flags, naca4, voxelize_airfoil
 
 Q = 19
 FLAG_OUTLET, FLAG_OUTLET_EQ = 3, 9
@@ -34,9 +34,9 @@ class PolarTunnel:
 
 
 def polar_tunnels(count: int = 24, seed: int = 0, span: int = 16, u_lat: float = 0.08, chord_range=(96, 192),
-                  cambers=(0, 2, 4), aoas=None, re_chord_m=1.2, airspeed=30.0, nu_air=1.48e-5,
-                  outlet_eq: bool = True):
-    """The polar's tunnels in (camber, angle) order; chord cells seeded."""
+                  cambers=(0, 2, 4), aoas=None, reynolds: float = 1000.0, outlet_eq: bool = True):
+    """The polar's tunnels in (camber, angle) order; chord cells seeded.
+    Reynolds number on the chord (tau = 1/2 + 3 u c / Re)."""
     aoas = [-4.0 + 2.5 * k for k in range(9)] if aoas is None else list(aoas)
     pairs = [(m, a) for m in cambers for a in aoas][:count]
     rng = np.random.default_rng(seed)
@@ -50,8 +50,8 @@ def polar_tunnels(count: int = 24, seed: int = 0, span: int = 16, u_lat: float =
         if outlet_eq:
             flags[flags == FLAG_OUTLET] = FLAG_OUTLET_EQ
         voxelize_airfoil(dims, flags, naca4(digits, 200), aoa, c, 0.3 * dims[0], 0.5 * dims[1])
-        sc = compute_scaling(re_chord_m, airspeed, nu_air, c, u_lat)
-        out.append(PolarTunnel(digits, aoa, c, dims, flags, float(sc.tau), u_lat))
+        tau = float(np.float32(0.5 + 3.0 * u_lat * c / reynolds))
+        out.append(PolarTunnel(digits, aoa, c, dims, flags, tau, u_lat))
     return out
 
 
@@ -149,6 +149,14 @@ class BatchSolver:
         out = np.zeros((len(self.tunnels), 3), np.float64)
         self._check(self._lib.fcfd_batch_forces_now(self._h, capi.ptr(out)), "forces")
         return out
+
+    def health(self):
+        """(max speed per tunnel, non-finite cells per tunnel)."""
+        nt = len(self.tunnels)
+        sp = np.zeros(nt, np.float32)
+        bad = np.zeros(nt, np.int32)
+        self._check(self._lib.fcfd_batch_health(self._h, capi.ptr(sp), capi.ptr(bad)), "health")
+        return sp, bad
 
     def export_f32(self, i: int) -> np.ndarray:
         f = np.empty(Q * int(np.prod(self.tunnels[i].dims)), np.float32)

@@ -497,6 +497,29 @@ int fcfd_batch_forces_now(fcfd_batch* b, double* out) {
     return cudaMemcpy(out, b->dForceCur, 3 * b->ntun() * sizeof(double), cudaMemcpyDeviceToHost);
 }
 
+int fcfd_batch_health(fcfd_batch* b, float* maxSpeed, int* nonFinite) {
+    if (!b || !b->initialized || !maxSpeed || !nonFinite) return cudaErrorInvalidValue;
+    const int nt = b->ntun();
+    int* d = nullptr;
+    if (auto e = cudaMalloc(&d, 2 * nt * sizeof(int)); e != cudaSuccess) return e;
+    cudaError_t e = cudaMemsetAsync(d, 0, 2 * nt * sizeof(int), b->stream);
+    for (int i = 0; i < nt && e == cudaSuccess; ++i) {
+        const Tunnel& x = b->t[i];
+        ++b->launches;
+        e = launch_batch_health(b->storage == Storage::F32, x.f[b->parity], x.kind, x.n, d + i, d + nt + i, b->stream);
+    }
+    std::vector<int> h(2 * nt);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d, h.size() * sizeof(int), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < nt; ++i) {
+        std::memcpy(&maxSpeed[i], &h[i], sizeof(float));
+        nonFinite[i] = h[nt + i];
+    }
+    return 0;
+}
+
 int fcfd_batch_export_f32(fcfd_batch* b, int tunnel, float* f, size_t n) {
     if (!b || !b->initialized || !f || tunnel < 0 || tunnel >= b->ntun()) return cudaErrorInvalidValue;
     const Tunnel& x = b->t[tunnel];

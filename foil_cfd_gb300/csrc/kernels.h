@@ -146,6 +146,10 @@ cudaError_t launch_batch_collide_f16(const BatchTable& tab, unsigned itemBase, u
 int batch_occupancy_f32(BatchShape sh);
 int batch_occupancy_f16(BatchShape sh);
 cudaError_t launch_force_append(const double* cur, int n3, double* hist, int cap, int* count, cudaStream_t st);
+/// Per-tunnel health: max speed over non-solid cells (float bits into
+/// *maxSpeedBits, which must start at 0) and non-finite cell count.
+cudaError_t launch_batch_health(bool fp32, const void* f, const std::uint8_t* kind, long long n, int* maxSpeedBits,
+                                int* nonFinite, cudaStream_t st);
 
 // ---- refinement (refine_kernels.cu) ----------------------------------------
 struct RefineGeom {

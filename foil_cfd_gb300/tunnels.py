@@ -1,7 +1,10 @@
 """Tunnel builders for the benchmark and test workloads (host fixtures).
 
 * ``taylor_green_periodic``: 64^3 fully periodic Taylor-Green vortex.
-* ``square_cylinder``: 384x128x64 channel, 24-cell square at x = 96.
+* ``square_cylinder``: 384x128x64 channel, 24-cell square at x = 96; the
+  channel walls are free-slip (the reference's open-domain flags,
+  tests/m2_cylinder.cpp:76-90, so the momentum exchange is the body's force)
+  or half-way bounce-back.
 * ``airfoil_tunnel``: 640x192x192, NACA 0012 at 6 deg, 256 cells/chord, one
   2:1 patch around the section +- 0.1 chord (the reference's fine-patch
   flags: fluid base, voxelised foil, trailing-edge closure, interface shell,
@@ -56,13 +59,17 @@ def taylor_green_periodic(n: int = 64, u0: float = 0.05):
     return t
 
 
-def square_cylinder(nx=384, ny=128, nz=64, side=24, cx=96, u_lat=0.08, outlet_eq=False):
+def square_cylinder(nx=384, ny=128, nz=64, side=24, cx=96, u_lat=0.08, outlet_eq=False, walls="bounce"):
     dims = (nx, ny, nz)
     f = np.zeros((nz, ny, nx), np.uint8)
     f[:, :, 0] = 2
     f[:, :, -1] = 9 if outlet_eq else 3
-    f[:, 0, :] = 1          # half-way bounce-back channel walls
-    f[:, -1, :] = 1
+    if walls == "slip":     # free-slip bottom / top, inlet wins the corners
+        f[:, 0, 1:] = 5
+        f[:, -1, 1:] = 4
+    else:                   # half-way bounce-back channel walls
+        f[:, 0, :] = 1
+        f[:, -1, :] = 1
     y0 = ny // 2 - side // 2
     x0 = cx - side // 2
     f[:, y0:y0 + side, x0:x0 + side] = 1

@@ -106,6 +106,13 @@ int fcfd_batch_force_history(fcfd_batch* b, double* out, int max_samples, int* w
 /* Momentum-exchange force of every tunnel now (3 doubles per tunnel). */
 int fcfd_batch_forces_now(fcfd_batch* b, double* out);
 
+/* Health of every tunnel at the current state: largest speed |u| over the
+ * non-solid cells (max_speed, count floats) and the number of cells with a
+ * non-finite density or momentum (non_finite, count ints). The batch has no
+ * watchdog latch: a caller checks this after a run (a speed at the 0.3
+ * limiter or any non-finite cell marks a diverged tunnel). */
+int fcfd_batch_health(fcfd_batch* b, float* max_speed, int* non_finite);
+
 /* FP32 SoA populations of one tunnel (19 * cells floats). */
 int fcfd_batch_export_f32(fcfd_batch* b, int tunnel, float* f, size_t n);
 int fcfd_batch_import_f32(fcfd_batch* b, int tunnel, const float* f, size_t n);

@@ -121,3 +121,11 @@ def test_bad_arguments(fc):
     bb = batch.BatchSolver()
     with pytest.raises(Exception):
         bb.init(ts, storage="fp16", force_every=3)
+
+
+def test_health_reads_speeds(fc):
+    ts = small_polar()
+    b = make_batch(ts, "fp16")
+    assert b.step_n(40) == 0
+    speed, bad = b.health()
+    assert (bad == 0).all() and (speed > 0.05).all() and (speed < 0.285).all()
