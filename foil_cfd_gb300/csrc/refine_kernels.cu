@@ -18,7 +18,8 @@
 // m tau_c / tau_f and blend into the coarse post-collision state over a
 // 3-cell edge ramp. The reference recomputes each neighbour's child average
 // inside the filter (19 averages per cell); here pass 1 stores every child
-// average once in scratch and pass 2 filters from scratch.
+// average once in scratch (one 96-byte record per coarse cell) and pass 2
+// filters from scratch.
 //
 // Built with --fmad=false: every expression keeps the reference's rounding,
 // so fill and restriction are bit-identical to the reference kernels (the
@@ -34,7 +35,9 @@ namespace {
 constexpr int kRefineBlock = 128;
 constexpr int kRestrictBand = 2;   // coarse band skipped by the restriction
 constexpr int kRestrictBlend = 3;  // edge-blend ramp width (coarse cells)
-constexpr int kScratchVals = 24;   // fneq[19], rho, ux, uy, uz, valid
+constexpr int kScratchVals = 24;   // per coarse cell: fneq[19], valid, rho, ux, uy, uz
+constexpr int kScratchValid = 19;  // record layout: 6 float4, valid flag closes the fneq part
+constexpr int kScratchRho = 20;
 
 __device__ __forceinline__ int wrapi(int v, int n) {
     v %= n;
@@ -153,7 +156,8 @@ fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restri
     for (int q = 0; q < kQ; ++q) S::st(ff + q * fn, t, feq[q] + neqScale * fneq[q], wgt(q));
 }
 
-/// Pass 1: child average of every coarse cell of the restricted sub-box.
+/// Pass 1: child average of every coarse cell of the restricted sub-box, as
+/// one 96-byte record per coarse cell (six float4).
 template <class S>
 __global__ void __launch_bounds__(kRefineBlock)
 child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __restrict__ fkind,
@@ -181,8 +185,9 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
 #pragma unroll
                 for (int q = 0; q < kQ; ++q) fi[q] += S::ld(ff + q * fn, c, wgt(q));
             }
+    float4* rec = reinterpret_cast<float4*>(scratch) + t * (kScratchVals / 4);
     if (nFluid == 0) {
-        scratch[23 * M + t] = 0.0f;
+        rec[kScratchValid / 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return;
     }
     const float invN = 1.0f / static_cast<float>(nFluid);
@@ -191,41 +196,52 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
     float rho, ux, uy, uz;
     limited_moments(fi, rho, ux, uy, uz);
     const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
+    float r[kScratchVals];
 #pragma unroll
-    for (int q = 0; q < kQ; ++q) scratch[q * M + t] = fi[q] - feq_q(q, rho, ux, uy, uz, usq);
-    scratch[19 * M + t] = rho;
-    scratch[20 * M + t] = ux;
-    scratch[21 * M + t] = uy;
-    scratch[22 * M + t] = uz;
-    scratch[23 * M + t] = 1.0f;
+    for (int q = 0; q < kQ; ++q) r[q] = fi[q] - feq_q(q, rho, ux, uy, uz, usq);
+    r[kScratchValid] = 1.0f;
+    r[kScratchRho] = rho; r[kScratchRho + 1] = ux; r[kScratchRho + 2] = uy; r[kScratchRho + 3] = uz;
+#pragma unroll
+    for (int k = 0; k < kScratchVals / 4; ++k) rec[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
 }
 
 /// Pass 2: Lagrava filter, regularise, inverse rescale, edge blend, write.
+/// Blocks of 32 x 2 x 2 coarse cells, so a neighbour's record is often in L1
+/// from a sibling thread; a neighbour costs five float4 loads.
+constexpr int kRestrictTX = 32, kRestrictTY = 2, kRestrictTZ = 2;
+
 template <class S>
-__global__ void __launch_bounds__(kRefineBlock)
+__global__ void __launch_bounds__(kRestrictTX * kRestrictTY * kRestrictTZ)
 restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__ ckind,
                 RefineGeom g, int rx0, int ry0, int rw, int rh, float neqScaleInv,
                 const float* __restrict__ scratch, float* __restrict__ mRho,
                 float* __restrict__ mU, float* __restrict__ mV, float* __restrict__ mW) {
-    const int lx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (lx >= rw) return;
-    const int ly = blockIdx.y, zc = blockIdx.z;
+    const int lx = blockIdx.x * kRestrictTX + threadIdx.x;
+    const int ly = blockIdx.y * kRestrictTY + threadIdx.y;
+    const int zc = blockIdx.z * kRestrictTZ + threadIdx.z;
     const int nz = g.coarse.nz;
-    const long long M = static_cast<long long>(rw) * rh * nz;
+    if (lx >= rw || ly >= rh || zc >= nz) return;
     const long long t = lx + static_cast<long long>(rw) * (ly + static_cast<long long>(rh) * zc);
     const int xc = rx0 + lx, yc = ry0 + ly;
     const long long cn = g.coarse.cells();
     const unsigned cell = static_cast<unsigned>(xc) + static_cast<unsigned>(g.coarse.nx)
                         * (static_cast<unsigned>(yc) + static_cast<unsigned>(g.coarse.ny) * zc);
     if ((ckind[cell] & kFlagMask) != kFluid) return;
-    if (scratch[23 * M + t] == 0.0f) return;
+    const float4* rec = reinterpret_cast<const float4*>(scratch);
+    constexpr int kRec = kScratchVals / 4;
+    float fneq[kQ];
+    float4 v4 = __ldg(rec + t * kRec + kScratchValid / 4);  // fneq[16..18], valid
+    if (v4.w == 0.0f) return;
+    fneq[16] = v4.x; fneq[17] = v4.y; fneq[18] = v4.z;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float4 a = __ldg(rec + t * kRec + k);
+        fneq[4 * k] = a.x; fneq[4 * k + 1] = a.y; fneq[4 * k + 2] = a.z; fneq[4 * k + 3] = a.w;
+    }
 
     const int dEdge = min(min(lx, rw - 1 - lx), min(ly, rh - 1 - ly));
     const float blend = fminf(1.0f, static_cast<float>(dEdge + 1) / static_cast<float>(kRestrictBlend + 1));
 
-    float fneq[kQ];
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) fneq[q] = scratch[q * M + t];
     int nStencil = 1;
 #pragma unroll
     for (int nb = 1; nb < kQ; ++nb) {
@@ -233,17 +249,23 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
         if (nlx < 0 || nlx >= rw || nly < 0 || nly >= rh) continue;
         const int nzw = wrapi(zc + cz(nb), nz);
         const long long tn = nlx + static_cast<long long>(rw) * (nly + static_cast<long long>(rh) * nzw);
-        if (scratch[23 * M + tn] == 0.0f) continue;
+        const float4 last = __ldg(rec + tn * kRec + kScratchValid / 4);
+        if (last.w == 0.0f) continue;
+        // Same per-q accumulation order as summing slot by slot.
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) fneq[q] += scratch[q * M + tn];
+        for (int k = 0; k < 4; ++k) {
+            const float4 a = __ldg(rec + tn * kRec + k);
+            fneq[4 * k] += a.x; fneq[4 * k + 1] += a.y; fneq[4 * k + 2] += a.z; fneq[4 * k + 3] += a.w;
+        }
+        fneq[16] += last.x; fneq[17] += last.y; fneq[18] += last.z;
         ++nStencil;
     }
     const float invS = 1.0f / static_cast<float>(nStencil);
 #pragma unroll
     for (int q = 0; q < kQ; ++q) fneq[q] *= invS;
     regularize(fneq);
-    const float rho = scratch[19 * M + t], ux = scratch[20 * M + t];
-    const float uy = scratch[21 * M + t], uz = scratch[22 * M + t];
+    const float4 m4 = __ldg(rec + t * kRec + kScratchRho / 4);
+    const float rho = m4.x, ux = m4.y, uy = m4.z, uz = m4.w;
     const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
     float br = 0.f, bjx = 0.f, bjy = 0.f, bjz = 0.f;
 #pragma unroll
@@ -309,16 +331,20 @@ cudaError_t launch_restrict_f2c(Storage s, const void* fineF, const std::uint8_t
     const dim3 grid(static_cast<unsigned>((rw + kRefineBlock - 1) / kRefineBlock),
                     static_cast<unsigned>(rh), static_cast<unsigned>(g.coarse.nz));
     const bool macro = rho && u && v && w;
+    const dim3 rblock(kRestrictTX, kRestrictTY, kRestrictTZ);
+    const dim3 rgrid(static_cast<unsigned>((rw + kRestrictTX - 1) / kRestrictTX),
+                     static_cast<unsigned>((rh + kRestrictTY - 1) / kRestrictTY),
+                     static_cast<unsigned>((g.coarse.nz + kRestrictTZ - 1) / kRestrictTZ));
     if (s == Storage::F32) {
         child_avg_kernel<StoreF32><<<grid, kRefineBlock, 0, st>>>(
             static_cast<const float*>(fineF), fineKind, g, rx0, ry0, rw, rh, scratch);
-        restrict_kernel<StoreF32><<<grid, kRefineBlock, 0, st>>>(
+        restrict_kernel<StoreF32><<<rgrid, rblock, 0, st>>>(
             static_cast<float*>(coarseF), coarseKind, g, rx0, ry0, rw, rh, neqScaleInv, scratch,
             macro ? rho : nullptr, u, v, w);
     } else {
         child_avg_kernel<StoreF16><<<grid, kRefineBlock, 0, st>>>(
             static_cast<const __half*>(fineF), fineKind, g, rx0, ry0, rw, rh, scratch);
-        restrict_kernel<StoreF16><<<grid, kRefineBlock, 0, st>>>(
+        restrict_kernel<StoreF16><<<rgrid, rblock, 0, st>>>(
             static_cast<__half*>(coarseF), coarseKind, g, rx0, ry0, rw, rh, neqScaleInv, scratch,
             macro ? rho : nullptr, u, v, w);
     }
