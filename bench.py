@@ -185,6 +185,7 @@ def measure(t, storage, steps, warmup, clocks=None):
     sol.enable_collide_timing(True)
     timed_steps(sol, min(steps, 40))
     col_ms, col_n, col_cells, col_bytes = sol.collide_time_ms()
+    fu_ms, fu_n, fu_cells, fu_bytes = sol.fused_collide_time_ms()
     sol.enable_collide_timing(False)
     if sol.nan_detected():
         raise RuntimeError("the solver latched its watchdog inside the collide timing: no valid timing")
@@ -192,15 +193,16 @@ def measure(t, storage, steps, warmup, clocks=None):
     res = dict(ms=ms, glups=upd * steps / (ms * 1e-3) / 1e9,
                coarse_glups=float(np.prod(t.dims)) * steps / (ms * 1e-3) / 1e9, launches=launches, clocks=clk,
                collide=dict(ms=col_ms, launches=col_n, cells=col_cells, bytes=col_bytes),
+               fused=dict(ms=fu_ms, launches=fu_n, cells=fu_cells, bytes=fu_bytes),
                nan=sol.nan_detected(), force=sol.force_raw().tolist(), solver=sol, scaling=scaling,
                snapshot=snap)
     return res
 
 
-def roofline(storage, col):
-    """Dominant kernel (the collide, coarse and fine launches): algorithmic
-    bytes per launch (per cell class, counted by the library) over the mean
-    CUDA-event duration of a launch."""
+def roofline(storage, col, kernel=None):
+    """Dominant kernel (the plain collide: the coarse launch and the first
+    fine sub-step's): algorithmic bytes per launch (per cell class, counted
+    by the library) over the mean CUDA-event duration of a launch."""
     peak, kind = peaks()
     nl = max(col["launches"], 1)
     avg_ms = col["ms"] / nl
@@ -211,7 +213,7 @@ def roofline(storage, col):
             "frac": round(achieved / peak, 4), "peak_kind": kind,
             "traffic": round(NCU_TRAFFIC_OVER_ALG[storage] * alg),
             "alg_bytes_per_launch": round(alg),
-            "kernel": f"collide ({storage} storage), coarse + fine launches",
+            "kernel": kernel or f"collide ({storage} storage), coarse + first fine sub-step launches",
             "bytes_per_update_rw_cell": BYTES_PER_LUP[storage], "avg_launch_ms": round(avg_ms, 4),
             "cells_per_launch": round(cells_per_launch)}
 
@@ -698,6 +700,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
             "coarse_only_glups": round(r32["coarse_glups"] * ws, 3),
             "roofline": roofline("fp32", r32["collide"]),
+            "roofline_fused_fine_collide": roofline(
+                "fp32", r32["fused"], "fine collide with the restriction's child averages fused in (fp32), "
+                "bytes incl. the 96 B scratch record per restricted coarse cell") if r32["fused"]["launches"] else None,
             "gpu_launches": int(r32["launches"]), "clocks": r32["clocks"],
             "force_lattice": r32["force"], "nan": bool(r32["nan"])}
     line["e2e"] = e2e(t, r32, args.steps)

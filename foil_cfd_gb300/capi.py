@@ -127,6 +127,7 @@ _SIGS = {
     "fcfd_refinement_info": (C.c_int, [P, C.POINTER(RefineInfo)]),
     "fcfd_import_fine_f32": (C.c_int, [P, P, C.c_size_t]),
     "fcfd_export_fine_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_set_fused_restriction": (C.c_int, [P, C.c_int]),
     "fcfd_build_wall_list": (C.c_longlong, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P]),
     "fcfd_boundary_flags": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
     "fcfd_naca4": (C.c_int, [C.c_char_p, C.c_int, P, C.c_int]),
@@ -137,6 +138,7 @@ _SIGS = {
     "fcfd_kernel_launches": (C.c_longlong, [P]),
     "fcfd_enable_collide_timing": (C.c_int, [P, C.c_int]),
     "fcfd_collide_time_ms": (C.c_int, [P, P, P, P, P]),
+    "fcfd_fused_collide_time_ms": (C.c_int, [P, P, P, P, P]),
     "fcfd_timer_start": (C.c_int, [P]),
     "fcfd_timer_stop": (C.c_int, [P, P]),
     "fcfd_host_alloc": (P, [C.c_size_t]),

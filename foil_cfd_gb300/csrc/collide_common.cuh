@@ -23,6 +23,7 @@
 // set; the kernels live in an anonymous namespace.
 #pragma once
 
+#include "child_record.cuh"
 #include "d3q19.cuh"
 #include "kernels.h"
 
@@ -325,6 +326,112 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= a.nx) return;
     collide_one<S, WM, EXACT>(src, dst, kind, a, x, blockIdx.y, blockIdx.z);
+}
+
+// ---- last fine sub-step with the restriction's child averages fused in --------
+// Factor-2 patches only. A thread owns one fine x column of a 2 x 2 (y, z)
+// cell group and updates its four cells in the children's summation order
+// (z, then y); after each cell the even lane (child x offset 0) takes its
+// odd partner's stored values with a warp shuffle and adds its own, then the
+// partner's -- the stand-alone pass's order (z, y, x; solid children
+// skipped) -- into its own column of a shared-memory accumulator (private to
+// the lane: no block barrier, and no extra registers during the collide). The values used are the stored ones, exactly as a later
+// load would return them. The even lane then writes the scratch record. This
+// saves the stand-alone pass's full re-read of the fine populations.
+constexpr int kFuseX = 128;
+
+template <class S, bool WM, bool EXACT>
+__global__ void __launch_bounds__(kFuseX, 8)
+collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                     const std::uint8_t* __restrict__ kind, CollideArgs a, ChildFuse cf) {
+    const int x = blockIdx.x * kFuseX + threadIdx.x;
+    const bool inX = x < a.nx;
+    const bool even = (threadIdx.x & 1) == 0;
+    const int lx = cf.boxX0 + (x >> 1) - cf.rx0, ly = cf.boxY0 + static_cast<int>(blockIdx.y) - cf.ry0;
+    const bool record = even && x + 1 < a.nx && lx >= 0 && lx < cf.rw && ly >= 0 && ly < cf.rh;
+    __shared__ float acc[kQ][kFuseX / 2];
+    const int col = threadIdx.x >> 1;
+    if (record) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) acc[q][col] = 0.0f;
+    }
+    int nFluid = 0;
+    for (int kz = 0; kz < 2; ++kz)
+        for (int jy = 0; jy < 2; ++jy) {
+            const int y = 2 * blockIdx.y + jy, z = 2 * blockIdx.z + kz;
+            float v[kQ];
+            bool solid = true;
+            if (inX) {
+                const unsigned cell = static_cast<unsigned>(x)
+                                    + static_cast<unsigned>(a.nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z);
+                const std::uint8_t k = kind[cell];
+                const int flag = k & kFlagMask;
+                if (flag == kFluid) {
+                    const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
+                    if (!(k & kNearWall)) gather_bulk<S>(src, a, b, v);
+                    else gather_wall<S, WM>(src, kind, a, b, cell, y, z, v);
+                    float rr, ux, uy, uz;
+                    collide_body<EXACT>(v, a, rr, ux, uy, uz);
+#pragma unroll
+                    for (int q = 0; q < kQ; ++q) {
+                        S::st(dst + q * a.n, cell, v[q], wgt(q));
+                        v[q] = S::rt(v[q], wgt(q));
+                    }
+                    solid = false;
+                } else {
+                    boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
+                    if (flag != kSolid) {
+                        // Written or untouched, the child average sees what dst holds.
+#pragma unroll
+                        for (int q = 0; q < kQ; ++q) v[q] = S::ld(dst + q * a.n, cell, wgt(q));
+                        solid = false;
+                    }
+                }
+            }
+            const bool partnerSolid = __shfl_xor_sync(0xffffffffu, static_cast<int>(solid), 1) != 0;
+            if (record && !solid) {
+                ++nFluid;
+#pragma unroll
+                for (int q = 0; q < kQ; ++q) acc[q][col] += v[q];
+            }
+#pragma unroll
+            for (int q = 0; q < kQ; ++q) {
+                const float pv = __shfl_xor_sync(0xffffffffu, v[q], 1);
+                if (record && !partnerSolid) acc[q][col] += pv;
+            }
+            if (record && !partnerSolid) ++nFluid;
+        }
+    if (!record) return;
+    float fi[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) fi[q] = acc[q][col];
+    const long long t = lx + static_cast<long long>(cf.rw) * (ly + static_cast<long long>(cf.rh) * blockIdx.z);
+    write_child_record(fi, nFluid, reinterpret_cast<float4*>(cf.scratch) + t * (kScratchVals / 4));
+}
+
+template <class S, bool EXACT>
+cudaError_t launch_collide_child_impl(const void* srcv, void* dstv, const std::uint8_t* kind, LevelDims d,
+                                      const CollideParams& p, SlipField slip, const ChildFuse& cf,
+                                      cudaStream_t st) {
+    using T = typename S::T;
+    if (d.ny % 2 || d.nz % 2 || !cf.scratch) return cudaErrorInvalidValue;
+    CollideArgs a;
+    a.nx = d.nx; a.ny = d.ny; a.nz = d.nz; a.n = d.cells();
+    a.tau0 = p.tau; a.lambda = p.magicLambda; a.smagPre = p.smagPrefactor; a.uIn = p.uInlet;
+    a.writeMacro = 0;
+    a.rho = a.u = a.v = a.w = nullptr;
+    a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
+    a.status = nullptr;
+    const dim3 block(kFuseX);
+    const dim3 grid(static_cast<unsigned>((d.nx + kFuseX - 1) / kFuseX), static_cast<unsigned>(d.ny / 2),
+                    static_cast<unsigned>(d.nz / 2));
+    const T* src = static_cast<const T*>(srcv);
+    T* dst = static_cast<T*>(dstv);
+    if (slip.active())
+        collide_child_kernel<S, true, EXACT><<<grid, block, 0, st>>>(src, dst, kind, a, cf);
+    else
+        collide_child_kernel<S, false, EXACT><<<grid, block, 0, st>>>(src, dst, kind, a, cf);
+    return cudaGetLastError();
 }
 
 // ---- staged: x-rows through shared memory with bulk async copies -------------

@@ -53,6 +53,11 @@ cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint
     return launch_collide_impl<StoreF32, true>(src, dst, kind, d, p, rho, u, v, w, slip, st);
 }
 
+cudaError_t launch_collide_child_f32(const float* src, float* dst, const std::uint8_t* kind, LevelDims d,
+                                     const CollideParams& p, SlipField slip, const ChildFuse& cf, cudaStream_t st) {
+    return launch_collide_child_impl<StoreF32, true>(src, dst, kind, d, p, slip, cf, st);
+}
+
 cudaError_t launch_init_eq_f32(float* f, const std::uint8_t* kind, long long n, float uIn, cudaStream_t st) {
     init_eq_f32_kernel<<<static_cast<unsigned>((n + kBlock1D - 1) / kBlock1D), kBlock1D, 0, st>>>(f, kind, n, uIn);
     return cudaGetLastError();

@@ -117,6 +117,8 @@ struct StoreF32 {
     __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float) {
         p[i] = v;
     }
+    /// The value a load returns after st(v): the storage round trip.
+    __device__ __forceinline__ static float rt(float v, float) { return v; }
     /// Load element i of a shared-memory row at shared address `row`.
     __device__ __forceinline__ static float lds(unsigned row, int i, float) {
         float v;
@@ -133,6 +135,7 @@ struct StoreF16 {
     __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float w) {
         p[i] = __float2half_rn(v - w);
     }
+    __device__ __forceinline__ static float rt(float v, float w) { return w + __half2float(__float2half_rn(v - w)); }
     __device__ __forceinline__ static float lds(unsigned row, int i, float w) {
         unsigned short h;
         asm volatile("ld.shared.u16 %0, [%1];" : "=h"(h) : "r"(row + 2u * static_cast<unsigned>(i)));

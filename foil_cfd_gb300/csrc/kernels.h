@@ -69,6 +69,16 @@ cudaError_t launch_store_to_f32(Storage s, const void* in, float* out,
                                 long long cells, cudaStream_t st);
 cudaError_t launch_fill(float* dst, long long n, float v, cudaStream_t st);
 
+/// The restriction's child-average pass fused into the last fine sub-step
+/// (factor 2): scratch records of the coarse cells of the restricted sub-box.
+struct ChildFuse {
+    float* scratch = nullptr;
+    int boxX0 = 0, boxY0 = 0;       ///< patch origin (coarse cells)
+    int rx0 = 0, ry0 = 0, rw = 0, rh = 0;  ///< restricted sub-box (coarse cells)
+};
+cudaError_t launch_collide_child(Storage s, const void* src, void* dst, const std::uint8_t* kind, LevelDims d,
+                                 const CollideParams& p, SlipField slip, const ChildFuse& cf, cudaStream_t st);
+
 // ---- FP32 reference-order kernels (collide_f32.cu, built with --fmad=false)
 cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint8_t* kind,
                                    LevelDims d, const CollideParams& p, float* rho,
@@ -78,6 +88,8 @@ cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint
 bool staged_applies(LevelDims d, Storage s);
 cudaError_t launch_init_eq_f32(float* f, const std::uint8_t* kind, long long n, float uIn,
                                cudaStream_t st);
+cudaError_t launch_collide_child_f32(const float* src, float* dst, const std::uint8_t* kind, LevelDims d,
+                                     const CollideParams& p, SlipField slip, const ChildFuse& cf, cudaStream_t st);
 cudaError_t launch_init_macro_f32(float* f, const std::uint8_t* kind, long long n,
                                   const float* rho, const float* u, const float* v,
                                   const float* w, cudaStream_t st);
@@ -165,11 +177,14 @@ cudaError_t launch_fill_c2f(Storage s, const void* cT0, const void* cT1,
 /// Fine-to-coarse restriction. `scratch` holds 24 floats per coarse cell of
 /// the restricted sub-box (child-averaged fneq[19], rho, ux, uy, uz, valid).
 long long restrict_scratch_floats(const RefineGeom& g);
+/// Restricted sub-box of a patch (the patch minus its 2-cell coarse band).
+void restrict_sub_box(const RefineGeom& g, int& rx0, int& ry0, int& rw, int& rh);
+/// childDone: the scratch records are already written (fused fine collide).
 cudaError_t launch_restrict_f2c(Storage s, const void* fineF,
                                 const std::uint8_t* fineKind, void* coarseF,
                                 const std::uint8_t* coarseKind,
                                 const RefineGeom& g, float neqScaleInv,
                                 float* scratch, float* rho, float* u, float* v,
-                                float* w, cudaStream_t st);
+                                float* w, cudaStream_t st, bool childDone = false);
 
 } // namespace fcfd

@@ -24,6 +24,7 @@
 // Built with --fmad=false: every expression keeps the reference's rounding,
 // so fill and restriction are bit-identical to the reference kernels (the
 // limiter's 1/sqrt is evaluated as IEEE operations).
+#include "child_record.cuh"
 #include "d3q19.cuh"
 #include "kernels.h"
 
@@ -35,9 +36,6 @@ namespace {
 constexpr int kRefineBlock = 128;
 constexpr int kRestrictBand = 2;   // coarse band skipped by the restriction
 constexpr int kRestrictBlend = 3;  // edge-blend ramp width (coarse cells)
-constexpr int kScratchVals = 24;   // per coarse cell: fneq[19], valid, rho, ux, uy, uz
-constexpr int kScratchValid = 19;  // record layout: 6 float4, valid flag closes the fneq part
-constexpr int kScratchRho = 20;
 
 __device__ __forceinline__ int wrapi(int v, int n) {
     v %= n;
@@ -63,24 +61,6 @@ __device__ __forceinline__ void regularize(float (&fneq)[kQ]) {
     }
 }
 
-/// Moments of fi with the density floor and the |u| <= 0.3 limiter.
-__device__ __forceinline__ void limited_moments(const float (&fi)[kQ], float& rho, float& ux,
-                                                float& uy, float& uz) {
-    float r = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) {
-        r += fi[q]; jx += cx(q) * fi[q]; jy += cy(q) * fi[q]; jz += cz(q) * fi[q];
-    }
-    r = fmaxf(r, kRhoFloor);
-    const float inv = 1.0f / r;
-    ux = jx * inv; uy = jy * inv; uz = jz * inv;
-    const float u2 = ux * ux + uy * uy + uz * uz;
-    if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
-        const float sc = kMaxSimSpeed * (1.0f / sqrtf(u2));
-        ux *= sc; uy *= sc; uz *= sc;
-    }
-    rho = r;
-}
 
 template <class S>
 __global__ void __launch_bounds__(kRefineBlock)
@@ -165,7 +145,6 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
     const int lx = blockIdx.x * blockDim.x + threadIdx.x;
     if (lx >= rw) return;
     const int ly = blockIdx.y, zc = blockIdx.z;
-    const long long M = static_cast<long long>(rw) * rh * g.coarse.nz;
     const long long t = lx + static_cast<long long>(rw) * (ly + static_cast<long long>(rh) * zc);
     const int m = g.factor;
     const int fx = m * (rx0 + lx - g.boxX0), fy = m * (ry0 + ly - g.boxY0), fz = m * zc;
@@ -185,29 +164,9 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
 #pragma unroll
                 for (int q = 0; q < kQ; ++q) fi[q] += S::ld(ff + q * fn, c, wgt(q));
             }
-    float4* rec = reinterpret_cast<float4*>(scratch) + t * (kScratchVals / 4);
-    if (nFluid == 0) {
-        rec[kScratchValid / 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        return;
-    }
-    const float invN = 1.0f / static_cast<float>(nFluid);
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) fi[q] *= invN;
-    float rho, ux, uy, uz;
-    limited_moments(fi, rho, ux, uy, uz);
-    const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
-    float r[kScratchVals];
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) r[q] = fi[q] - feq_q(q, rho, ux, uy, uz, usq);
-    r[kScratchValid] = 1.0f;
-    r[kScratchRho] = rho; r[kScratchRho + 1] = ux; r[kScratchRho + 2] = uy; r[kScratchRho + 3] = uz;
-#pragma unroll
-    for (int k = 0; k < kScratchVals / 4; ++k) rec[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+    write_child_record(fi, nFluid, reinterpret_cast<float4*>(scratch) + t * (kScratchVals / 4));
 }
 
-/// Pass 2: Lagrava filter, regularise, inverse rescale, edge blend, write.
-/// Blocks of 32 x 2 x 2 coarse cells, so a neighbour's record is often in L1
-/// from a sibling thread; a neighbour costs five float4 loads.
 constexpr int kRestrictTX = 32, kRestrictTY = 2, kRestrictTZ = 2;
 
 template <class S>
@@ -319,10 +278,12 @@ long long restrict_scratch_floats(const RefineGeom& g) {
     return static_cast<long long>(kScratchVals) * rw * rh * g.coarse.nz;
 }
 
+void restrict_sub_box(const RefineGeom& g, int& rx0, int& ry0, int& rw, int& rh) { sub_box(g, rx0, ry0, rw, rh); }
+
 cudaError_t launch_restrict_f2c(Storage s, const void* fineF, const std::uint8_t* fineKind,
                                 void* coarseF, const std::uint8_t* coarseKind,
                                 const RefineGeom& g, float neqScaleInv, float* scratch,
-                                float* rho, float* u, float* v, float* w, cudaStream_t st) {
+                                float* rho, float* u, float* v, float* w, cudaStream_t st, bool childDone) {
     int rx0, ry0, rw, rh;
     sub_box(g, rx0, ry0, rw, rh);
     if (!fineF || !fineKind || !coarseF || !coarseKind || !scratch || rw <= 0 || rh <= 0
@@ -336,14 +297,16 @@ cudaError_t launch_restrict_f2c(Storage s, const void* fineF, const std::uint8_t
                      static_cast<unsigned>((rh + kRestrictTY - 1) / kRestrictTY),
                      static_cast<unsigned>((g.coarse.nz + kRestrictTZ - 1) / kRestrictTZ));
     if (s == Storage::F32) {
-        child_avg_kernel<StoreF32><<<grid, kRefineBlock, 0, st>>>(
-            static_cast<const float*>(fineF), fineKind, g, rx0, ry0, rw, rh, scratch);
+        if (!childDone)
+            child_avg_kernel<StoreF32><<<grid, kRefineBlock, 0, st>>>(
+                static_cast<const float*>(fineF), fineKind, g, rx0, ry0, rw, rh, scratch);
         restrict_kernel<StoreF32><<<rgrid, rblock, 0, st>>>(
             static_cast<float*>(coarseF), coarseKind, g, rx0, ry0, rw, rh, neqScaleInv, scratch,
             macro ? rho : nullptr, u, v, w);
     } else {
-        child_avg_kernel<StoreF16><<<grid, kRefineBlock, 0, st>>>(
-            static_cast<const __half*>(fineF), fineKind, g, rx0, ry0, rw, rh, scratch);
+        if (!childDone)
+            child_avg_kernel<StoreF16><<<grid, kRefineBlock, 0, st>>>(
+                static_cast<const __half*>(fineF), fineKind, g, rx0, ry0, rw, rh, scratch);
         restrict_kernel<StoreF16><<<rgrid, rblock, 0, st>>>(
             static_cast<__half*>(coarseF), coarseKind, g, rx0, ry0, rw, rh, neqScaleInv, scratch,
             macro ? rho : nullptr, u, v, w);

@@ -112,6 +112,47 @@ struct ForceSample {
     float fx, fy;
 };
 
+/// CUDA-event pairs around a class of launches (reused across calls), with
+/// the cells and algorithmic bytes each launch covered.
+struct TimedLaunches {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    std::vector<double> cells, bytes;
+    size_t used = 0;
+
+    /// Events for the next launch; records the start on `st`.
+    cudaEvent_t begin(double c, double b, cudaStream_t st) {
+        if (used == ev.size()) {
+            cudaEvent_t a, e;
+            cudaEventCreate(&a);
+            cudaEventCreate(&e);
+            ev.emplace_back(a, e);
+            cells.push_back(0.0);
+            bytes.push_back(0.0);
+        }
+        cells[used] = c;
+        bytes[used] = b;
+        cudaEventRecord(ev[used].first, st);
+        return ev[used++].second;
+    }
+    /// Totals since the last call (ms, launches, cells, bytes); resets.
+    void take(double& t, long long& n, double& c, double& b) {
+        t = c = b = 0.0;
+        for (size_t i = 0; i < used; ++i) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev[i].first, ev[i].second) == cudaSuccess) t += ms;
+            c += cells[i];
+            b += bytes[i];
+        }
+        n = static_cast<long long>(used);
+        used = 0;
+    }
+    void release() {
+        for (auto& pr : ev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        ev.clear(); cells.clear(); bytes.clear();
+        used = 0;
+    }
+};
+
 } // namespace
 } // namespace fcfd
 
@@ -173,6 +214,7 @@ struct fcfd_solver {
     int nanKind = 0;
     bool wmEnabled = false;
     bool zSlipWalls = false;
+    bool fuseChild = true;              // child averages fused into the last fine sub-step
     int wallMethod = 0;                 // FCFD_UTAU_* solve of the wall updates
     std::uint16_t* dNetW = nullptr;     // learned seed: solver-owned BF16 weights
     wallnet::NetDev netView{};
@@ -180,9 +222,8 @@ struct fcfd_solver {
     // ---- diagnostics ----
     long long launches = 0;
     bool collideTiming = false;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> colEv;
-    std::vector<double> colCells, colBytes;
-    size_t colEvUsed = 0;
+    TimedLaunches colT;   // plain stream-collide launches (both levels)
+    TimedLaunches fuseT;  // fine collides with the child averages fused in
     cudaEvent_t tmr0 = nullptr, tmr1 = nullptr;
 
     // ------------------------------------------------------------------
@@ -394,13 +435,10 @@ struct fcfd_solver {
         if (hNan) { cudaFreeHost(hNan); hNan = nullptr; }
         for (cudaEvent_t* e : {&evT0, &evT1, &evForce, &evNan})
             if (*e) { cudaEventDestroy(*e); *e = nullptr; }
-        for (auto& pr : colEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
-        colEv.clear();
-        colCells.clear();
-        colBytes.clear();
+        colT.release();
+        fuseT.release();
         for (cudaEvent_t* e : {&tmr0, &tmr1})
             if (*e) { cudaEventDestroy(*e); *e = nullptr; }
-        colEvUsed = 0;
         timingPending = forcePending = nanPending = false;
         emaStepMs = lastStepMs = 0.0;
         initialized = false;
@@ -408,26 +446,32 @@ struct fcfd_solver {
 
     // ---- stepping ----
     cudaError_t collide(Level& L, const CollideParams& p, float* r, float* uu, float* vv, float* ww) {
-        cudaEvent_t e1 = nullptr, e2 = nullptr;
-        if (collideTiming) {
-            if (colEvUsed == colEv.size()) {
-                cudaEvent_t a, b;
-                cudaEventCreate(&a);
-                cudaEventCreate(&b);
-                colEv.emplace_back(a, b);
-                colCells.push_back(0.0);
-                colBytes.push_back(0.0);
-            }
-            e1 = colEv[colEvUsed].first;
-            e2 = colEv[colEvUsed].second;
-            colCells[colEvUsed] = static_cast<double>(L.n);
-            colBytes[colEvUsed] = L.collideBytes(storage);
-            ++colEvUsed;
-            cudaEventRecord(e1, stream);
-        }
+        cudaEvent_t e2 = collideTiming ? colT.begin(static_cast<double>(L.n), L.collideBytes(storage), stream)
+                                       : nullptr;
         ++launches;
         const cudaError_t e = launch_collide(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, p, r, uu,
                                              vv, ww, L.wm.slip(), stream);
+        if (e2) cudaEventRecord(e2, stream);
+        return e;
+    }
+
+    /// Fine collide of the last sub-step with the restriction's child
+    /// averages fused in (factor 2); timed with the collide launches, its
+    /// algorithmic bytes include the scratch records it writes.
+    cudaError_t collideChild(Level& L, const CollideParams& p) {
+        ChildFuse cf;
+        cf.scratch = dScratch;
+        cf.boxX0 = box.x0;
+        cf.boxY0 = box.y0;
+        restrict_sub_box(geom(), cf.rx0, cf.ry0, cf.rw, cf.rh);
+        cudaEvent_t e2 = collideTiming
+                             ? fuseT.begin(static_cast<double>(L.n),
+                                           L.collideBytes(storage) + 96.0 * static_cast<double>(cf.rw) * cf.rh * coarse.d.nz,
+                                           stream)
+                             : nullptr;
+        ++launches;
+        const cudaError_t e = launch_collide_child(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, p,
+                                                   L.wm.slip(), cf, stream);
         if (e2) cudaEventRecord(e2, stream);
         return e;
     }
@@ -469,6 +513,9 @@ struct fcfd_solver {
                 CollideParams fp = p;
                 fp.tau = tf;
                 fp.writeMacro = 0;
+                // Factor 2: the last sub-step's collide also forms the
+                // restriction's child averages (no re-read of the fine level).
+                const bool fuse = fuseChild && m == 2;
                 for (int k = 0; k < m; ++k) {
                     ++launches;
                     if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src],
@@ -477,16 +524,17 @@ struct fcfd_solver {
                                                  tf / (static_cast<float>(m) * tc), stream);
                         e != cudaSuccess)
                         return e;
-                    if (auto e = collide(fine, fp, nullptr, nullptr, nullptr, nullptr); e != cudaSuccess)
-                        return e;
+                    const cudaError_t ce = (fuse && k == m - 1) ? collideChild(fine, fp)
+                                                                : collide(fine, fp, nullptr, nullptr, nullptr, nullptr);
+                    if (ce != cudaSuccess) return ce;
                     fine.src = 1 - fine.src;
                 }
-                launches += 2;
+                launches += fuse ? 1 : 2;
                 const bool mac = p.writeMacro != 0;
                 if (auto e = launch_restrict_f2c(storage, fine.f[fine.src], fine.kind, coarse.f[1 - coarse.src],
                                                  coarse.kind, geom(), (static_cast<float>(m) * tc) / tf,
                                                  dScratch, mac ? rho : nullptr, mac ? u : nullptr,
-                                                 mac ? v : nullptr, mac ? w : nullptr, stream);
+                                                 mac ? v : nullptr, mac ? w : nullptr, stream, fuse);
                     e != cudaSuccess)
                     return e;
             }
@@ -1232,7 +1280,8 @@ int fcfd_enable_collide_timing(fcfd_solver* s, int enabled) {
     if (!s) return cudaErrorInvalidValue;
     if (s->stream) cudaStreamSynchronize(s->stream);
     s->collideTiming = enabled != 0;
-    s->colEvUsed = 0;
+    s->colT.used = 0;
+    s->fuseT.used = 0;
     return 0;
 }
 
@@ -1240,18 +1289,21 @@ int fcfd_collide_time_ms(fcfd_solver* s, double* total, long long* count, double
                          double* alg_bytes) {
     if (!s || !total || !count) return cudaErrorInvalidValue;
     if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return e;
-    double t = 0.0, c = 0.0, b = 0.0;
-    for (size_t i = 0; i < s->colEvUsed; ++i) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, s->colEv[i].first, s->colEv[i].second) == cudaSuccess) t += ms;
-        c += s->colCells[i];
-        b += s->colBytes[i];
-    }
-    *total = t;
-    *count = static_cast<long long>(s->colEvUsed);
+    double c = 0.0, b = 0.0;
+    s->colT.take(*total, *count, c, b);
     if (cells) *cells = c;
     if (alg_bytes) *alg_bytes = b;
-    s->colEvUsed = 0;
+    return 0;
+}
+
+int fcfd_fused_collide_time_ms(fcfd_solver* s, double* total, long long* count, double* cells,
+                               double* alg_bytes) {
+    if (!s || !total || !count) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return e;
+    double c = 0.0, b = 0.0;
+    s->fuseT.take(*total, *count, c, b);
+    if (cells) *cells = c;
+    if (alg_bytes) *alg_bytes = b;
     return 0;
 }
 
@@ -1350,5 +1402,11 @@ int fcfd_wall_update_timed(fcfd_solver* s, int level, int reps, float* ms, fcfd_
         stats->fallbacks = st.fallbackCells;
         stats->newton_iterations = static_cast<long long>(st.newtonIters);
     }
+    return 0;
+}
+
+int fcfd_set_fused_restriction(fcfd_solver* s, int enabled) {
+    if (!s) return cudaErrorInvalidValue;
+    s->fuseChild = enabled != 0;
     return 0;
 }

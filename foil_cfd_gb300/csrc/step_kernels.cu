@@ -160,11 +160,20 @@ cudaError_t launch_collide(Storage s, const void* src, void* dst, const std::uin
     if (!src || !dst || !kind || d.cells() <= 0) return cudaErrorInvalidValue;
     // FP32 storage runs the reference-order kernels (bit-identical to the
     // reference step without FMA contraction); FP16 storage runs the
-    // pair-sum collision. Both pick the staged kernel when rows fit it.
+    // pair-sum collision. The staged kernel is used only when selected.
     if (s == Storage::F32)
         return launch_collide_f32_ref(static_cast<const float*>(src), static_cast<float*>(dst), kind, d, p,
                                       rho, u, v, w, slip, st);
     return launch_collide_impl<StoreF16, false>(src, dst, kind, d, p, rho, u, v, w, slip, st);
+}
+
+cudaError_t launch_collide_child(Storage s, const void* src, void* dst, const std::uint8_t* kind, LevelDims d,
+                                 const CollideParams& p, SlipField slip, const ChildFuse& cf, cudaStream_t st) {
+    if (!src || !dst || !kind || d.cells() <= 0) return cudaErrorInvalidValue;
+    if (s == Storage::F32)
+        return launch_collide_child_f32(static_cast<const float*>(src), static_cast<float*>(dst), kind, d, p, slip,
+                                        cf, st);
+    return launch_collide_child_impl<StoreF16, false>(src, dst, kind, d, p, slip, cf, st);
 }
 
 cudaError_t launch_init_equilibrium(Storage s, void* f, const std::uint8_t* kind, LevelDims d,

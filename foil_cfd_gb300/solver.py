@@ -290,6 +290,9 @@ class LBMSolver:
         if rc != 0:
             raise SolverError(err.value.decode() or f"initRefinement failed ({rc})")
 
+    def set_fused_restriction(self, enabled: bool):
+        self._lib.fcfd_set_fused_restriction(self._h, int(enabled))
+
     def shutdown_refinement(self):
         self._lib.fcfd_shutdown_refinement(self._h)
 
@@ -335,6 +338,16 @@ class LBMSolver:
         c = C.c_double()
         b = C.c_double()
         self._lib.fcfd_collide_time_ms(self._h, C.byref(t), C.byref(n), C.byref(c), C.byref(b))
+        return t.value, n.value, c.value, b.value
+
+    def fused_collide_time_ms(self):
+        """(total ms, launches, cells, algorithmic bytes) of the timed fine
+        collides with fused child averages since the last call."""
+        t = C.c_double()
+        n = C.c_longlong()
+        c = C.c_double()
+        b = C.c_double()
+        self._lib.fcfd_fused_collide_time_ms(self._h, C.byref(t), C.byref(n), C.byref(c), C.byref(b))
         return t.value, n.value, c.value, b.value
 
     def timer_start(self):

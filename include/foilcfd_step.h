@@ -279,6 +279,11 @@ int fcfd_refinement_info(const fcfd_solver* s, fcfd_refine_info* out);
 /* FP32 SoA import/export of the fine level's current buffer. */
 int fcfd_import_fine_f32(fcfd_solver* s, const float* host_f, size_t count);
 int fcfd_export_fine_f32(fcfd_solver* s, float* host_f, size_t count);
+/* Factor-2 patches: form the restriction's child averages inside the last
+ * fine sub-step's collide (default 1) instead of re-reading the fine level
+ * (lbm_refine.cu:274-429 reads it in the restriction). Both settings give
+ * the same populations bit for bit; 0 is kept for that comparison. */
+int fcfd_set_fused_restriction(fcfd_solver* s, int enabled);
 
 /* ---- host fixture builders (src/sim/wall_model.h, src/geom/) ------------- */
 
@@ -317,13 +322,19 @@ fcfd_patch_box fcfd_derive_patch_box(const fcfd_dims* dims,
 long long fcfd_kernel_launches(const fcfd_solver* s);
 /* Per-kernel timing on the solver stream with CUDA events: when enabled,
  * every stream-collide launch (both levels) is bracketed by events and
- * fcfd_collide_time_ms returns the total ms, the launch count, the cells
+ * fcfd_collide_time_ms returns, for the plain collides, the total ms, the
+ * launch count, the cells
  * those launches covered and their algorithmic DRAM bytes (per cell class:
  * read+write cells 2*19 populations + kind byte, inlet cells 19 + 1,
  * untouched solid/slip/interface cells 1) since the last call. */
 int fcfd_enable_collide_timing(fcfd_solver* s, int enabled);
 int fcfd_collide_time_ms(fcfd_solver* s, double* total_ms, long long* count,
                          double* cells, double* alg_bytes);
+/* The same for the fine collides that form the restriction's child averages
+ * (fcfd_set_fused_restriction): their bytes add the 96-byte scratch record
+ * of every coarse cell of the restricted box. No reference counterpart. */
+int fcfd_fused_collide_time_ms(fcfd_solver* s, double* total_ms, long long* count,
+                               double* cells, double* alg_bytes);
 /* Event pair on the solver stream: start, then stop returns elapsed ms. */
 int fcfd_timer_start(fcfd_solver* s);
 int fcfd_timer_stop(fcfd_solver* s, double* ms);

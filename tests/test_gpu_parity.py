@@ -369,3 +369,25 @@ def test_error_behaviour(fc):
         s.init_refinement(fc.Box(0, 0, 4, 4), 2, np.zeros(1, np.uint8))
     with pytest.raises(fc.SolverError):
         s.import_f32(np.zeros(5, np.float32))
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_fused_child_average_equals_separate_pass(fc, storage):
+    """The last fine sub-step's collide with the restriction's child averages
+    fused in gives the same coarse and fine populations, bit for bit, as the
+    separate child-average pass (airfoil tunnel, 2:1 patch, wall model)."""
+    from foil_cfd_gb300.tunnels import airfoil_tunnel
+    t = airfoil_tunnel(160, 64, 16, chord=64, aoa=6.0)
+    out = {}
+    for fused in (True, False):
+        s = fc.LBMSolver()
+        s.init(t.dims, fc.scaling_direct(0.52, t.u_lat, t.chord_cells), t.flags, storage=storage, les_cs=0.1)
+        s.set_wall_model_enabled(True)
+        s.set_startup_ramp_enabled(False)
+        s.reset()
+        s.init_refinement(t.box, t.factor, t.fine_flags)
+        s.set_fused_restriction(fused)
+        assert s.step_n(30) == 0 and not s.nan_detected()
+        out[fused] = (s.export_f32(), s.export_fine_f32())
+    assert np.array_equal(out[True][0], out[False][0])
+    assert np.array_equal(out[True][1], out[False][1])
