@@ -128,6 +128,8 @@ _SIGS = {
     "fcfd_import_fine_f32": (C.c_int, [P, P, C.c_size_t]),
     "fcfd_export_fine_f32": (C.c_int, [P, P, C.c_size_t]),
     "fcfd_set_fused_restriction": (C.c_int, [P, C.c_int]),
+    "fcfd_set_q_links": (C.c_int, [P, C.c_int, P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int]),
+    "fcfd_q_link_info": (C.c_int, [P, C.c_int, P, P, P]),
     "fcfd_build_wall_list": (C.c_longlong, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P]),
     "fcfd_boundary_flags": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
     "fcfd_naca4": (C.c_int, [C.c_char_p, C.c_int, P, C.c_int]),

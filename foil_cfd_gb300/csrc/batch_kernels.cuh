@@ -44,6 +44,8 @@ batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, un
         a.rho = a.u = a.v = a.w = nullptr;
         a.uwx = a.uwy = a.uwz = nullptr;
         a.status = nullptr;
+        a.qFrac = nullptr;
+        a.ffMask = nullptr;
         const T* src = static_cast<const T*>(tp.f[parity]);
         T* dst = static_cast<T*>(tp.f[parity ^ 1]);
         const unsigned ny = static_cast<unsigned>(tp.ny);

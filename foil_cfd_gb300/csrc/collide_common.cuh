@@ -40,6 +40,8 @@ struct CollideArgs {
     float *rho, *u, *v, *w;
     const std::uint16_t *uwx, *uwy, *uwz;
     int* status; // staged kernel: nonzero when a pipeline wait timed out
+    const std::uint8_t* qFrac;   // q-LIBB cut bytes [cell * 19 + q], or null
+    const std::uint32_t* ffMask; // q-LIBB two-node bits [cell]
 };
 
 // ---- equilibrium in the reference expression order ------------------------
@@ -248,7 +250,7 @@ __device__ __forceinline__ void gather_bulk(const typename S::T* __restrict__ sr
 
 /// Near-wall fluid cell: the upstream flag picks the (slot, cell) pair per
 /// link; the wall-model Ladd term 6 w_q (c_q . u_w) on solid links.
-template <class S, bool WM>
+template <class S, bool WM, bool QL = false>
 __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ src,
                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a,
                                             const Nbr& b, unsigned cell, int y, int z, float (&f)[kQ]) {
@@ -270,6 +272,26 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
         const int qs = solid ? opp(q) : (slipY ? mir_y(q) : (slipZ ? mir_z(q) : q));
         const unsigned cs = solid ? cell : (slipY ? pY : (slipZ ? pZ : pn));
         float fq = S::ld(src + static_cast<long long>(qs) * n, cs, wgt(q));
+        // Interpolated bounce-back (Bouzidi 2001) on a solid link with an
+        // analytic cut fraction, in the reference's expression order
+        // (lbm_core.cu:332-364): the wall sits at q = byte/255 of the link.
+        if (QL && solid) {
+            const std::uint8_t qb = a.qFrac[static_cast<long long>(cell) * kQ + q];
+            if (qb != 0) {
+                const float qf = static_cast<float>(qb) * (1.0f / 255.0f);
+                const float fOut = S::ld(src + static_cast<long long>(q) * n, cell, wgt(q));
+                if (qf >= 0.5f) {
+                    const float inv2q = 0.5f / qf;
+                    fq = inv2q * fOut + (1.0f - inv2q) * fq;
+                } else if (a.ffMask[cell] & (1u << q)) {
+                    // Second fluid node x + c_q (opposite the wall).
+                    const unsigned pff = b.sx[1 - cx(q)] + unx * (b.sy[1 - cy(q)] + uny * b.sz[1 - cz(q)]);
+                    const float fOutFF = S::ld(src + static_cast<long long>(q) * n, pff, wgt(q));
+                    fq = 2.0f * qf * fOut + (1.0f - 2.0f * qf) * fOutFF;
+                }
+                // else: x + c_q solid (thin vane): keep the half-way value.
+            }
+        }
         if constexpr (WM) {
             if (solid) {
                 if (!uwLoaded) {
@@ -297,7 +319,7 @@ __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, con
 
 /// One full cell update at (x, y, z): boundary cells by flag, fluid cells
 /// by their 19 pulls (bulk or near-wall path) and the collision.
-template <class S, bool WM, bool EXACT>
+template <class S, bool WM, bool EXACT, bool QL = false>
 __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a, int x, int y,
                                             int z) {
@@ -312,20 +334,20 @@ __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ sr
     const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
     float f[kQ];
     if (!(k & kNearWall)) gather_bulk<S>(src, a, b, f);
-    else gather_wall<S, WM>(src, kind, a, b, cell, y, z, f);
+    else gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, f);
     finish_cell<S, EXACT>(dst, a, cell, f);
 }
 
 // ---- one cell per thread -----------------------------------------------------
 constexpr int kCellBlockX = 128;
 
-template <class S, bool WM, bool EXACT>
+template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kCellBlockX)
 collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                     const std::uint8_t* __restrict__ kind, CollideArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= a.nx) return;
-    collide_one<S, WM, EXACT>(src, dst, kind, a, x, blockIdx.y, blockIdx.z);
+    collide_one<S, WM, EXACT, QL>(src, dst, kind, a, x, blockIdx.y, blockIdx.z);
 }
 
 // ---- last fine sub-step with the restriction's child averages fused in --------
@@ -340,7 +362,7 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
 // saves the stand-alone pass's full re-read of the fine populations.
 constexpr int kFuseX = 128;
 
-template <class S, bool WM, bool EXACT>
+template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kFuseX, 8)
 collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                      const std::uint8_t* __restrict__ kind, CollideArgs a, ChildFuse cf) {
@@ -369,7 +391,7 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                 if (flag == kFluid) {
                     const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
                     if (!(k & kNearWall)) gather_bulk<S>(src, a, b, v);
-                    else gather_wall<S, WM>(src, kind, a, b, cell, y, z, v);
+                    else gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, v);
                     float rr, ux, uy, uz;
                     collide_body<EXACT>(v, a, rr, ux, uy, uz);
 #pragma unroll
@@ -422,15 +444,19 @@ cudaError_t launch_collide_child_impl(const void* srcv, void* dstv, const std::u
     a.rho = a.u = a.v = a.w = nullptr;
     a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
     a.status = nullptr;
+    a.qFrac = p.qFrac; a.ffMask = p.ffMask;
     const dim3 block(kFuseX);
     const dim3 grid(static_cast<unsigned>((d.nx + kFuseX - 1) / kFuseX), static_cast<unsigned>(d.ny / 2),
                     static_cast<unsigned>(d.nz / 2));
     const T* src = static_cast<const T*>(srcv);
     T* dst = static_cast<T*>(dstv);
+    const bool ql = a.qFrac != nullptr;
     if (slip.active())
-        collide_child_kernel<S, true, EXACT><<<grid, block, 0, st>>>(src, dst, kind, a, cf);
+        (ql ? collide_child_kernel<S, true, EXACT, true> : collide_child_kernel<S, true, EXACT, false>)
+            <<<grid, block, 0, st>>>(src, dst, kind, a, cf);
     else
-        collide_child_kernel<S, false, EXACT><<<grid, block, 0, st>>>(src, dst, kind, a, cf);
+        (ql ? collide_child_kernel<S, false, EXACT, true> : collide_child_kernel<S, false, EXACT, false>)
+            <<<grid, block, 0, st>>>(src, dst, kind, a, cf);
     return cudaGetLastError();
 }
 
@@ -533,7 +559,7 @@ __device__ __forceinline__ void issue_row(const typename S::T* __restrict__ src,
     (void)kindBytes;
 }
 
-template <class S, bool WM, bool EXACT>
+template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kStagedThreads, 2)
 collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                       const std::uint8_t* __restrict__ kind, CollideArgs a, int stages) {
@@ -621,7 +647,7 @@ collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __re
                 for (int q = 0; q < kQ; ++q) f[q] = S::lds(sbase + q * rowBytes, xs[1 + cx(q)], wgt(q));
             } else {
                 const Nbr b = neighbours(x, y, z, nx, a.ny, a.nz);
-                gather_wall<S, WM>(src, kind, a, b, cell, y, z, f);
+                gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, f);
             }
             finish_cell<S, EXACT>(dst, a, cell, f);
         }
@@ -676,6 +702,7 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     a.rho = rho; a.u = u; a.v = v; a.w = w;
     a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
     a.status = p.status;
+    a.qFrac = p.qFrac; a.ffMask = p.ffMask;
     const T* src = static_cast<const T*>(srcv);
     T* dst = static_cast<T*>(dstv);
     const bool wm = slip.active();
@@ -686,11 +713,13 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     // on shared-memory reads and ring bookkeeping.
     const bool staged = p.status && plan.stages >= 2 && p.kernel == 2;
     if (staged) {
-        auto kern = wm ? collide_staged_kernel<S, true, EXACT> : collide_staged_kernel<S, false, EXACT>;
+        const bool ql = a.qFrac != nullptr;
+        auto kern = wm ? (ql ? collide_staged_kernel<S, true, EXACT, true> : collide_staged_kernel<S, true, EXACT, false>)
+                       : (ql ? collide_staged_kernel<S, false, EXACT, true> : collide_staged_kernel<S, false, EXACT, false>);
         // The dynamic shared-memory limit is a per-kernel attribute: raise it
         // once to the device's opt-in maximum (levels of one solver use
         // different stage sizes); occupancy is cached per (kernel, size).
-        static const void* raised[4] = {};
+        static const void* raised[8] = {};
         bool isRaised = false;
         for (const void* k : raised) isRaised |= (k == reinterpret_cast<const void*>(kern));
         if (!isRaised) {
@@ -705,7 +734,7 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
                 if (!k) { k = reinterpret_cast<const void*>(kern); break; }
         }
         struct Entry { const void* k; size_t smem; int perSm; };
-        static Entry cache[8] = {};
+        static Entry cache[16] = {};
         int perSm = 0;
         for (const Entry& c : cache)
             if (c.k == reinterpret_cast<const void*>(kern) && c.smem == plan.smem) perSm = c.perSm;
@@ -726,8 +755,13 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     const int bx = d.nx >= kCellBlockX ? kCellBlockX : ((d.nx + 31) / 32) * 32;
     const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),
                     static_cast<unsigned>(d.nz));
-    if (wm) collide_cell_kernel<S, true, EXACT><<<grid, bx, 0, st>>>(src, dst, kind, a);
-    else collide_cell_kernel<S, false, EXACT><<<grid, bx, 0, st>>>(src, dst, kind, a);
+    if (a.qFrac) {
+        if (wm) collide_cell_kernel<S, true, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a);
+        else collide_cell_kernel<S, false, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a);
+    } else {
+        if (wm) collide_cell_kernel<S, true, EXACT, false><<<grid, bx, 0, st>>>(src, dst, kind, a);
+        else collide_cell_kernel<S, false, EXACT, false><<<grid, bx, 0, st>>>(src, dst, kind, a);
+    }
     return cudaGetLastError();
 }
 

@@ -35,6 +35,10 @@ struct CollideParams {
     int writeMacro = 0;
     int* status = nullptr;  ///< Device int set nonzero if a staged copy wait timed out.
     int kernel = 0;         ///< 0 automatic, 1 one-cell kernel, 2 staged kernel.
+    /// Interpolated bounce-back (q-LIBB) link field of the level, or null:
+    /// cut bytes [cell * 19 + q] (q = byte / 255) and two-node bits [cell].
+    const std::uint8_t* qFrac = nullptr;
+    const std::uint32_t* ffMask = nullptr;
 };
 
 /// Half-bit slip field of a level (WallSlipView, lbm_core.cuh:201-208).

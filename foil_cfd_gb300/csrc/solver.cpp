@@ -86,6 +86,10 @@ struct Level {
     int linkCount = 0;
     double* dPartials = nullptr;
     WMLevel wm;
+    // Interpolated bounce-back link field (null when the level has none).
+    std::uint8_t* dQFrac = nullptr;
+    std::uint32_t* dFFMask = nullptr;
+    int qLinks = 0, qFallback = 0;
     // Cell classes of the level for the collide's algorithmic byte count:
     // cells the step reads and writes (fluid, outlets), inlet cells (write
     // only) and cells it leaves untouched (solid, slip, interface; the kind
@@ -101,6 +105,8 @@ struct Level {
     void free_all() {
         dfree(f[0]); dfree(f[1]); dfree(flags); dfree(kind);
         dfree(dLinkCells); dfree(dLinkMasks); dfree(dPartials);
+        dfree(dQFrac); dfree(dFFMask);
+        qLinks = qFallback = 0;
         wm.free();
         hostFlags.clear(); surfaceRef.clear();
         linkCount = 0; src = 0; n = 0; d = LevelDims{};
@@ -449,7 +455,10 @@ struct fcfd_solver {
         cudaEvent_t e2 = collideTiming ? colT.begin(static_cast<double>(L.n), L.collideBytes(storage), stream)
                                        : nullptr;
         ++launches;
-        const cudaError_t e = launch_collide(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, p, r, uu,
+        CollideParams lp = p;
+        lp.qFrac = L.dQFrac;
+        lp.ffMask = L.dFFMask;
+        const cudaError_t e = launch_collide(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, lp, r, uu,
                                              vv, ww, L.wm.slip(), stream);
         if (e2) cudaEventRecord(e2, stream);
         return e;
@@ -470,7 +479,10 @@ struct fcfd_solver {
                                            stream)
                              : nullptr;
         ++launches;
-        const cudaError_t e = launch_collide_child(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, p,
+        CollideParams lp = p;
+        lp.qFrac = L.dQFrac;
+        lp.ffMask = L.dFFMask;
+        const cudaError_t e = launch_collide_child(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, lp,
                                                    L.wm.slip(), cf, stream);
         if (e2) cudaEventRecord(e2, stream);
         return e;
@@ -1408,5 +1420,42 @@ int fcfd_wall_update_timed(fcfd_solver* s, int level, int reps, float* ms, fcfd_
 int fcfd_set_fused_restriction(fcfd_solver* s, int enabled) {
     if (!s) return cudaErrorInvalidValue;
     s->fuseChild = enabled != 0;
+    return 0;
+}
+
+// ---- interpolated bounce-back link fields (setCoarseQLinks / setFineQLinks,
+// src/sim/lbm_solver.cpp:1041-1056; uploadQLevel, :373-410) ---------------
+
+int fcfd_set_q_links(fcfd_solver* s, int level, const uint8_t* qFrac, size_t nq, const uint32_t* ffMask,
+                     size_t nm, int links, int fallback) {
+    Level* L = level_of(s, level);
+    if (!L) return cudaErrorInvalidValue;
+    cudaStreamSynchronize(s->stream);
+    dfree(L->dQFrac);
+    dfree(L->dFFMask);
+    L->qLinks = L->qFallback = 0;
+    if (nq == 0) return 0;  // cleared: plain half-way bounce-back
+    if (!qFrac || !ffMask || nq != static_cast<size_t>(L->n) * 19 || nm != static_cast<size_t>(L->n))
+        return cudaErrorInvalidValue;
+    if (auto e = dalloc(&L->dQFrac, nq); e != cudaSuccess) return e;
+    if (auto e = dalloc(&L->dFFMask, nm * 4); e != cudaSuccess) { dfree(L->dQFrac); return e; }
+    cudaError_t e = cudaMemcpy(L->dQFrac, qFrac, nq, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(L->dFFMask, ffMask, nm * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        dfree(L->dQFrac);
+        dfree(L->dFFMask);
+        return e;
+    }
+    L->qLinks = links;
+    L->qFallback = fallback;
+    return 0;
+}
+
+int fcfd_q_link_info(fcfd_solver* s, int level, int* active, int* links, int* fallback) {
+    Level* L = level_of(s, level);
+    if (!L) return cudaErrorInvalidValue;
+    if (active) *active = L->dQFrac ? 1 : 0;
+    if (links) *links = L->qLinks;
+    if (fallback) *fallback = L->qFallback;
     return 0;
 }

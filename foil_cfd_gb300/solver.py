@@ -290,6 +290,22 @@ class LBMSolver:
         if rc != 0:
             raise SolverError(err.value.decode() or f"initRefinement failed ({rc})")
 
+    def set_q_links(self, level: int, q_frac=None, ff_mask=None, links: int = 0, fallback: int = 0):
+        """Interpolated bounce-back field of a level (None clears it)."""
+        if q_frac is None:
+            rc = self._lib.fcfd_set_q_links(self._h, level, None, 0, None, 0, 0, 0)
+        else:
+            qf = np.ascontiguousarray(q_frac, np.uint8)
+            fm = np.ascontiguousarray(ff_mask, np.uint32)
+            rc = self._lib.fcfd_set_q_links(self._h, level, ptr(qf), qf.size, ptr(fm), fm.size, links, fallback)
+        if rc:
+            raise SolverError(f"q-link upload failed ({rc})")
+
+    def q_link_info(self, level: int = 0):
+        a, l, f = C.c_int(), C.c_int(), C.c_int()
+        self._lib.fcfd_q_link_info(self._h, level, C.byref(a), C.byref(l), C.byref(f))
+        return bool(a.value), l.value, f.value
+
     def set_fused_restriction(self, enabled: bool):
         self._lib.fcfd_set_fused_restriction(self._h, int(enabled))
 

@@ -265,6 +265,20 @@ int fcfd_import_wall_state(fcfd_solver* s, int level, const float* utau,
 int fcfd_wall_update_now(fcfd_solver* s, int level, float nu_lat,
                          float ut_cutoff);
 
+/* ---- interpolated bounce-back (q-LIBB) link fields ----------------------- */
+
+/* setCoarseQLinks / setFineQLinks (lbm_solver.h:330-340, lbm_solver.cpp:
+ * 1041-1056): per cell and direction the cut fraction of a resolved surface
+ * on a solid link (byte b -> q = b/255, 0 = plain half-way bounce-back),
+ * q_frac[cell * 19 + q] (count = 19 * cells), and per cell the bits of the
+ * links whose second fluid node x + c_q exists, ff_mask[cell]. The collide
+ * then applies Bouzidi's linear interpolation on those links
+ * (lbm_core.cu:332-364). level 0 coarse, 1 fine; nq == 0 clears the field.
+ * links / fallback are the caller's counts, kept for fcfd_q_link_info. */
+int fcfd_set_q_links(fcfd_solver* s, int level, const uint8_t* q_frac, size_t nq,
+                     const uint32_t* ff_mask, size_t nm, int links, int fallback);
+int fcfd_q_link_info(fcfd_solver* s, int level, int* active, int* links, int* fallback);
+
 /* ---- refinement (lbm_solver.h:192-246) ------------------------------------ */
 
 /* initRefinement (lbm_solver.cpp:1812-1888). */

@@ -115,7 +115,8 @@ void equilibrium19(T rho, T ux, T uy, T uz, T feq[Q]) {
 template <class T>
 void collide(const Dims& d, const T* src, T* dst, const uint8_t* flags, T tau0, T lambda, T smagPre,
              T uIn, int writeMacro, T* mr, T* mu, T* mv, T* mw, const uint16_t* uwxA,
-             const uint16_t* uwyA, const uint16_t* uwzA) {
+             const uint16_t* uwyA, const uint16_t* uwzA, const uint8_t* qFrac = nullptr,
+             const uint32_t* ffMask = nullptr) {
     const long long N = d.n();
     const bool wm = uwxA && uwyA && uwzA;
 #pragma omp parallel for schedule(static)
@@ -168,6 +169,23 @@ void collide(const Dims& d, const T* src, T* dst, const uint8_t* flags, T tau0, 
             const int qs = solid ? OPP[q] : (slipY ? MIRY[q] : (slipZ ? MIRZ[q] : q));
             const long long cs = solid ? cell : (slipY ? pY : (slipZ ? pZ : pn));
             fpop[q] = src[qs * N + cs];
+            // Interpolated bounce-back (Bouzidi 2001) on a solid link with an
+            // analytic cut fraction (lbm_core.cu:332-364).
+            if (qFrac && solid) {
+                const uint8_t qb = qFrac[cell * Q + q];
+                if (qb != 0) {
+                    const T qf = T(qb) * (T(1) / T(255));
+                    const T fOut = src[q * N + cell];
+                    if (qf >= T(0.5)) {
+                        const T inv2q = T(0.5) / qf;
+                        fpop[q] = inv2q * fOut + (T(1) - inv2q) * fpop[q];
+                    } else if (ffMask[cell] & (1u << q)) {
+                        const long long pff = d.at(wrap(x + CX[q], d.nx), wrap(y + CY[q], d.ny), wrap(z + CZ[q], d.nz));
+                        const T fOutFF = src[q * N + pff];
+                        fpop[q] = T(2) * qf * fOut + (T(1) - T(2) * qf) * fOutFF;
+                    }
+                }
+            }
             if (wm && solid) {
                 if (!uwLoaded) {
                     uwx = (T)h2f(uwxA[cell]); uwy = (T)h2f(uwyA[cell]); uwz = (T)h2f(uwzA[cell]);
@@ -276,17 +294,18 @@ extern "C" {
 
 void oracle_collide_f32(int nx, int ny, int nz, const float* src, float* dst, const uint8_t* flags, float tau0,
                         float lambda, float smagPre, float uIn, int writeMacro, float* r, float* u, float* v,
-                        float* w, const uint16_t* uwx, const uint16_t* uwy, const uint16_t* uwz) {
+                        float* w, const uint16_t* uwx, const uint16_t* uwy, const uint16_t* uwz,
+                        const uint8_t* qFrac, const uint32_t* ffMask) {
     collide<float>(Dims{nx, ny, nz}, src, dst, flags, tau0, lambda, smagPre, uIn, writeMacro, r, u, v, w, uwx,
-                   uwy, uwz);
+                   uwy, uwz, qFrac, ffMask);
 }
 
 void oracle_collide_f64(int nx, int ny, int nz, const double* src, double* dst, const uint8_t* flags,
                         double tau0, double lambda, double smagPre, double uIn, int writeMacro, double* r,
                         double* u, double* v, double* w, const uint16_t* uwx, const uint16_t* uwy,
-                        const uint16_t* uwz) {
+                        const uint16_t* uwz, const uint8_t* qFrac, const uint32_t* ffMask) {
     collide<double>(Dims{nx, ny, nz}, src, dst, flags, tau0, lambda, smagPre, uIn, writeMacro, r, u, v, w, uwx,
-                    uwy, uwz);
+                    uwy, uwz, qFrac, ffMask);
 }
 
 void oracle_force_f32(int nx, int ny, int nz, const float* f, const uint8_t* flags, const uint16_t* uwx,

@@ -55,8 +55,8 @@ def lib():
         _lib = C.CDLL(str(build()))
         P = C.c_void_p
         i, f, d = C.c_int, C.c_float, C.c_double
-        _lib.oracle_collide_f32.argtypes = [i, i, i, P, P, P, f, f, f, f, i, P, P, P, P, P, P, P]
-        _lib.oracle_collide_f64.argtypes = [i, i, i, P, P, P, d, d, d, d, i, P, P, P, P, P, P, P]
+        _lib.oracle_collide_f32.argtypes = [i, i, i, P, P, P, f, f, f, f, i, P, P, P, P, P, P, P, P, P]
+        _lib.oracle_collide_f64.argtypes = [i, i, i, P, P, P, d, d, d, d, i, P, P, P, P, P, P, P, P, P]
         _lib.oracle_force_f32.argtypes = [i, i, i, P, P, P, P, P, P]
         _lib.oracle_force_f64.argtypes = [i, i, i, P, P, P, P, P, P]
         _lib.oracle_init_eq.argtypes = [i, i, i, P, P, f]
@@ -92,8 +92,10 @@ def smag_prefactor(cs: float) -> float:
     return float(np.float32(18.0) * np.float32(1.41421356) * np.float32(cs) * np.float32(cs))
 
 
-def collide(dims, src, flags, tau, lam, smag_pre, u_in, write_macro=False, slip=None, dst=None):
+def collide(dims, src, flags, tau, lam, smag_pre, u_in, write_macro=False, slip=None, dst=None, qlinks=None):
     """One reference stream-collide over the whole grid; returns (dst, macro).
+    ``qlinks`` = (qFrac uint8 [cell * 19 + q], ffMask uint32 [cell]) turns on
+    the interpolated bounce-back (q-LIBB) on solid links.
 
     ``dst`` is the other buffer of an A/B pair and is written in place; the
     cells a step does not write (solid, slip, interface) keep its previous
@@ -107,8 +109,10 @@ def collide(dims, src, flags, tau, lam, smag_pre, u_in, write_macro=False, slip=
     macro = [np.zeros(n, dtype) for _ in range(4)] if write_macro else [None] * 4
     sx = [None] * 3 if slip is None else [np.ascontiguousarray(s) for s in slip]
     fn = lib().oracle_collide_f32 if dtype == np.float32 else lib().oracle_collide_f64
+    ql = (None, None) if qlinks is None else (np.ascontiguousarray(qlinks[0], np.uint8),
+                                               np.ascontiguousarray(qlinks[1], np.uint32))
     fn(nx, ny, nz, _p(src), _p(dst), _p(flags), tau, lam, smag_pre, u_in, int(write_macro),
-       *[_p(m) for m in macro], *[_p(s) for s in sx])
+       *[_p(m) for m in macro], *[_p(s) for s in sx], _p(ql[0]), _p(ql[1]))
     return dst, (macro if write_macro else None)
 
 

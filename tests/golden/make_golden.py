@@ -7,7 +7,8 @@ reference tree (``FOILCFD_REFERENCE``, default /root/reference) and is run
 by hand in the build container; the fixtures it writes are committed, so
 the tests never need the reference at run time.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every case
+    python tests/golden/make_golden.py qlibb      # one case
 """
 from __future__ import annotations
 
@@ -36,6 +37,7 @@ def load():
     libs = ref_build.build()
     core = C.CDLL(str(libs["core"]))
     core.ref_collide.argtypes = [I, I, I, P, P, P, F, F, F, F, I, P, P, P, P, P, P, P]
+    core.ref_collide_q.argtypes = [I, I, I, P, P, P, F, F, F, F, I, P, P, P, P, P, P, P, P, P]
     core.ref_force.argtypes = [I, I, I, P, P, P, P, P, P]
     core.ref_init.argtypes = [I, I, I, P, P, F, F, C.c_uint, I]
     wall = C.CDLL(str(libs["wall"]))
@@ -77,10 +79,11 @@ def reset_state(core, dims, flags, u):
     return f
 
 
-def run_collide(core, dims, f, flags, steps, tau, lam, cs, u_in, slip=None):
+def run_collide(core, dims, f, flags, steps, tau, lam, cs, u_in, slip=None, qlinks=None):
     """`steps` steps on an A/B buffer pair: A = the uploaded state, B = the
     reset state (uploadF writes the current buffer only), so cells a step
-    never writes carry the same contents the reference solver would have."""
+    never writes carry the same contents the reference solver would have.
+    qlinks = (qFrac, ffMask) runs the reference's q-LIBB instantiation."""
     n = int(np.prod(dims))
     mac = [np.zeros(n, np.float32) for _ in range(4)]
     sl = slip if slip is not None else [None] * 3
@@ -88,10 +91,61 @@ def run_collide(core, dims, f, flags, steps, tau, lam, cs, u_in, slip=None):
     other = reset_state(core, dims, flags, u_in)
     for s in range(steps):
         dst = other
-        core.ref_collide(*dims, p(f), p(dst), p(flags), tau, lam, cs, u_in, int(s == steps - 1),
-                         *[p(m) for m in mac], *[p(x) for x in sl])
+        if qlinks is None:
+            core.ref_collide(*dims, p(f), p(dst), p(flags), tau, lam, cs, u_in, int(s == steps - 1),
+                             *[p(m) for m in mac], *[p(x) for x in sl])
+        else:
+            core.ref_collide_q(*dims, p(f), p(dst), p(flags), tau, lam, cs, u_in, int(s == steps - 1),
+                               *[p(m) for m in mac], *[p(x) for x in sl], p(qlinks[0]), p(qlinks[1]))
         f, other = dst, f
     return f, mac
+
+
+def qlink_field(dims, flags, rng, p_link=0.8, p_ff=0.8):
+    """Seeded q-LIBB field: a cut byte in [1, 255] on ~p_link of the solid
+    links of fluid cells (the pull source x - c_q solid), and the two-node
+    bit where x + c_q is fluid (~p_ff of those)."""
+    nx, ny, nz = dims
+    fl = flags.reshape(nz, ny, nx)
+    qf = np.zeros((nz, ny, nx, 19), np.uint8)
+    ff = np.zeros((nz, ny, nx), np.uint32)
+    for z in range(nz):
+        for y in range(ny):
+            for x in range(nx):
+                if fl[z, y, x] != 0:
+                    continue
+                for q in range(1, 19):
+                    xs, ys, zs = x - CX[q], y - CY[q], (z - CZ[q]) % nz
+                    if not (0 <= xs < nx and 0 <= ys < ny) or fl[zs, ys, xs] != 1:
+                        continue
+                    if rng.random() < p_link:
+                        qf[z, y, x, q] = rng.integers(1, 256)
+                    xf, yf, zf = x + CX[q], y + CY[q], (z + CZ[q]) % nz
+                    if 0 <= xf < nx and 0 <= yf < ny and fl[zf, yf, xf] == 0 and rng.random() < p_ff:
+                        ff[z, y, x] |= np.uint32(1 << q)
+    return qf.ravel(), ff.ravel()
+
+
+def case_qlibb(core):
+    """Interpolated bounce-back (streamCollideKernel<WM, true>) around the
+    square block of the collide case, with and without wall slip."""
+    rng = np.random.default_rng(20261204)
+    dims = (24, 16, 8)
+    n = int(np.prod(dims))
+    fl = open_flags(24, 16, 8)
+    fl[:, 6:10, 8:12] = 1
+    flags = fl.ravel().copy()
+    f0 = perturbed_state(rng, n)
+    qfrac, ffmask = qlink_field(dims, flags, rng)
+    params = dict(tau=0.52, lam=3.0 / 16.0, cs=0.1733, u_in=0.05)
+    f1, m1 = run_collide(core, dims, f0, flags, 1, qlinks=(qfrac, ffmask), **params)
+    f20, m20 = run_collide(core, dims, f0, flags, 20, qlinks=(qfrac, ffmask), **params)
+    slip = [(0.01 * rng.standard_normal(n)).astype(np.float16).view(np.uint16) for _ in range(3)]
+    f20w, m20w = run_collide(core, dims, f0, flags, 20, slip=slip, qlinks=(qfrac, ffmask), **params)
+    np.savez_compressed(OUT / "qlibb.npz", dims=np.array(dims), flags=flags, f0=f0, qfrac=qfrac, ffmask=ffmask,
+                        params=np.array([params["tau"], params["lam"], params["cs"], params["u_in"]], np.float32),
+                        f1=f1, m1=np.stack(m1), f20=f20, m20=np.stack(m20), slip=np.stack(slip), f20w=f20w,
+                        m20w=np.stack(m20w))
 
 
 def case_collide(core, rng):
@@ -279,8 +333,17 @@ def case_refine(core, refine, rng):
                         taus=np.array([tauC, tauF], np.float32))
 
 
-def main():
+def main(cases=None):
+    """All cases, or the named ones (e.g. `qlibb`) to leave the others'
+    fixtures untouched."""
     core, wall, refine, wl = load()
+    if cases:
+        for c in cases:
+            if c == "qlibb":
+                case_qlibb(core)
+            else:
+                raise SystemExit(f"unknown case {c}")
+        return
     rng = np.random.default_rng(20261203)
     case_collide(core, rng)
     case_taylor_green(core)
@@ -288,9 +351,10 @@ def main():
     case_wall(core, wall, wl, rng)
     case_wall_list(wl)
     case_refine(core, refine, rng)
+    case_qlibb(core)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -391,3 +391,36 @@ def test_fused_child_average_equals_separate_pass(fc, storage):
         out[fused] = (s.export_f32(), s.export_fine_f32())
     assert np.array_equal(out[True][0], out[False][0])
     assert np.array_equal(out[True][1], out[False][1])
+
+
+@pytest.mark.parametrize("kernel", ["cell", "staged"])
+@pytest.mark.parametrize("case,steps,slip", [("f1", 1, False), ("f20", 20, False), ("f20w", 20, True)])
+def test_qlibb_collide_vs_reference_golden(fc, golden, case, steps, slip, kernel):
+    """Interpolated bounce-back (the reference's streamCollideKernel<WM,
+    true>) through the C ABI against the reference's own output."""
+    g = golden("qlibb")
+    dims = tuple(int(x) for x in g["dims"])
+    tau, lam, cs, u_in = (float(x) for x in g["params"])
+    flags = g["flags"]
+    s = make(fc, dims, flags, tau, u_in, cs, kernel=kernel)
+    s.set_q_links(0, g["qfrac"], g["ffmask"], links=int((g["qfrac"] > 0).sum()))
+    assert s.q_link_info(0)[:2] == (True, int((g["qfrac"] > 0).sum()))
+    if slip:
+        s.set_wall_model_enabled(True)
+        utau = np.zeros(s.wall_count(0), np.float32)
+        s.import_wall_state(0, utau, g["slip"])
+    s.import_f32(g["f0"])
+    if slip:
+        for _ in range(steps):
+            assert s.step_n(1) == 0
+            s.import_wall_state(0, utau, g["slip"])
+    else:
+        assert s.step_n(steps) == 0
+    f = s.export_f32()
+    m = written_mask(flags)
+    assert np.array_equal(f.reshape(19, -1)[:, m], g[case].reshape(19, -1)[:, m])
+    macro = np.stack(s.download_macro())
+    assert np.array_equal(macro[:, m], g["m" + case[1:]][:, m])
+    # Clearing the field returns to plain half-way bounce-back.
+    s.set_q_links(0, None)
+    assert s.q_link_info(0)[0] is False
