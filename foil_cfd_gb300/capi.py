@@ -55,6 +55,11 @@ class RefineInfo(C.Structure):
                 ("forces_from_fine", C.c_int), ("vram_bytes", C.c_double)]
 
 
+class FinerInfo(C.Structure):
+    _fields_ = [("active", C.c_int), ("factor", C.c_int), ("box", PatchBox), ("dims", Dims),
+                ("vram_bytes", C.c_double)]
+
+
 class WallNetNorm(C.Structure):
     _fields_ = [("in_mean", C.c_float * 3), ("in_std", C.c_float * 3), ("out_mean", C.c_float),
                 ("out_std", C.c_float)]
@@ -129,6 +134,14 @@ _SIGS = {
     "fcfd_export_fine_f32": (C.c_int, [P, P, C.c_size_t]),
     "fcfd_set_fused_restriction": (C.c_int, [P, C.c_int]),
     "fcfd_set_q_links": (C.c_int, [P, C.c_int, P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int]),
+    "fcfd_init_finer_refinement": (C.c_int, [P, C.POINTER(PatchBox), C.c_int, P, C.c_size_t, C.c_char_p,
+                                             C.c_size_t]),
+    "fcfd_shutdown_finer_refinement": (None, [P]),
+    "fcfd_set_refined_finer_flags": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_set_refined_finer_surface_reference": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_finer_refinement_info": (C.c_int, [P, C.POINTER(FinerInfo)]),
+    "fcfd_import_finer_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_export_finer_f32": (C.c_int, [P, P, C.c_size_t]),
     "fcfd_q_link_info": (C.c_int, [P, C.c_int, P, P, P]),
     "fcfd_build_wall_list": (C.c_longlong, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P]),
     "fcfd_boundary_flags": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),

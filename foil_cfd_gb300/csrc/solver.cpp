@@ -182,6 +182,14 @@ struct fcfd_solver {
     int factor = 2;
     fcfd_patch_box box{};
     fcfd_scaling fineScaling{};
+    // Nested finer level inside the fine patch (box in fine cells).
+    Level finer;
+    bool finerActive = false;
+    int finerFactor = 2;
+    fcfd_patch_box finerBox{};
+    std::uint32_t *dShellFiner = nullptr, *dSeedFiner = nullptr;
+    int shellCountFiner = 0, seedCountFiner = 0;
+    float* dScratchFiner = nullptr;
     std::uint32_t* dShell = nullptr;
     int shellCount = 0;
     std::uint32_t* dSeed = nullptr;
@@ -391,6 +399,37 @@ struct fcfd_solver {
         return g;
     }
 
+    RefineGeom geomFiner() const {
+        RefineGeom g;
+        g.coarse = fine.d; g.fine = finer.d;
+        g.boxX0 = finerBox.x0; g.boxY0 = finerBox.y0; g.boxX1 = finerBox.x1; g.boxY1 = finerBox.y1;
+        g.factor = finerFactor;
+        return g;
+    }
+
+    /// Both finer buffers from the fine level's current state (full-volume
+    /// fill, lbm_solver.cpp:523-545).
+    cudaError_t seedFiner() {
+        if (!finerActive) return cudaSuccess;
+        const float tf = fineTau(effTau(), factor), tr = fineTau(tf, finerFactor);
+        for (int i = 0; i < 2; ++i) {
+            ++launches;
+            if (auto e = launch_fill_c2f(storage, fine.f[fine.src], fine.f[fine.src], fine.kind, finer.f[i],
+                                         dSeedFiner, seedCountFiner, geomFiner(), 0.0f,
+                                         tr / (static_cast<float>(finerFactor) * tf), stream);
+                e != cudaSuccess)
+                return e;
+        }
+        return cudaSuccess;
+    }
+
+    void freeFiner() {
+        finer.free_all();
+        dfree(dShellFiner); dfree(dSeedFiner); dfree(dScratchFiner);
+        shellCountFiner = seedCountFiner = 0;
+        finerActive = false;
+    }
+
     cudaError_t seedFine() {
         if (!fineActive) return cudaSuccess;
         const float tc = effTau(), tf = fineTau(tc, factor);
@@ -422,6 +461,7 @@ struct fcfd_solver {
     }
 
     void freeFine() {
+        freeFiner();  // the finer level nests in the fine one
         fine.free_all();
         dfree(dShell); dfree(dSeed); dfree(dScratch);
         shellCount = seedCount = 0;
@@ -467,15 +507,15 @@ struct fcfd_solver {
     /// Fine collide of the last sub-step with the restriction's child
     /// averages fused in (factor 2); timed with the collide launches, its
     /// algorithmic bytes include the scratch records it writes.
-    cudaError_t collideChild(Level& L, const CollideParams& p) {
+    cudaError_t collideChild(Level& L, const CollideParams& p, const RefineGeom& g, float* scratch) {
         ChildFuse cf;
-        cf.scratch = dScratch;
-        cf.boxX0 = box.x0;
-        cf.boxY0 = box.y0;
-        restrict_sub_box(geom(), cf.rx0, cf.ry0, cf.rw, cf.rh);
+        cf.scratch = scratch;
+        cf.boxX0 = g.boxX0;
+        cf.boxY0 = g.boxY0;
+        restrict_sub_box(g, cf.rx0, cf.ry0, cf.rw, cf.rh);
         cudaEvent_t e2 = collideTiming
                              ? fuseT.begin(static_cast<double>(L.n),
-                                           L.collideBytes(storage) + 96.0 * static_cast<double>(cf.rw) * cf.rh * coarse.d.nz,
+                                           L.collideBytes(storage) + 96.0 * static_cast<double>(cf.rw) * cf.rh * g.coarse.nz,
                                            stream)
                              : nullptr;
         ++launches;
@@ -526,8 +566,9 @@ struct fcfd_solver {
                 fp.tau = tf;
                 fp.writeMacro = 0;
                 // Factor 2: the last sub-step's collide also forms the
-                // restriction's child averages (no re-read of the fine level).
-                const bool fuse = fuseChild && m == 2;
+                // restriction's child averages (no re-read of the fine level)
+                // -- unless a finer level rewrites the fine state after it.
+                const bool fuse = fuseChild && m == 2 && !finerActive;
                 for (int k = 0; k < m; ++k) {
                     ++launches;
                     if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src],
@@ -536,9 +577,40 @@ struct fcfd_solver {
                                                  tf / (static_cast<float>(m) * tc), stream);
                         e != cudaSuccess)
                         return e;
-                    const cudaError_t ce = (fuse && k == m - 1) ? collideChild(fine, fp)
+                    const cudaError_t ce = (fuse && k == m - 1) ? collideChild(fine, fp, geom(), dScratch)
                                                                 : collide(fine, fp, nullptr, nullptr, nullptr, nullptr);
                     if (ce != cudaSuccess) return ce;
+                    // Nested finer level (lbm_solver.cpp:1209-1270): m2
+                    // sub-steps between the fine pair's two time levels, then
+                    // restriction into the fine t+1 buffer, before the swap.
+                    if (finerActive) {
+                        const int m2 = finerFactor;
+                        const float tr = fineTau(tf, m2);
+                        CollideParams rp = fp;
+                        rp.tau = tr;
+                        const bool fuseR = fuseChild && m2 == 2;
+                        for (int q = 0; q < m2; ++q) {
+                            ++launches;
+                            if (auto e = launch_fill_c2f(storage, fine.f[fine.src], fine.f[1 - fine.src], fine.kind,
+                                                         finer.f[finer.src], dShellFiner, shellCountFiner,
+                                                         geomFiner(), static_cast<float>(q) / static_cast<float>(m2),
+                                                         tr / (static_cast<float>(m2) * tf), stream);
+                                e != cudaSuccess)
+                                return e;
+                            const cudaError_t cr = (fuseR && q == m2 - 1)
+                                                       ? collideChild(finer, rp, geomFiner(), dScratchFiner)
+                                                       : collide(finer, rp, nullptr, nullptr, nullptr, nullptr);
+                            if (cr != cudaSuccess) return cr;
+                            finer.src = 1 - finer.src;
+                        }
+                        launches += fuseR ? 1 : 2;
+                        if (auto e = launch_restrict_f2c(storage, finer.f[finer.src], finer.kind, fine.f[1 - fine.src],
+                                                         fine.kind, geomFiner(), (static_cast<float>(m2) * tf) / tr,
+                                                         dScratchFiner, nullptr, nullptr, nullptr, nullptr, stream,
+                                                         fuseR);
+                            e != cudaSuccess)
+                            return e;
+                    }
                     fine.src = 1 - fine.src;
                 }
                 launches += fuse ? 1 : 2;
@@ -560,6 +632,10 @@ struct fcfd_solver {
                 if (fineActive) {
                     ++launches;
                     launch_watchdog(storage, fine.f[fine.src], fine.d, dNan, steps * 977, 2, stream);
+                }
+                if (finerActive) {  // verdicts 5/6 name the finer level
+                    ++launches;
+                    launch_watchdog(storage, finer.f[finer.src], finer.d, dNan, steps * 977, 4, stream);
                 }
                 cudaMemcpyAsync(hNan, dNan, sizeof(int), cudaMemcpyDeviceToHost, stream);
                 cudaMemcpyAsync(hNan + 1, dStatus, sizeof(int), cudaMemcpyDeviceToHost, stream);
@@ -584,6 +660,8 @@ struct fcfd_solver {
         const float tauNow = effTau();
         if (coarse.wm.active) wallUpdate(coarse, (tauNow - 0.5f) / 3.0f);
         if (fineActive && fine.wm.active) wallUpdate(fine, (fineTau(tauNow, factor) - 0.5f) / 3.0f);
+        if (finerActive && finer.wm.active)
+            wallUpdate(finer, (fineTau(fineTau(tauNow, factor), finerFactor) - 0.5f) / 3.0f);
         return static_cast<int>(cudaGetLastError());
     }
 
@@ -613,6 +691,7 @@ struct fcfd_solver {
                          kSpeckSeed, stream);
         }
         seedFine();
+        seedFiner();
         resetWMState();
     }
 
@@ -965,6 +1044,7 @@ int fcfd_restore_from_macro(fcfd_solver* s, const float* r, const float* u, cons
     }
     s->notifyRestored(false);
     if (auto e = s->seedFine(); e != cudaSuccess) return e;
+    if (auto e = s->seedFiner(); e != cudaSuccess) return e;
     return cudaStreamSynchronize(s->stream);
 }
 
@@ -973,6 +1053,8 @@ int fcfd_perf_stats(const fcfd_solver* s, fcfd_perf* p) {
     *p = fcfd_perf{};
     double upd = static_cast<double>(s->coarse.n);
     if (s->fineActive) upd += static_cast<double>(s->factor) * static_cast<double>(s->fine.n);
+    if (s->finerActive)  // every finer cell m * m2 times per coarse step (lbm_solver.cpp:1703-1712)
+        upd += static_cast<double>(s->factor) * s->finerFactor * static_cast<double>(s->finer.n);
     p->updates_per_step = upd;
     p->last_step_ms = s->lastStepMs;
     if (s->lastStepMs > 0.0) p->mlups = upd / (s->lastStepMs * 1000.0);
@@ -1001,6 +1083,8 @@ int fcfd_set_wall_model(fcfd_solver* s, int enabled) {
     if (auto e = s->buildWM(s->coarse, kWallSampleCoarse); e != cudaSuccess) return e;
     if (s->fineActive)
         if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return e;
+    if (s->finerActive)
+        if (auto e = s->buildWM(s->finer, kWallSampleFine); e != cudaSuccess) return e;
     return 0;
 }
 
@@ -1048,6 +1132,7 @@ static Level* level_of(fcfd_solver* s, int level) {
     if (!s || !s->initialized) return nullptr;
     if (level == 0) return &s->coarse;
     if (level == 1 && s->fineActive) return &s->fine;
+    if (level == 2 && s->finerActive) return &s->finer;
     return nullptr;
 }
 
@@ -1194,7 +1279,8 @@ int fcfd_set_refined_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {
     if (!seed.empty()) cudaMemcpy(s->dSeed, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
     s->updateForcesFromFine();
     if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return e;
-    return s->seedFine();
+    if (auto e = s->seedFine(); e != cudaSuccess) return e;
+    return s->seedFiner();  // the finer level restarts from the re-seeded fine field
 }
 
 int fcfd_refinement_info(const fcfd_solver* s, fcfd_refine_info* r) {
@@ -1458,4 +1544,128 @@ int fcfd_q_link_info(fcfd_solver* s, int level, int* active, int* links, int* fa
     if (links) *links = L->qLinks;
     if (fallback) *fallback = L->qFallback;
     return 0;
+}
+
+// ---- nested finer level (initFinerRefinement & co, lbm_solver.cpp:1916-2010)
+
+static int finer_lists(fcfd_solver* s, const uint8_t* ff, size_t n) {
+    std::vector<std::uint32_t> shell, seed;
+    for (size_t i = 0; i < n; ++i) {
+        if (ff[i] == FCFD_FLAG_INTERFACE) shell.push_back(static_cast<std::uint32_t>(i));
+        if (ff[i] != FCFD_FLAG_SOLID) seed.push_back(static_cast<std::uint32_t>(i));
+    }
+    dfree(s->dShellFiner);
+    dfree(s->dSeedFiner);
+    s->shellCountFiner = static_cast<int>(shell.size());
+    s->seedCountFiner = static_cast<int>(seed.size());
+    if (auto e = dalloc(&s->dShellFiner, shell.size() * 4); e != cudaSuccess) return e;
+    if (auto e = dalloc(&s->dSeedFiner, seed.size() * 4); e != cudaSuccess) return e;
+    if (!shell.empty()) cudaMemcpy(s->dShellFiner, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice);
+    if (!seed.empty()) cudaMemcpy(s->dSeedFiner, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
+    return 0;
+}
+
+int fcfd_init_finer_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor, const uint8_t* ff,
+                               size_t n, char* err, size_t errlen) {
+    if (!s || !s->initialized) {
+        set_err(err, errlen, "solver not initialized");
+        return cudaErrorNotReady;
+    }
+    if (!s->fineActive) {
+        set_err(err, errlen, "fine level not active (finer level nests in it)");
+        return cudaErrorInvalidValue;
+    }
+    fcfd_shutdown_finer_refinement(s);
+    if (!box || !ff) {
+        set_err(err, errlen, "null argument");
+        return cudaErrorInvalidValue;
+    }
+    if (factor < 2 || factor > 4) {
+        set_err(err, errlen, "finer factor out of range (2..4)");
+        return cudaErrorInvalidValue;
+    }
+    const LevelDims& pd = s->fine.d;
+    if (box->x1 - box->x0 <= 8 || box->y1 - box->y0 <= 8 || box->x0 < 1 || box->y0 < 1 || box->x1 > pd.nx - 1
+        || box->y1 > pd.ny - 1) {
+        set_err(err, errlen, "finer patch box out of range");
+        return cudaErrorInvalidValue;
+    }
+    LevelDims fd{factor * (box->x1 - box->x0), factor * (box->y1 - box->y0), factor * pd.nz};
+    if (n != static_cast<size_t>(fd.cells())) {
+        set_err(err, errlen, "finer flag field size does not match the patch");
+        return cudaErrorInvalidValue;
+    }
+    if (fd.cells() >= (1LL << 31)) {
+        set_err(err, errlen, "finer grid too large for 32-bit cell indices");
+        return cudaErrorInvalidValue;
+    }
+    cudaStreamSynchronize(s->stream);
+    s->finerFactor = factor;
+    s->finerBox = *box;
+    auto fail = [&](const char* what, cudaError_t e) {
+        set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));
+        s->freeFiner();
+        (void)cudaGetLastError();
+        return static_cast<int>(e);
+    };
+    if (auto e = s->allocLevel(s->finer, fd); e != cudaSuccess) return fail("finer buffer allocation failed", e);
+    if (auto e = s->uploadLevelFlags(s->finer, ff); e != cudaSuccess) return fail("finer flag upload failed", e);
+    if (auto e = static_cast<cudaError_t>(finer_lists(s, ff, n)); e != cudaSuccess)
+        return fail("finer target lists failed", e);
+    s->finerActive = true;
+    const long long sf = restrict_scratch_floats(s->geomFiner());
+    if (sf <= 0) return fail("finer restriction sub-box is empty", cudaErrorInvalidValue);
+    if (auto e = dalloc(&s->dScratchFiner, static_cast<size_t>(sf) * 4); e != cudaSuccess)
+        return fail("finer restriction scratch allocation failed", e);
+    if (auto e = s->buildWM(s->finer, kWallSampleFine); e != cudaSuccess) return fail("finer wall list failed", e);
+    if (auto e = s->seedFiner(); e != cudaSuccess) return fail("finer level seeding failed", e);
+    if (auto e = cudaStreamSynchronize(s->stream); e != cudaSuccess) return fail("finer level seeding failed", e);
+    set_err(err, errlen, "");
+    return 0;
+}
+
+void fcfd_shutdown_finer_refinement(fcfd_solver* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->freeFiner();
+}
+
+int fcfd_set_refined_finer_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {
+    if (!s || !s->initialized || !s->finerActive || !ff || n != static_cast<size_t>(s->finer.n))
+        return cudaErrorInvalidValue;
+    if (auto e = s->uploadLevelFlags(s->finer, ff); e != cudaSuccess) return e;
+    if (auto e = finer_lists(s, ff, n); e != 0) return e;
+    if (auto e = s->buildWM(s->finer, kWallSampleFine); e != cudaSuccess) return e;
+    return s->seedFiner();
+}
+
+int fcfd_set_refined_finer_surface_reference(fcfd_solver* s, const uint8_t* clean, size_t n) {
+    if (!s || !s->initialized || !s->finerActive || !clean || n != static_cast<size_t>(s->finer.n))
+        return cudaErrorInvalidValue;
+    cudaStreamSynchronize(s->stream);
+    s->finer.surfaceRef.assign(clean, clean + n);
+    return s->buildWM(s->finer, kWallSampleFine);
+}
+
+int fcfd_finer_refinement_info(const fcfd_solver* s, fcfd_finer_info* r) {
+    if (!s || !r) return cudaErrorInvalidValue;
+    *r = fcfd_finer_info{};
+    if (!s->finerActive) return 0;
+    r->active = 1;
+    r->factor = s->finerFactor;
+    r->box = s->finerBox;
+    r->dims = fcfd_dims{s->finer.d.nx, s->finer.d.ny, s->finer.d.nz};
+    r->vram_bytes = 2.0 * 19.0 * static_cast<double>(s->finer.n) * (s->storage == Storage::F32 ? 4 : 2)
+                  + 2.0 * static_cast<double>(s->finer.n);
+    return 0;
+}
+
+int fcfd_import_finer_f32(fcfd_solver* s, const float* f, size_t count) {
+    if (!s || !s->initialized || !s->finerActive || !f) return cudaErrorInvalidValue;
+    return s->importF32(s->finer, f, count);
+}
+
+int fcfd_export_finer_f32(fcfd_solver* s, float* f, size_t count) {
+    if (!s || !s->initialized || !s->finerActive || !f) return cudaErrorInvalidValue;
+    return s->exportF32(s->finer, f, count);
 }

@@ -306,6 +306,42 @@ class LBMSolver:
         self._lib.fcfd_q_link_info(self._h, level, C.byref(a), C.byref(l), C.byref(f))
         return bool(a.value), l.value, f.value
 
+    # ---- nested finer level ----------------------------------------------
+    def init_finer_refinement(self, box: Box, factor: int, finer_flags) -> None:
+        """A patch inside the fine level (box in fine cells)."""
+        ff = np.ascontiguousarray(finer_flags, np.uint8)
+        err = C.create_string_buffer(512)
+        b = box.as_c()
+        rc = self._lib.fcfd_init_finer_refinement(self._h, C.byref(b), factor, ptr(ff), ff.size, err, 512)
+        if rc != 0:
+            raise SolverError(err.value.decode() or f"initFinerRefinement failed ({rc})")
+
+    def shutdown_finer_refinement(self):
+        self._lib.fcfd_shutdown_finer_refinement(self._h)
+
+    def set_refined_finer_flags(self, finer_flags):
+        ff = np.ascontiguousarray(finer_flags, np.uint8)
+        return self._lib.fcfd_set_refined_finer_flags(self._h, ptr(ff), ff.size)
+
+    def finer_refinement_info(self) -> capi.FinerInfo:
+        r = capi.FinerInfo()
+        self._lib.fcfd_finer_refinement_info(self._h, C.byref(r))
+        return r
+
+    def export_finer_f32(self) -> np.ndarray:
+        r = self.finer_refinement_info()
+        f = np.empty(Q * r.dims.nx * r.dims.ny * r.dims.nz, np.float32)
+        rc = self._lib.fcfd_export_finer_f32(self._h, ptr(f), f.size)
+        if rc:
+            raise SolverError(f"finer export failed ({rc})")
+        return f
+
+    def import_finer_f32(self, f):
+        f = np.ascontiguousarray(f, np.float32)
+        rc = self._lib.fcfd_import_finer_f32(self._h, ptr(f), f.size)
+        if rc:
+            raise SolverError(f"finer import failed ({rc})")
+
     def set_fused_restriction(self, enabled: bool):
         self._lib.fcfd_set_fused_restriction(self._h, int(enabled))
 

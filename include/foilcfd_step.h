@@ -273,7 +273,7 @@ int fcfd_wall_update_now(fcfd_solver* s, int level, float nu_lat,
  * q_frac[cell * 19 + q] (count = 19 * cells), and per cell the bits of the
  * links whose second fluid node x + c_q exists, ff_mask[cell]. The collide
  * then applies Bouzidi's linear interpolation on those links
- * (lbm_core.cu:332-364). level 0 coarse, 1 fine; nq == 0 clears the field.
+ * (lbm_core.cu:332-364). level 0 coarse, 1 fine, 2 finer; nq == 0 clears.
  * links / fallback are the caller's counts, kept for fcfd_q_link_info. */
 int fcfd_set_q_links(fcfd_solver* s, int level, const uint8_t* q_frac, size_t nq,
                      const uint32_t* ff_mask, size_t nm, int links, int fallback);
@@ -298,6 +298,33 @@ int fcfd_export_fine_f32(fcfd_solver* s, float* host_f, size_t count);
  * (lbm_refine.cu:274-429 reads it in the restriction). Both settings give
  * the same populations bit for bit; 0 is kept for that comparison. */
 int fcfd_set_fused_restriction(fcfd_solver* s, int enabled);
+
+/* ---- nested finer level (lbm_solver.h:118-124, 207-243) ----------------- */
+
+/* Finer level state (the RefinementInfo finer* fields). */
+typedef struct fcfd_finer_info {
+    int active;
+    int factor;
+    fcfd_patch_box box;   /* in FINE cells */
+    fcfd_dims dims;       /* factor * box extent, factor * fine nz */
+    double vram_bytes;
+} fcfd_finer_info;
+
+/* initFinerRefinement (lbm_solver.cpp:1916-2000): a nested patch inside the
+ * fine level, box in FINE cells, factor 2..4, finer flags with their
+ * INTERFACE shell; the finer level is seeded from the fine field. Each fine
+ * sub-step then runs `factor` finer sub-steps and a finer -> fine
+ * restriction (lbm_solver.cpp:1209-1270). Forces stay on the fine level. */
+int fcfd_init_finer_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor,
+                               const uint8_t* finer_flags, size_t n, char* err, size_t errlen);
+void fcfd_shutdown_finer_refinement(fcfd_solver* s);
+/* setRefinedFinerFlags / setRefinedFinerSurfaceReference. */
+int fcfd_set_refined_finer_flags(fcfd_solver* s, const uint8_t* finer_flags, size_t n);
+int fcfd_set_refined_finer_surface_reference(fcfd_solver* s, const uint8_t* clean, size_t n);
+int fcfd_finer_refinement_info(const fcfd_solver* s, fcfd_finer_info* out);
+/* FP32 SoA import/export of the finer level's current buffer. */
+int fcfd_import_finer_f32(fcfd_solver* s, const float* host_f, size_t count);
+int fcfd_export_finer_f32(fcfd_solver* s, float* host_f, size_t count);
 
 /* ---- host fixture builders (src/sim/wall_model.h, src/geom/) ------------- */
 

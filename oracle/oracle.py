@@ -236,6 +236,7 @@ class OracleSolver:
         self.g = self.f.copy()
         self.macro = None
         self.fine = None
+        self.finer = None
         self.wall = None
         self.slip = None
         self.last_force = np.zeros(3)
@@ -260,6 +261,34 @@ class OracleSolver:
                  np.float32(tf) / (np.float32(factor) * np.float32(tc)), True)
         fine["g"] = fine["f"].copy()
 
+    def enable_finer_refinement(self, box, factor, finer_flags):
+        """Nested patch inside the fine level (box in fine cells), seeded from
+        the fine field (lbm_solver.cpp:1916-2000, 523-545)."""
+        fine = self.fine
+        fd0 = fine["dims"]
+        rd = (factor * (box[2] - box[0]), factor * (box[3] - box[1]), factor * fd0[2])
+        self.finer = dict(dims=rd, box=tuple(box), m=factor, flags=np.ascontiguousarray(finer_flags, np.uint8),
+                          f=np.zeros(Q * int(np.prod(rd)), np.float32))
+        tf = np.float32(fine["m"]) * (np.float32(self.tau) - np.float32(0.5)) + np.float32(0.5)
+        tr = np.float32(factor) * (tf - np.float32(0.5)) + np.float32(0.5)
+        fill_c2f(fd0, fine["f"], fine["f"], fine["flags"], rd, self.finer["f"], self.finer["flags"], box, factor,
+                 0.0, tr / (np.float32(factor) * tf), True)
+        self.finer["g"] = self.finer["f"].copy()
+
+    def _finer_substeps(self, tf, fine_t1):
+        """m2 finer sub-steps between the fine pair's time levels, then the
+        finer -> fine restriction into fine_t1 (lbm_solver.cpp:1209-1270)."""
+        fr, fine = self.finer, self.fine
+        rd, m2, box = fr["dims"], fr["m"], fr["box"]
+        tr = np.float32(m2) * (tf - np.float32(0.5)) + np.float32(0.5)
+        for q in range(m2):
+            fill_c2f(fine["dims"], fine["f"], fine_t1, fine["flags"], rd, fr["f"], fr["flags"], box, m2,
+                     np.float32(q) / np.float32(m2), tr / (np.float32(m2) * tf), False)
+            nr, _ = collide(rd, fr["f"], fr["flags"], tr, self.lam, self.smag, self.u_lat, False, None, dst=fr["g"])
+            fr["g"], fr["f"] = fr["f"], nr
+        restrict_f2c(rd, fr["f"], fr["flags"], fine["dims"], fine_t1, fine["flags"], box, m2,
+                     (np.float32(m2) * tf) / tr, None)
+
     def step_n(self, n):
         tau = np.float32(self.tau)
         for i in range(n):
@@ -274,6 +303,8 @@ class OracleSolver:
                              np.float32(k) / np.float32(m), tf / (np.float32(m) * tau), False)
                     nf, _ = collide(fd, self.fine["f"], self.fine["flags"], tf, self.lam, self.smag,
                                     self.u_lat, False, None, dst=self.fine["g"])
+                    if self.finer is not None:
+                        self._finer_substeps(tf, nf)
                     self.fine["g"], self.fine["f"] = self.fine["f"], nf
                 restrict_f2c(fd, self.fine["f"], self.fine["flags"], self.dims, dst, self.flags, box, m,
                              (np.float32(m) * tau) / tf, macro)

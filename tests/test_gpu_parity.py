@@ -424,3 +424,81 @@ def test_qlibb_collide_vs_reference_golden(fc, golden, case, steps, slip, kernel
     # Clearing the field returns to plain half-way bounce-back.
     s.set_q_links(0, None)
     assert s.q_link_info(0)[0] is False
+
+
+def _three_level_case(fc, oracle_mod):
+    """Coarse 48x32x4 open channel, a 2:1 patch, and a 2:1 finer patch nested
+    in it, around a block voxelised at every level."""
+    cd = (48, 32, 4)
+    cf = np.zeros((cd[2], cd[1], cd[0]), np.uint8)
+    cf[:, 0, :] = 5
+    cf[:, -1, :] = 4
+    cf[:, :, 0] = 2
+    cf[:, 1:-1, -1] = 3
+    cf[:, 14:18, 22:26] = 1
+    box = (8, 6, 40, 26)
+    fd = (2 * (box[2] - box[0]), 2 * (box[3] - box[1]), 2 * cd[2])
+    ff = np.zeros((fd[2], fd[1], fd[0]), np.uint8)
+    ff[:, 16:24, 28:36] = 1
+    ff = ff.ravel()
+    fc.stamp_interface_shell(fd, ff)
+    rbox = (20, 10, 44, 30)
+    rd = (2 * (rbox[2] - rbox[0]), 2 * (rbox[3] - rbox[1]), 2 * fd[2])
+    rf = np.zeros((rd[2], rd[1], rd[0]), np.uint8)
+    rf[:, 12:28, 16:32] = 1
+    rf = rf.ravel()
+    fc.stamp_interface_shell(rd, rf)
+    rng = np.random.default_rng(7)
+    n = int(np.prod(cd))
+    f0 = oracle_mod.equilibrium(1 + 0.01 * rng.standard_normal(n), 0.05 + 0.01 * rng.standard_normal(n),
+                                0.01 * rng.standard_normal(n), 0.01 * rng.standard_normal(n))
+    return cd, cf.ravel(), box, ff, rbox, rf, f0
+
+
+def test_three_level_step_vs_oracle(fc, oracle_mod):
+    """Nested finer level (initFinerRefinement, lbm_solver.cpp:1209-1270):
+    each fine sub-step runs two finer sub-steps and a finer -> fine
+    restriction; 20 coarse steps against the oracle's replay, bit for bit on
+    all three levels."""
+    cd, cflags, box, ff, rbox, rf, f0 = _three_level_case(fc, oracle_mod)
+    tauC = 0.55
+    s = make(fc, cd, cflags, tauC, 0.05)
+    s.import_f32(f0)
+    s.init_refinement(fc.Box(*box), 2, ff)
+    s.init_finer_refinement(fc.Box(*rbox), 2, rf)
+    info = s.finer_refinement_info()
+    assert info.active == 1 and (info.dims.nx, info.dims.ny, info.dims.nz) == (48, 40, 16)
+    assert s.perf_stats().updates_per_step == np.prod(cd) + 2 * ff.size + 4 * rf.size
+    o = oracle_mod.OracleSolver(cd, cflags, np.float32(tauC), np.float32(0.05))
+    o.set_state(f0)
+    o.enable_refinement(box, 2, ff)
+    o.enable_finer_refinement(rbox, 2, rf)
+    keep = rf != 1
+    assert np.array_equal(s.export_finer_f32().reshape(19, -1)[:, keep], o.finer["f"].reshape(19, -1)[:, keep])
+    for _ in range(4):
+        assert s.step_n(5) == 0
+        o.step_n(5)
+    assert not s.nan_detected()
+    m = written_mask(cflags)
+    assert np.array_equal(s.export_f32().reshape(19, -1)[:, m], o.f.reshape(19, -1)[:, m])
+    fm = ff == 0
+    assert np.array_equal(s.export_fine_f32().reshape(19, -1)[:, fm], o.fine["f"].reshape(19, -1)[:, fm])
+    rm = rf == 0
+    assert np.array_equal(s.export_finer_f32().reshape(19, -1)[:, rm], o.finer["f"].reshape(19, -1)[:, rm])
+    # Shutting the finer level down leaves a working two-level solver.
+    s.shutdown_finer_refinement()
+    assert s.finer_refinement_info().active == 0 and s.step_n(5) == 0
+
+
+def test_finer_refinement_errors(fc, oracle_mod):
+    cd, cflags, box, ff, rbox, rf, f0 = _three_level_case(fc, oracle_mod)
+    s = make(fc, cd, cflags, 0.55, 0.05)
+    with pytest.raises(Exception):
+        s.init_finer_refinement(fc.Box(*rbox), 2, rf)  # no fine level yet
+    s.init_refinement(fc.Box(*box), 2, ff)
+    with pytest.raises(Exception):
+        s.init_finer_refinement(fc.Box(0, 10, 44, 30), 2, rf)  # touches the fine face
+    with pytest.raises(Exception):
+        s.init_finer_refinement(fc.Box(*rbox), 5, rf)
+    with pytest.raises(Exception):
+        s.init_finer_refinement(fc.Box(*rbox), 2, rf[:-1])
