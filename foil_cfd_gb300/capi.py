@@ -96,6 +96,7 @@ _SIGS = {
                             C.c_char_p, C.c_size_t]),
     "fcfd_reset": (None, [P]),
     "fcfd_set_flags": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_apply_edited_flags": (C.c_int, [P, P, C.c_size_t, P]),
     "fcfd_set_startup_ramp": (None, [P, C.c_int]),
     "fcfd_set_force_ema_window": (None, [P, C.c_float]),
     "fcfd_step_n": (C.c_int, [P, C.c_int]),

@@ -350,6 +350,77 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
     collide_one<S, WM, EXACT, QL>(src, dst, kind, a, x, blockIdx.y, blockIdx.z);
 }
 
+// ---- warm-restart flag edits (applyFlagEditsKernel, lbm_core.cu:644-717) -----
+// mask 1: newly solid -> every population of both buffers zeroed; mask 2:
+// newly fluid -> equilibrium of the mean rho, u of the neighbours (x + c_q,
+// no wrap in x/y, periodic z) that are fluid and unedited, read from fA
+// (rest state when there are none), written to both buffers. Edited cells
+// never read each other, so the kernel has no races.
+template <class S>
+__global__ void apply_flag_edits_kernel(typename S::T* __restrict__ fA, typename S::T* __restrict__ fB,
+                                        const std::uint8_t* __restrict__ flags,
+                                        const std::uint8_t* __restrict__ mask, int nx, int ny, int nz) {
+    const long long n = static_cast<long long>(nx) * ny * nz;
+    const long long cell = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (cell >= n) return;
+    const std::uint8_t edit = mask[cell];
+    if (edit == 0) return;
+    if (edit == 1) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            S::st(fA + q * n, cell, 0.0f, wgt(q));
+            S::st(fB + q * n, cell, 0.0f, wgt(q));
+        }
+        return;
+    }
+    const long long nxny = static_cast<long long>(nx) * ny;
+    const int z = static_cast<int>(cell / nxny);
+    const long long rem = cell - static_cast<long long>(z) * nxny;
+    const int y = static_cast<int>(rem / nx), x = static_cast<int>(rem - static_cast<long long>(y) * nx);
+    float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    int found = 0;
+    for (int q = 1; q < kQ; ++q) {
+        const int xn = x + cx(q), yn = y + cy(q), zn = z + cz(q);
+        if (xn < 0 || xn >= nx || yn < 0 || yn >= ny) continue;
+        const int znw = zn < 0 ? nz - 1 : (zn >= nz ? 0 : zn);
+        const long long nc = xn + static_cast<long long>(nx) * yn + nxny * znw;
+        if (flags[nc] != kFluid || mask[nc] != 0) continue;
+        float r = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+#pragma unroll
+        for (int p = 0; p < kQ; ++p) {
+            const float fq = S::ld(fA + p * n, nc, wgt(p));
+            r += fq;
+            jx += cx(p) * fq; jy += cy(p) * fq; jz += cz(p) * fq;
+        }
+        rho += r;
+        ux += jx / r; uy += jy / r; uz += jz / r;
+        ++found;
+    }
+    if (found > 0) {
+        const float inv = 1.0f / static_cast<float>(found);
+        rho *= inv; ux *= inv; uy *= inv; uz *= inv;
+    } else {
+        rho = 1.0f; ux = uy = uz = 0.0f;
+    }
+    float feq[kQ];
+    eq19(rho, ux, uy, uz, feq);
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+        S::st(fA + q * n, cell, feq[q], wgt(q));
+        S::st(fB + q * n, cell, feq[q], wgt(q));
+    }
+}
+
+template <class S>
+cudaError_t launch_apply_flag_edits_impl(void* fA, void* fB, const std::uint8_t* flags, const std::uint8_t* mask,
+                                         LevelDims d, cudaStream_t st) {
+    using T = typename S::T;
+    const long long n = d.cells();
+    apply_flag_edits_kernel<S><<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(
+        static_cast<T*>(fA), static_cast<T*>(fB), flags, mask, d.nx, d.ny, d.nz);
+    return cudaGetLastError();
+}
+
 // ---- last fine sub-step with the restriction's child averages fused in --------
 // Factor-2 patches only. A thread owns one fine x column of a 2 x 2 (y, z)
 // cell group and updates its four cells in the children's summation order

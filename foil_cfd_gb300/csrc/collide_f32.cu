@@ -58,6 +58,11 @@ cudaError_t launch_collide_child_f32(const float* src, float* dst, const std::ui
     return launch_collide_child_impl<StoreF32, true>(src, dst, kind, d, p, slip, cf, st);
 }
 
+cudaError_t launch_apply_flag_edits_f32(float* fA, float* fB, const std::uint8_t* flags, const std::uint8_t* mask,
+                                        LevelDims d, cudaStream_t st) {
+    return launch_apply_flag_edits_impl<StoreF32>(fA, fB, flags, mask, d, st);
+}
+
 cudaError_t launch_init_eq_f32(float* f, const std::uint8_t* kind, long long n, float uIn, cudaStream_t st) {
     init_eq_f32_kernel<<<static_cast<unsigned>((n + kBlock1D - 1) / kBlock1D), kBlock1D, 0, st>>>(f, kind, n, uIn);
     return cudaGetLastError();

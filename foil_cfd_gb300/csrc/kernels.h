@@ -82,6 +82,12 @@ struct ChildFuse {
 };
 cudaError_t launch_collide_child(Storage s, const void* src, void* dst, const std::uint8_t* kind, LevelDims d,
                                  const CollideParams& p, SlipField slip, const ChildFuse& cf, cudaStream_t st);
+/// Warm-restart flag-edit fixup of both buffers (mask 1 newly solid, 2 newly
+/// fluid; flags = the new CellFlag bytes).
+cudaError_t launch_apply_flag_edits(Storage s, void* fA, void* fB, const std::uint8_t* flags,
+                                    const std::uint8_t* mask, LevelDims d, cudaStream_t st);
+cudaError_t launch_apply_flag_edits_f32(float* fA, float* fB, const std::uint8_t* flags, const std::uint8_t* mask,
+                                        LevelDims d, cudaStream_t st);
 
 // ---- FP32 reference-order kernels (collide_f32.cu, built with --fmad=false)
 cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint8_t* kind,

@@ -894,6 +894,45 @@ int fcfd_set_flags(fcfd_solver* s, const uint8_t* flags, size_t n) {
     return 0;
 }
 
+int fcfd_apply_edited_flags(fcfd_solver* s, const uint8_t* flags, size_t n, long long* edited) {
+    if (edited) *edited = 0;
+    if (!s || !s->initialized || !flags || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
+    Level& L = s->coarse;
+    // Diff before the host copy is replaced: 1 newly solid, 2 newly fluid.
+    std::vector<std::uint8_t> mask(static_cast<size_t>(L.n), 0);
+    long long count = 0;
+    for (long long i = 0; i < L.n; ++i) {
+        const bool was = L.hostFlags[static_cast<size_t>(i)] == FCFD_FLAG_SOLID;
+        const bool now = flags[i] == FCFD_FLAG_SOLID;
+        if (was == now) continue;
+        mask[static_cast<size_t>(i)] = now ? 1 : 2;
+        ++count;
+    }
+    if (auto e = s->uploadLevelFlags(L, flags); e != cudaSuccess) return e;
+    if (count > 0) {
+        std::uint8_t* dMaskBuf = nullptr;
+        if (auto e = cudaMalloc(&dMaskBuf, static_cast<size_t>(L.n)); e != cudaSuccess) return e;
+        cudaError_t e = cudaMemcpyAsync(dMaskBuf, mask.data(), static_cast<size_t>(L.n), cudaMemcpyHostToDevice,
+                                        s->stream);
+        if (e == cudaSuccess) {
+            ++s->launches;
+            e = launch_apply_flag_edits(s->storage, L.f[L.src], L.f[1 - L.src], L.flags, dMaskBuf, L.d, s->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        cudaFree(dMaskBuf);
+        if (e != cudaSuccess) return e;
+    }
+    s->updateForcesFromFine();
+    if (auto e = s->buildWM(L, kWallSampleCoarse); e != cudaSuccess) return e;
+    s->rampActive = false;
+    s->emaSeeded = false;
+    if (s->forcePending) { cudaStreamSynchronize(s->stream); s->forcePending = false; }
+    s->stepsAtLastFold = s->steps;
+    s->gateOpenAt = s->steps + static_cast<long long>(kWarmGateFT * s->flowThroughSteps());
+    if (edited) *edited = count;
+    return 0;
+}
+
 void fcfd_set_startup_ramp(fcfd_solver* s, int enabled) {
     if (s) s->rampEnabled = enabled != 0;
 }

@@ -176,6 +176,14 @@ cudaError_t launch_collide_child(Storage s, const void* src, void* dst, const st
     return launch_collide_child_impl<StoreF16, false>(src, dst, kind, d, p, slip, cf, st);
 }
 
+cudaError_t launch_apply_flag_edits(Storage s, void* fA, void* fB, const std::uint8_t* flags,
+                                    const std::uint8_t* mask, LevelDims d, cudaStream_t st) {
+    if (!fA || !fB || !flags || !mask || d.cells() <= 0) return cudaErrorInvalidValue;
+    if (s == Storage::F32)
+        return launch_apply_flag_edits_f32(static_cast<float*>(fA), static_cast<float*>(fB), flags, mask, d, st);
+    return launch_apply_flag_edits_impl<StoreF16>(fA, fB, flags, mask, d, st);
+}
+
 cudaError_t launch_init_equilibrium(Storage s, void* f, const std::uint8_t* kind, LevelDims d,
                                     float uInlet, cudaStream_t st) {
     const long long n = d.cells();

@@ -124,6 +124,17 @@ class LBMSolver:
         flags = np.ascontiguousarray(flags, np.uint8)
         return self._lib.fcfd_set_flags(self._h, ptr(flags), flags.size)
 
+    def apply_edited_flags(self, flags) -> int:
+        """LBMSolver::applyEditedFlags (src/sim/lbm_solver.cpp:1086-1126):
+        warm restart after a geometry edit; returns the number of cells whose
+        solid state changed. Raises on a CUDA error."""
+        flags = np.ascontiguousarray(flags, np.uint8)
+        edited = C.c_longlong(0)
+        rc = self._lib.fcfd_apply_edited_flags(self._h, ptr(flags), flags.size, C.byref(edited))
+        if rc != 0:
+            raise RuntimeError(f"fcfd_apply_edited_flags failed ({rc})")
+        return int(edited.value)
+
     def set_startup_ramp_enabled(self, enabled: bool):
         self._lib.fcfd_set_startup_ramp(self._h, int(enabled))
 

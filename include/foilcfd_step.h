@@ -156,6 +156,16 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims,
 void fcfd_reset(fcfd_solver* s);
 /* LBMSolver::setFlags (lbm_solver.cpp:946-952): upload + cold restart. */
 int fcfd_set_flags(fcfd_solver* s, const uint8_t* flags, size_t n);
+/* LBMSolver::applyEditedFlags (lbm_solver.cpp:1086-1126) with the
+ * applyFlagEditsKernel fixup (lbm_core.cu:644-717): warm restart after a
+ * geometry edit of the coarse level. Cells whose SOLID state changed are
+ * fixed in both population buffers - newly solid zeroed, newly fluid set to
+ * the equilibrium of the mean density and velocity of their unedited fluid
+ * neighbours (rest state when there are none) - the new flags, force links
+ * and wall list are uploaded, and the run continues without ramp; the force
+ * average restarts and the force gate reopens half a flow-through later.
+ * *edited (nullable) <- number of cells changed. */
+int fcfd_apply_edited_flags(fcfd_solver* s, const uint8_t* flags, size_t n, long long* edited);
 /* LBMSolver::setStartupRampEnabled (lbm_solver.h:269). */
 void fcfd_set_startup_ramp(fcfd_solver* s, int enabled);
 /* LBMSolver::setForceEmaWindow (lbm_solver.h:490). */

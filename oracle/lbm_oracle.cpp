@@ -444,6 +444,55 @@ void oracle_utau_newton_f64(int n, const double* ut, const double* ys, const dou
     }
 }
 
+/// Warm-restart flag-edit fixup (lbm_core.cu:644-717): mask 1 = newly solid
+/// (both buffers zeroed), 2 = newly fluid (equilibrium of the mean rho/u of
+/// the neighbours that are fluid and unedited, read from fA; rest state if
+/// none). flags = the new flags. FP32, reference operation order.
+void oracle_apply_flag_edits(int nx, int ny, int nz, float* fA, float* fB, const uint8_t* flags,
+                             const uint8_t* mask) {
+    const Dims d{nx, ny, nz};
+    const long long N = d.n();
+    std::vector<float> a(fA, fA + Q * N);  // neighbours read the pre-edit state
+    for (long long cell = 0; cell < N; ++cell) {
+        const uint8_t edit = mask[cell];
+        if (edit == 0) continue;
+        if (edit == 1) {
+            for (int q = 0; q < Q; ++q) { fA[q * N + cell] = 0.0f; fB[q * N + cell] = 0.0f; }
+            continue;
+        }
+        const int z = (int)(cell / ((long long)nx * ny));
+        const long long rem = cell - (long long)z * nx * ny;
+        const int y = (int)(rem / nx), x = (int)(rem - (long long)y * nx);
+        float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+        int found = 0;
+        for (int q = 1; q < Q; ++q) {
+            const int xn = x + CX[q], yn = y + CY[q], zn = z + CZ[q];
+            if (xn < 0 || xn >= nx || yn < 0 || yn >= ny) continue;
+            const int znw = zn < 0 ? nz - 1 : (zn >= nz ? 0 : zn);
+            const long long nc = d.at(xn, yn, znw);
+            if (flags[nc] != FLUID || mask[nc] != 0) continue;
+            float r = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+            for (int p = 0; p < Q; ++p) {
+                const float fq = a[p * N + nc];
+                r += fq;
+                jx += (float)CX[p] * fq; jy += (float)CY[p] * fq; jz += (float)CZ[p] * fq;
+            }
+            rho += r;
+            ux += jx / r; uy += jy / r; uz += jz / r;
+            ++found;
+        }
+        if (found > 0) {
+            const float inv = 1.0f / (float)found;
+            rho *= inv; ux *= inv; uy *= inv; uz *= inv;
+        } else {
+            rho = 1.0f; ux = uy = uz = 0.0f;
+        }
+        float feq[Q];
+        equilibrium19<float>(rho, ux, uy, uz, feq);
+        for (int q = 0; q < Q; ++q) { fA[q * N + cell] = feq[q]; fB[q * N + cell] = feq[q]; }
+    }
+}
+
 uint16_t oracle_f2h(float f) { return f2h(f); }
 float oracle_h2f(uint16_t h) { return h2f(h); }
 

@@ -63,6 +63,7 @@ def lib():
         _lib.oracle_speck.argtypes = [i, i, i, P, P, f, C.c_uint]
         _lib.oracle_wall_update.argtypes = [i, i, i, P, i, P, P, P, P, P, P, P, P, P, P, P, f, f, f, P]
         _lib.oracle_utau_newton_f64.argtypes = [i, P, P, P, d, i, P]
+        _lib.oracle_apply_flag_edits.argtypes = [i, i, i, P, P, P, P]
         _lib.oracle_f2h.argtypes = [f]
         _lib.oracle_f2h.restype = C.c_uint16
         _lib.oracle_h2f.argtypes = [C.c_uint16]
@@ -150,6 +151,13 @@ def f2h(x: float) -> int:
 
 def h2f(h: int) -> float:
     return float(lib().oracle_h2f(h))
+
+
+def apply_flag_edits(dims, fA, fB, flags, mask):
+    """Warm-restart flag-edit fixup of both buffers (in place)."""
+    lib().oracle_apply_flag_edits(*dims, _p(fA), _p(fB), _p(np.ascontiguousarray(flags, np.uint8)),
+                                  _p(np.ascontiguousarray(mask, np.uint8)))
+    return fA, fB
 
 
 def utau_newton_f64(ut, ys, nu, tol=1e-8, max_iter=100):

@@ -38,6 +38,7 @@ def load():
     core = C.CDLL(str(libs["core"]))
     core.ref_collide.argtypes = [I, I, I, P, P, P, F, F, F, F, I, P, P, P, P, P, P, P]
     core.ref_collide_q.argtypes = [I, I, I, P, P, P, F, F, F, F, I, P, P, P, P, P, P, P, P, P]
+    core.ref_apply_flag_edits.argtypes = [I, I, I, P, P, P, P]
     core.ref_force.argtypes = [I, I, I, P, P, P, P, P, P]
     core.ref_init.argtypes = [I, I, I, P, P, F, F, C.c_uint, I]
     wall = C.CDLL(str(libs["wall"]))
@@ -333,6 +334,30 @@ def case_refine(core, refine, rng):
                         taus=np.array([tauC, tauF], np.float32))
 
 
+def case_edits(core):
+    """Warm-restart flag edit (applyFlagEditsKernel): the collide case's
+    block moved by two cells in x after 20 steps; both buffers fixed up."""
+    rng = np.random.default_rng(20261205)
+    dims = (24, 16, 8)
+    n = int(np.prod(dims))
+    fl = open_flags(24, 16, 8)
+    fl[:, 6:10, 8:12] = 1
+    flags0 = fl.ravel().copy()
+    fl2 = open_flags(24, 16, 8)
+    fl2[:, 6:10, 10:14] = 1
+    fl2[1:3, 5, 10:12] = 1  # and a small new vane
+    flags1 = fl2.ravel().copy()
+    params = dict(tau=0.52, lam=3.0 / 16.0, cs=0.1733, u_in=0.05)
+    fA, _ = run_collide(core, dims, perturbed_state(rng, n), flags0, 20, **params)
+    fB = reset_state(core, dims, flags0, params["u_in"])
+    solid = np.uint8(1)
+    mask = np.where((flags0 == solid) == (flags1 == solid), 0, np.where(flags1 == solid, 1, 2)).astype(np.uint8)
+    outA, outB = fA.copy(), fB.copy()
+    core.ref_apply_flag_edits(*dims, p(outA), p(outB), p(flags1), p(mask))
+    np.savez_compressed(OUT / "edits.npz", dims=np.array(dims), flags0=flags0, flags1=flags1, mask=mask, fA=fA,
+                        fB=fB, outA=outA, outB=outB)
+
+
 def main(cases=None):
     """All cases, or the named ones (e.g. `qlibb`) to leave the others'
     fixtures untouched."""
@@ -341,6 +366,8 @@ def main(cases=None):
         for c in cases:
             if c == "qlibb":
                 case_qlibb(core)
+            elif c == "edits":
+                case_edits(core)
             else:
                 raise SystemExit(f"unknown case {c}")
         return
@@ -352,6 +379,7 @@ def main(cases=None):
     case_wall_list(wl)
     case_refine(core, refine, rng)
     case_qlibb(core)
+    case_edits(core)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -426,6 +426,56 @@ def test_qlibb_collide_vs_reference_golden(fc, golden, case, steps, slip, kernel
     assert s.q_link_info(0)[0] is False
 
 
+def test_flag_edit_warm_restart_vs_reference_golden(fc, golden, oracle_mod):
+    """Warm-restart geometry edit (the reference's applyEditedFlags with its
+    applyFlagEditsKernel fixup) through the C ABI against the reference's
+    own output, then 30 steps on the edited geometry against the oracle."""
+    g = golden("edits")
+    dims = tuple(int(x) for x in g["dims"])
+    s = make(fc, dims, g["flags0"], 0.52, 0.05)
+    s.import_f32(g["fA"])
+    steps0 = s.step_count()
+    assert s.apply_edited_flags(g["flags1"]) == int((g["mask"] != 0).sum())
+    assert s.step_count() == steps0
+    f = s.export_f32()
+    assert np.array_equal(f, g["outA"])
+    # A second call with the same flags changes nothing.
+    assert s.apply_edited_flags(g["flags1"]) == 0
+    assert np.array_equal(s.export_f32(), g["outA"])
+    o = oracle_mod.OracleSolver(dims, g["flags1"], np.float32(0.52), np.float32(0.05))
+    o.set_state(g["outA"])
+    assert s.step_n(30) == 0 and not s.nan_detected()
+    o.step_n(30)
+    m = written_mask(g["flags1"])
+    assert np.array_equal(s.export_f32().reshape(19, -1)[:, m], o.f.reshape(19, -1)[:, m])
+    fg = s.force_raw()
+    assert np.allclose(fg, o.last_force, rtol=1e-5, atol=1e-6 * np.abs(o.last_force).max())
+
+
+def test_flag_edit_fp16_storage(fc, golden, oracle_mod):
+    """The same edit with FP16 deviation storage: the oracle fixup of the
+    stored (rounded) state, rounded on store, within half an FP16 ulp of the
+    deviation."""
+    g = golden("edits")
+    dims = tuple(int(x) for x in g["dims"])
+    s = make(fc, dims, g["flags0"], 0.52, 0.05, storage="fp16")
+    s.import_f32(g["fA"])
+    a = s.export_f32()
+    b = a.copy()
+    oracle_mod.apply_flag_edits(dims, a, b, g["flags1"], g["mask"])
+    s.apply_edited_flags(g["flags1"])
+    f = s.export_f32()
+    edited = np.tile(g["mask"] != 0, 19)
+    assert np.array_equal(f[~edited], a[~edited])
+    # Newly fluid: FP32 equilibrium, deviation rounded to FP16 (|f - w| <
+    # 0.03, so half an ulp < 2e-5). Newly solid: a zero population stores
+    # half(-w_q), half an ulp of w_q <= 1/3 away from zero.
+    fluid = np.tile(g["mask"] == 2, 19)
+    solid = np.tile(g["mask"] == 1, 19)
+    assert np.abs(f[fluid] - a[fluid]).max() <= 2e-5
+    assert np.abs(f[solid]).max() <= 1.25e-4
+
+
 def _three_level_case(fc, oracle_mod):
     """Coarse 48x32x4 open channel, a 2:1 patch, and a 2:1 finer patch nested
     in it, around a block voxelised at every level."""

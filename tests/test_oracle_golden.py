@@ -116,3 +116,14 @@ def test_refine_fill_and_restrict(golden, oracle_mod):
                             (np.float32(m) * tauC) / tauF, mac)
     assert np.array_equal(fc, g["restricted"])
     assert np.array_equal(np.stack(mac), g["rmacro"])
+
+
+def test_flag_edit_fixup_bit_exact(golden, oracle_mod):
+    """applyFlagEditsKernel (lbm_core.cu:644-717): newly solid cells zeroed,
+    newly fluid cells equilibrium-filled from their unedited fluid
+    neighbours, in both buffers."""
+    g = golden("edits")
+    dims = tuple(int(x) for x in g["dims"])
+    a, b = g["fA"].copy(), g["fB"].copy()
+    oracle_mod.apply_flag_edits(dims, a, b, g["flags1"], g["mask"])
+    assert np.array_equal(a, g["outA"]) and np.array_equal(b, g["outB"])
