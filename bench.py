@@ -571,6 +571,54 @@ def precision_leg():
     return out
 
 
+def geometry_leg(t, reps=3):
+    """Flag fields, patch box and cell lists of the airfoil tunnel built on
+    the host (the C++ builders; wall lists on all host threads) and on the
+    device (geometry kernels); both produce the same bytes, checked here."""
+    import torch
+    import foil_cfd_gb300 as fc
+    from foil_cfd_gb300 import geometry as geo
+    from foil_cfd_gb300.tunnels import airfoil_tunnel, widen_box
+    nx, ny, nz = t.dims
+    aoa, chord = t.extra["aoa"], t.chord_cells
+    m = int(round(0.1 * chord))
+    t0 = time.perf_counter()
+    th = airfoil_tunnel(nx, ny, nz, chord=chord, aoa=aoa)
+    t1 = time.perf_counter()
+    wc = fc.build_wall_list(th.dims, th.flags, None, 2)
+    wf = fc.build_wall_list(th.fine_dims, th.fine_flags, None, 3)
+    t2 = time.perf_counter()
+    best = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        d0 = time.perf_counter()
+        cf = geo.clean_foil_flags(th.dims, "0012", aoa, chord)
+        box = widen_box(geo.derive_patch_box(th.dims, cf, m, m, m, m, 3), nx)
+        fd, ff = geo.fine_patch_flags(th.dims, box, 2, "0012", aoa, chord)
+        torch.cuda.synchronize()
+        d1 = time.perf_counter()
+        dwc = geo.wall_list(th.dims, cf, None, 2)
+        dwf = geo.wall_list(fd, ff, None, 3)
+        lc = geo.force_links(th.dims, cf)
+        lf = geo.force_links(fd, ff)
+        torch.cuda.synchronize()
+        d2 = time.perf_counter()
+        if best is None or d2 - d0 < best[0] + best[1]:
+            best = (d1 - d0, d2 - d1)
+    same = (box == th.box and bool(torch.equal(cf.cpu(), torch.from_numpy(th.flags)))
+            and bool(torch.equal(ff.cpu(), torch.from_numpy(th.fine_flags)))
+            and dwc["stats"] == wc["stats"] and dwf["stats"] == wf["stats"]
+            and np.array_equal(dwf["cell"].cpu().numpy().astype(np.int64), wf["cell"]))
+    del cf, ff, dwc, dwf, lc, lf
+    return {"what": "coarse clean-foil flags + patch box + fine-patch flags, then wall-model lists of both levels "
+                    "(device also builds both force-link lists)",
+            "cells": int(np.prod(th.dims) + np.prod(th.fine_dims)),
+            "host_flags_ms": round((t1 - t0) * 1e3, 1), "host_lists_ms": round((t2 - t1) * 1e3, 1),
+            "device_flags_ms": round(best[0] * 1e3, 2), "device_lists_ms": round(best[1] * 1e3, 2),
+            "speedup": round((t2 - t0) / (best[0] + best[1]), 1), "host_threads": os.cpu_count(),
+            "identical": same}
+
+
 def cpu_host():
     try:
         model = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -632,6 +680,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wallnet", action="store_true", help="skip the learned wall-seed leg")
     ap.add_argument("--no-polar", action="store_true", help="skip the batched-polar leg")
+    ap.add_argument("--no-geometry", action="store_true", help="skip the host-vs-device geometry build leg")
+    ap.add_argument("--only-geometry", action="store_true", help="run only the geometry build leg")
     ap.add_argument("--polar-steps", type=int, default=10000)
     ap.add_argument("--precision", action="store_true",
                     help="add the FP32/FP16/FP64 precision study (cylinder, airfoil, Taylor-Green)")
@@ -674,6 +724,10 @@ def main():
         if rank == 0:
             print(json.dumps({"precision": precision_leg()}))
         return
+    if args.only_geometry:
+        if rank == 0:
+            print(json.dumps({"geometry_build": geometry_leg(t)}))
+        return
     if args.only_polar:
         if rank == 0:
             fixed = tuple(int(v) for v in args.polar_config.split(",")) if args.polar_config else None
@@ -713,6 +767,8 @@ def main():
     r32["solver"] = None
     if not args.no_polar and ws == 1:
         line["batched_polar"] = polar_leg(args.polar_steps)
+    if not args.no_geometry and ws == 1 and not args.small:
+        line["geometry_build"] = geometry_leg(t)
     if args.precision and ws == 1:
         line["precision"] = precision_leg()
     del r32

@@ -12,7 +12,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import capi
-from .solver import STORE, SolverError, boundary_flags, naca4, voxelize_airfoil
+from .solver import STORE, SolverError, boundary_flags, layout_anchor, naca4, voxelize_airfoil
 
 Q = 19
 FLAG_OUTLET, FLAG_OUTLET_EQ = 3, 9
@@ -49,7 +49,7 @@ def polar_tunnels(count: int = 24, seed: int = 0, span: int = 16, u_lat: float =
         flags = boundary_flags(dims)
         if outlet_eq:
             flags[flags == FLAG_OUTLET] = FLAG_OUTLET_EQ
-        voxelize_airfoil(dims, flags, naca4(digits, 200), aoa, c, 0.3 * dims[0], 0.5 * dims[1])
+        voxelize_airfoil(dims, flags, naca4(digits, 200), aoa, c, *layout_anchor(dims))
         tau = float(np.float32(0.5 + 3.0 * u_lat * c / reynolds))
         out.append(PolarTunnel(digits, aoa, c, dims, flags, tau, u_lat))
     return out

@@ -23,11 +23,12 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr"] + ARCH
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off"]
 # Per-file extra flags: the FP32 reference-order kernels and the refinement
 # coupling must not contract multiply-adds (their rounding follows the
 # reference expression tree, so results are bit-identical to it).
-FILE_FLAGS = {"collide_f32.cu": ["--fmad=false"], "refine_kernels.cu": ["--fmad=false"], "batch_f32.cu": ["--fmad=false"]}
+FILE_FLAGS = {"collide_f32.cu": ["--fmad=false"], "refine_kernels.cu": ["--fmad=false"], "batch_f32.cu": ["--fmad=false"],
+              "geom_kernels.cu": ["--fmad=false"]}
 
 
 def _cuda_home() -> Path:

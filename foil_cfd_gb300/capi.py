@@ -1,6 +1,7 @@
 """ctypes binding of include/foilcfd_step.h (the solver step's C ABI),
-include/foilcfd_wallnet.h (the learned u_tau seed) and
-include/foilcfd_batch.h (the batched multi-tunnel step).
+include/foilcfd_wallnet.h (the learned u_tau seed),
+include/foilcfd_batch.h (the batched multi-tunnel step) and
+include/foilcfd_geom.h (the on-device geometry builders).
 
 Loading fails loudly when the compiled library is missing: there is no CPU
 fallback for the solver step. Build it with ``foil_cfd_gb300.build_lib``
@@ -32,6 +33,12 @@ class Options(C.Structure):
 
 class PatchBox(C.Structure):
     _fields_ = [("x0", C.c_int), ("y0", C.c_int), ("x1", C.c_int), ("y1", C.c_int)]
+
+
+class Foil(C.Structure):
+    """fcfd_foil (foilcfd_geom.h): host outline + placement."""
+    _fields_ = [("xy", C.c_void_p), ("npts", C.c_int), ("aoa_deg", C.c_float), ("chord_cells", C.c_int),
+                ("anchor_x", C.c_float), ("anchor_y", C.c_float)]
 
 
 class ForceReadout(C.Structure):
@@ -147,6 +154,13 @@ _SIGS = {
     "fcfd_build_wall_list": (C.c_longlong, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P]),
     "fcfd_boundary_flags": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
     "fcfd_naca4": (C.c_int, [C.c_char_p, C.c_int, P, C.c_int]),
+    "fcfd_close_trailing_edge_gaps": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
+    "fcfd_device_build_flags": (C.c_int, [C.POINTER(Dims), C.c_int, P, P, C.c_int, C.c_int, P, P, P]),
+    "fcfd_device_derive_patch_box": (C.c_int, [C.POINTER(Dims), P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P,
+                                               C.POINTER(PatchBox)]),
+    "fcfd_device_force_links": (C.c_int, [C.POINTER(Dims), P, P, P, C.c_longlong, P, P]),
+    "fcfd_device_build_wall_list": (C.c_int, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P,
+                                              P, P]),
     "fcfd_voxelize_airfoil": (C.c_int, [C.POINTER(Dims), P, C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, P,
                                         C.c_size_t]),
     "fcfd_stamp_interface_shell": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),

@@ -210,12 +210,20 @@ int naca4(const char* digits, int pps, std::vector<float>& xy) {
     return static_cast<int>(xy.size() / 2);
 }
 
-int voxelize_airfoil(const LevelDims& d, const float* xy, int npts, float aoaDeg, int chordCells,
-                     float ax, float ay, std::uint8_t* flags) {
-    if (d.nx < 3 || d.ny < 3 || d.nz < 1 || npts < 3) return 0;
+void foil_rotation(float aoaDeg, float& c, float& s) {
     const float pi = 3.14159265358979f;
     const float a = aoaDeg * pi / 180.0f;
-    const float ca = std::cos(-a), sa = std::sin(-a);
+    c = std::cos(-a);
+    s = std::sin(-a);
+}
+
+void voxelize_airfoil(const LevelDims& d, const float* xy, int npts, float aoaDeg, int chordCells,
+                      float ax, float ay, std::uint8_t* flags) {
+    // An outline of fewer than 20 points is not a valid section: nothing is
+    // stamped (AirfoilGeometry::isValid, src/geom/airfoil.h:37).
+    if (d.nx < 3 || d.ny < 3 || d.nz < 1 || npts < kMinOutlinePoints) return;
+    float ca, sa;
+    foil_rotation(aoaDeg, ca, sa);
     const float chord = static_cast<float>(chordCells);
     std::vector<float> px(npts), py(npts);
     float minY = 1e30f, maxY = -1e30f;
@@ -255,8 +263,12 @@ int voxelize_airfoil(const LevelDims& d, const float* xy, int npts, float aoaDeg
                 std::uint8_t& c = flags[idx(x, y, z, d)];
                 if (mask[static_cast<size_t>(y) * d.nx + x] && c == kFlagFluidHost) c = kFlagSolidHost;
             }
-    // Trailing-edge closure: a fluid cell with solid directly above and
-    // below (judged on the pre-closure field) becomes solid.
+}
+
+int close_trailing_edge_gaps(const LevelDims& d, std::uint8_t* flags) {
+    if (d.nx < 3 || d.ny < 3 || d.nz < 1) return 0;
+    // A fluid cell with solid directly above and below (judged on the
+    // pre-closure field, so closures do not cascade) becomes solid.
     const std::vector<std::uint8_t> before(flags, flags + d.cells());
     int closed = 0;
     const long long nx = d.nx;

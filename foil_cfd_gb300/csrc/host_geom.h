@@ -42,9 +42,16 @@ void build_force_links(const LevelDims& d, const std::uint8_t* flags,
 
 void boundary_flags(const LevelDims& d, std::uint8_t* flags);
 int naca4(const char* digits, int pointsPerSurface, std::vector<float>& xy);
-int voxelize_airfoil(const LevelDims& d, const float* xy, int npts, float aoaDeg,
-                     int chordCells, float anchorX, float anchorY,
-                     std::uint8_t* flags);
+constexpr int kMinOutlinePoints = 20;  ///< smallest valid section outline
+/// Cosine and sine of the outline rotation (-AoA about the quarter chord),
+/// evaluated as the reference's rotated(p, -aoaRad) does (src/core/vec.h:42-46).
+void foil_rotation(float aoaDeg, float& c, float& s);
+/// voxelizeAirfoil: only Fluid cells inside the outline become Solid.
+void voxelize_airfoil(const LevelDims& d, const float* xy, int npts, float aoaDeg,
+                      int chordCells, float anchorX, float anchorY,
+                      std::uint8_t* flags);
+/// closeTrailingEdgeGaps: returns the number of cells closed.
+int close_trailing_edge_gaps(const LevelDims& d, std::uint8_t* flags);
 void stamp_interface_shell(const LevelDims& d, std::uint8_t* flags, int shell);
 void derive_patch_box(const LevelDims& d, const std::uint8_t* flags, int mx0,
                       int mx1, int my0, int my1, int clearance, int out[4]);

@@ -197,4 +197,37 @@ cudaError_t launch_restrict_f2c(Storage s, const void* fineF,
                                 float* scratch, float* rho, float* u, float* v,
                                 float* w, cudaStream_t st, bool childDone = false);
 
+// ---- on-device geometry builders (geom_kernels.cu) ----------------------------
+/// An outline to rasterise: HOST xy pairs (normalised chord, Selig loop), the
+/// cosine/sine of the rotation (-AoA), chord in cells and the anchor (cells).
+struct FoilRaster {
+    const float* xy = nullptr;
+    int npts = 0;
+    float cosA = 1.0f, sinA = 0.0f, chord = 0.0f, anchorX = 0.0f, anchorY = 0.0f;
+};
+/// Device SoA outputs of the wall-model cell list.
+struct WallListOut {
+    std::uint32_t *cell = nullptr, *sample = nullptr, *mask = nullptr;
+    float *nX = nullptr, *nY = nullptr, *nZ = nullptr, *ys = nullptr;
+};
+/// Flag field into device `out`: base 0 domain faces, 1 all fluid, 2 the
+/// device field `in`; then the rasterised foil (nullable), the trailing-edge
+/// closure and the interface shell (width `shell`, 0 for none). A non-null
+/// closedOut synchronises and receives the closure count.
+cudaError_t device_build_flags(LevelDims d, int base, const std::uint8_t* in, const FoilRaster* foil, int closeGaps,
+                               int shell, std::uint8_t* out, cudaStream_t st, int* closedOut);
+/// Solid bounding box {x0, y0, x1, y1} (inclusive; x1 < 0 when no solid).
+cudaError_t device_solid_bbox(LevelDims d, const std::uint8_t* flags, cudaStream_t st, int box[4]);
+/// Cells whose flag is read and written / inlet / neither.
+cudaError_t device_flag_classes(LevelDims d, const std::uint8_t* flags, cudaStream_t st, long long out[3]);
+/// Ordered cell lists. *count <- the list length; nothing is written when it
+/// exceeds cap (size with a first call of capacity 0). All synchronise.
+cudaError_t device_force_links(LevelDims d, const std::uint8_t* flags, std::uint32_t* cells, std::uint32_t* masks,
+                               long long cap, long long* count, cudaStream_t st);
+cudaError_t device_cells_where(LevelDims d, const std::uint8_t* flags, std::uint8_t value, bool equal,
+                               std::uint32_t* cells, long long cap, long long* count, cudaStream_t st);
+cudaError_t device_wall_list(LevelDims d, const std::uint8_t* active, const std::uint8_t* clean, int sampleCells,
+                             const WallListOut& out, long long cap, long long* count, int stats[3],
+                             cudaStream_t st);
+
 } // namespace fcfd

@@ -42,6 +42,23 @@ void set_err(char* err, size_t len, const std::string& m) {
     std::snprintf(err, len, "%s", m.c_str());
 }
 
+/// True for a pointer into device memory (a flag field built on the GPU).
+bool on_device(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice;
+}
+
+/// Host copy of a flag field given in host or device memory.
+void assign_flags(std::vector<std::uint8_t>& v, const std::uint8_t* p, size_t n) {
+    v.resize(n);
+    if (on_device(p)) cudaMemcpy(v.data(), p, n, cudaMemcpyDeviceToHost);
+    else std::memcpy(v.data(), p, n);
+}
+
 template <class T>
 cudaError_t dalloc(T** p, size_t bytes) {
     return cudaMalloc(reinterpret_cast<void**>(p), bytes == 0 ? 1 : bytes);
@@ -307,74 +324,115 @@ struct fcfd_solver {
         return cudaSuccess;
     }
 
+    /// Flags of a level from host or device memory: the device copy, the
+    /// host copy (edit diffs), the cell classes, the kind bytes and the
+    /// force-link list, the last two built on the device.
     cudaError_t uploadLevelFlags(Level& L, const std::uint8_t* flags) {
-        L.hostFlags.assign(flags, flags + L.n);
-        L.nReadWrite = L.nInlet = L.nUntouched = 0;
-        for (long long i = 0; i < L.n; ++i) {
-            const std::uint8_t f = flags[i];
-            if (f == FCFD_FLAG_FLUID || f == FCFD_FLAG_OUTLET || f == FCFD_FLAG_OUTLET_EQ) ++L.nReadWrite;
-            else if (f == FCFD_FLAG_INLET) ++L.nInlet;
-            else ++L.nUntouched;
+        L.hostFlags.resize(static_cast<size_t>(L.n));
+        const size_t nb = static_cast<size_t>(L.n);
+        if (on_device(flags)) {
+            if (auto e = cudaMemcpyAsync(L.flags, flags, nb, cudaMemcpyDeviceToDevice, stream); e != cudaSuccess)
+                return e;
+            if (auto e = cudaMemcpyAsync(L.hostFlags.data(), flags, nb, cudaMemcpyDeviceToHost, stream);
+                e != cudaSuccess)
+                return e;
+        } else {
+            std::memcpy(L.hostFlags.data(), flags, nb);
+            if (auto e = cudaMemcpyAsync(L.flags, flags, nb, cudaMemcpyHostToDevice, stream); e != cudaSuccess)
+                return e;
         }
-        if (auto e = cudaMemcpyAsync(L.flags, flags, static_cast<size_t>(L.n), cudaMemcpyHostToDevice, stream);
-            e != cudaSuccess)
-            return e;
+        long long cls[3];
+        launches += 1;
+        if (auto e = device_flag_classes(L.d, L.flags, stream, cls); e != cudaSuccess) return e;
+        L.nReadWrite = cls[0]; L.nInlet = cls[1]; L.nUntouched = cls[2];
         ++launches;
         if (auto e = launch_classify(L.flags, L.kind, L.d, stream); e != cudaSuccess) return e;
-        // Compact force-link list of this level.
-        std::vector<std::uint32_t> cells, masks;
-        build_force_links(L.d, flags, cells, masks);
+        // Compact force-link list of this level (ascending cell order).
         dfree(L.dLinkCells); dfree(L.dLinkMasks); dfree(L.dPartials);
-        L.linkCount = static_cast<int>(cells.size());
-        if (auto e = dalloc(&L.dLinkCells, cells.size() * 4); e != cudaSuccess) return e;
-        if (auto e = dalloc(&L.dLinkMasks, masks.size() * 4); e != cudaSuccess) return e;
+        long long links = 0;
+        launches += 2;
+        if (auto e = device_force_links(L.d, L.flags, nullptr, nullptr, 0, &links, stream); e != cudaSuccess) return e;
+        L.linkCount = static_cast<int>(links);
+        if (auto e = dalloc(&L.dLinkCells, static_cast<size_t>(links) * 4); e != cudaSuccess) return e;
+        if (auto e = dalloc(&L.dLinkMasks, static_cast<size_t>(links) * 4); e != cudaSuccess) return e;
         if (auto e = dalloc(&L.dPartials, static_cast<size_t>(force_blocks(L.linkCount)) * 3 * sizeof(double));
             e != cudaSuccess)
             return e;
-        if (!cells.empty()) {
-            cudaMemcpyAsync(L.dLinkCells, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice, stream);
-            cudaMemcpyAsync(L.dLinkMasks, masks.data(), masks.size() * 4, cudaMemcpyHostToDevice, stream);
+        if (links > 0) {
+            launches += 3;
+            long long again = 0;
+            if (auto e = device_force_links(L.d, L.flags, L.dLinkCells, L.dLinkMasks, links, &again, stream);
+                e != cudaSuccess)
+                return e;
         }
         return cudaStreamSynchronize(stream);
+    }
+
+    /// Ascending list of the level's cells whose flag equals (or, with
+    /// equal false, differs from) `value`, into a fresh device array.
+    cudaError_t cellList(const Level& L, std::uint8_t value, bool equal, std::uint32_t** out, int* count) {
+        dfree(*out);
+        *count = 0;
+        long long c = 0;
+        launches += 2;
+        if (auto e = device_cells_where(L.d, L.flags, value, equal, nullptr, 0, &c, stream); e != cudaSuccess)
+            return e;
+        if (auto e = dalloc(out, static_cast<size_t>(c) * 4); e != cudaSuccess) return e;
+        if (c > 0) {
+            launches += 3;
+            long long again = 0;
+            if (auto e = device_cells_where(L.d, L.flags, value, equal, *out, c, &again, stream); e != cudaSuccess)
+                return e;
+        }
+        *count = static_cast<int>(c);
+        return cudaSuccess;
     }
 
     cudaError_t buildWM(Level& L, int sampleCells) {
         L.wm.free();
         if (!wmEnabled || L.hostFlags.size() != static_cast<size_t>(L.n)) return cudaSuccess;
-        const std::vector<std::uint8_t>& clean =
-            L.surfaceRef.size() == L.hostFlags.size() ? L.surfaceRef : L.hostFlags;
-        WallListStats st;
-        WallList wl = build_wall_list(L.d, L.hostFlags.data(), clean.data(), sampleCells, &st);
-        L.wm.build = st;
-        if (wl.size() == 0) return cudaSuccess;
-        const size_t n = wl.size();
-        std::vector<std::uint32_t> ci(n), si(n);
-        for (size_t i = 0; i < n; ++i) {
-            ci[i] = static_cast<std::uint32_t>(wl.cellIdx[i]);
-            si[i] = static_cast<std::uint32_t>(wl.sampleIdx[i]);
+        const size_t cells = static_cast<size_t>(L.n);
+        // Normals key off the clean surface reference when one is set.
+        std::uint8_t* dClean = nullptr;
+        cudaError_t e = cudaSuccess;
+        if (L.surfaceRef.size() == cells) {
+            e = dalloc(&dClean, cells);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(dClean, L.surfaceRef.data(), cells, cudaMemcpyHostToDevice, stream);
+        }
+        long long n = 0;
+        int st[3] = {0, 0, 0};
+        WallListOut none;
+        launches += 2;
+        if (e == cudaSuccess)
+            e = device_wall_list(L.d, L.flags, dClean ? dClean : L.flags, sampleCells, none, 0, &n, st, stream);
+        L.wm.build.listed = st[0]; L.wm.build.excludedVG = st[1]; L.wm.build.degenerate = st[2];
+        if (e != cudaSuccess || n == 0) {
+            dfree(dClean);
+            return e;
         }
         WMLevel& m = L.wm;
-        const size_t cells = static_cast<size_t>(L.n);
-        cudaError_t e = cudaSuccess;
         auto A = [&](auto** p, size_t b) { if (e == cudaSuccess) e = dalloc(p, b); };
-        A(&m.dCell, n * 4); A(&m.dSample, n * 4); A(&m.dMask, n * 4);
-        A(&m.dNx, n * 4); A(&m.dNy, n * 4); A(&m.dNz, n * 4); A(&m.dYs, n * 4); A(&m.dUTau, n * 4);
+        const size_t nn = static_cast<size_t>(n);
+        A(&m.dCell, nn * 4); A(&m.dSample, nn * 4); A(&m.dMask, nn * 4);
+        A(&m.dNx, nn * 4); A(&m.dNy, nn * 4); A(&m.dNz, nn * 4); A(&m.dYs, nn * 4); A(&m.dUTau, nn * 4);
         A(&m.dUwx, cells * 2); A(&m.dUwy, cells * 2); A(&m.dUwz, cells * 2);
         A(&m.dStats, sizeof(WallStatsDev));
-        if (e != cudaSuccess) { m.free(); return e; }
-        auto U = [&](void* d, const void* h, size_t b) {
-            if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, stream);
-        };
-        U(m.dCell, ci.data(), n * 4); U(m.dSample, si.data(), n * 4);
-        U(m.dMask, wl.linkMask.data(), n * 4);
-        U(m.dNx, wl.nX.data(), n * 4); U(m.dNy, wl.nY.data(), n * 4); U(m.dNz, wl.nZ.data(), n * 4);
-        U(m.dYs, wl.ys.data(), n * 4);
-        if (e == cudaSuccess) e = cudaMemsetAsync(m.dUTau, 0, n * 4, stream);
+        if (e == cudaSuccess) {
+            WallListOut o;
+            o.cell = m.dCell; o.sample = m.dSample; o.mask = m.dMask;
+            o.nX = m.dNx; o.nY = m.dNy; o.nZ = m.dNz; o.ys = m.dYs;
+            long long again = 0;
+            launches += 3;
+            e = device_wall_list(L.d, L.flags, dClean ? dClean : L.flags, sampleCells, o, n, &again, st, stream);
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(m.dUTau, 0, nn * 4, stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(m.dUwx, 0, cells * 2, stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(m.dUwy, 0, cells * 2, stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(m.dUwz, 0, cells * 2, stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(m.dStats, 0, sizeof(WallStatsDev), stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        dfree(dClean);
         if (e != cudaSuccess) { m.free(); return e; }
         m.count = static_cast<int>(n);
         m.active = true;
@@ -444,20 +502,17 @@ struct fcfd_solver {
         return cudaSuccess;
     }
 
+    /// Forces come from the fine level when every coarse solid cell lies in
+    /// the patch's restriction region (the reference's surface-cache test).
     void updateForcesFromFine() {
         forcesFromFine = false;
         if (!fineActive) return;
         const int x0 = box.x0 + kRestrictBandHost, x1 = box.x1 - kRestrictBandHost;
         const int y0 = box.y0 + kRestrictBandHost, y1 = box.y1 - kRestrictBandHost;
-        const LevelDims& d = dims;
-        for (int z = 0; z < d.nz; ++z)
-            for (int y = 0; y < d.ny; ++y)
-                for (int x = 0; x < d.nx; ++x) {
-                    const size_t i = static_cast<size_t>(x) + static_cast<size_t>(d.nx) * (y + static_cast<size_t>(d.ny) * z);
-                    if (coarse.hostFlags[i] != 1) continue;
-                    if (x < x0 || x >= x1 || y < y0 || y >= y1) return;
-                }
-        forcesFromFine = true;
+        int b[4];
+        ++launches;
+        if (device_solid_bbox(coarse.d, coarse.flags, stream, b) != cudaSuccess) return;
+        forcesFromFine = b[2] < 0 || (b[0] >= x0 && b[2] < x1 && b[1] >= y0 && b[3] < y1);
     }
 
     void freeFine() {
@@ -821,8 +876,14 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
         set_err(err, errlen, "flag field size does not match grid dimensions");
         return cudaErrorInvalidValue;
     }
+    std::vector<std::uint8_t> hostCopy;
+    const uint8_t* hf = flags;
+    if (on_device(flags)) {
+        assign_flags(hostCopy, flags, n);
+        hf = hostCopy.data();
+    }
     for (size_t i = 0; i < n; ++i)
-        if (flags[i] > FCFD_FLAG_OUTLET_EQ) {
+        if (hf[i] > FCFD_FLAG_OUTLET_EQ) {
             set_err(err, errlen, "flag field holds an unknown cell flag value");
             return cudaErrorInvalidValue;
         }
@@ -871,7 +932,7 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
     s->zSlipWalls = false;
     const size_t nxny = static_cast<size_t>(d.nx) * d.ny;
     for (size_t i = 0; i < nxny; ++i)
-        if (flags[i] == FCFD_FLAG_SLIP_FRONT) { s->zSlipWalls = true; break; }
+        if (hf[i] == FCFD_FLAG_SLIP_FRONT) { s->zSlipWalls = true; break; }
     if (auto e = s->buildWM(s->coarse, kWallSampleCoarse); e != cudaSuccess) return fail("wall list upload failed", e);
     s->initialized = true;
     s->reset();
@@ -898,12 +959,18 @@ int fcfd_apply_edited_flags(fcfd_solver* s, const uint8_t* flags, size_t n, long
     if (edited) *edited = 0;
     if (!s || !s->initialized || !flags || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
     Level& L = s->coarse;
+    std::vector<std::uint8_t> hostNew;
+    const std::uint8_t* nf = flags;
+    if (on_device(flags)) {
+        assign_flags(hostNew, flags, n);
+        nf = hostNew.data();
+    }
     // Diff before the host copy is replaced: 1 newly solid, 2 newly fluid.
     std::vector<std::uint8_t> mask(static_cast<size_t>(L.n), 0);
     long long count = 0;
     for (long long i = 0; i < L.n; ++i) {
         const bool was = L.hostFlags[static_cast<size_t>(i)] == FCFD_FLAG_SOLID;
-        const bool now = flags[i] == FCFD_FLAG_SOLID;
+        const bool now = nf[i] == FCFD_FLAG_SOLID;
         if (was == now) continue;
         mask[static_cast<size_t>(i)] = now ? 1 : 2;
         ++count;
@@ -1130,7 +1197,7 @@ int fcfd_set_wall_model(fcfd_solver* s, int enabled) {
 int fcfd_set_surface_reference(fcfd_solver* s, const uint8_t* clean, size_t n) {
     if (!s || !s->initialized || !clean || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
     cudaStreamSynchronize(s->stream);
-    s->coarse.surfaceRef.assign(clean, clean + n);
+    assign_flags(s->coarse.surfaceRef, clean, n);
     return s->buildWM(s->coarse, kWallSampleCoarse);
 }
 
@@ -1138,7 +1205,7 @@ int fcfd_set_refined_surface_reference(fcfd_solver* s, const uint8_t* clean, siz
     if (!s || !s->initialized || !s->fineActive || !clean || n != static_cast<size_t>(s->fine.n))
         return cudaErrorInvalidValue;
     cudaStreamSynchronize(s->stream);
-    s->fine.surfaceRef.assign(clean, clean + n);
+    assign_flags(s->fine.surfaceRef, clean, n);
     return s->buildWM(s->fine, kWallSampleFine);
 }
 
@@ -1270,17 +1337,10 @@ int fcfd_init_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor, 
     };
     if (auto e = s->allocLevel(s->fine, fd); e != cudaSuccess) return fail("fine buffer allocation failed", e);
     if (auto e = s->uploadLevelFlags(s->fine, ff); e != cudaSuccess) return fail("fine flag upload failed", e);
-    std::vector<std::uint32_t> shell, seed;
-    for (size_t i = 0; i < n; ++i) {
-        if (ff[i] == FCFD_FLAG_INTERFACE) shell.push_back(static_cast<std::uint32_t>(i));
-        if (ff[i] != FCFD_FLAG_SOLID) seed.push_back(static_cast<std::uint32_t>(i));
-    }
-    s->shellCount = static_cast<int>(shell.size());
-    s->seedCount = static_cast<int>(seed.size());
-    if (auto e = dalloc(&s->dShell, shell.size() * 4); e != cudaSuccess) return fail("shell list allocation failed", e);
-    if (auto e = dalloc(&s->dSeed, seed.size() * 4); e != cudaSuccess) return fail("seed list allocation failed", e);
-    if (!shell.empty()) cudaMemcpy(s->dShell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice);
-    if (!seed.empty()) cudaMemcpy(s->dSeed, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
+    if (auto e = s->cellList(s->fine, FCFD_FLAG_INTERFACE, true, &s->dShell, &s->shellCount); e != cudaSuccess)
+        return fail("shell list failed", e);
+    if (auto e = s->cellList(s->fine, FCFD_FLAG_SOLID, false, &s->dSeed, &s->seedCount); e != cudaSuccess)
+        return fail("seed list failed", e);
     s->fineActive = true;
     const long long sf = restrict_scratch_floats(s->geom());
     if (sf <= 0) return fail("restriction sub-box is empty", cudaErrorInvalidValue);
@@ -1304,18 +1364,9 @@ int fcfd_set_refined_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {
     if (!s || !s->initialized || !s->fineActive || !ff || n != static_cast<size_t>(s->fine.n))
         return cudaErrorInvalidValue;
     if (auto e = s->uploadLevelFlags(s->fine, ff); e != cudaSuccess) return e;
-    std::vector<std::uint32_t> shell, seed;
-    for (size_t i = 0; i < n; ++i) {
-        if (ff[i] == FCFD_FLAG_INTERFACE) shell.push_back(static_cast<std::uint32_t>(i));
-        if (ff[i] != FCFD_FLAG_SOLID) seed.push_back(static_cast<std::uint32_t>(i));
-    }
-    dfree(s->dShell); dfree(s->dSeed);
-    s->shellCount = static_cast<int>(shell.size());
-    s->seedCount = static_cast<int>(seed.size());
-    if (auto e = dalloc(&s->dShell, shell.size() * 4); e != cudaSuccess) return e;
-    if (auto e = dalloc(&s->dSeed, seed.size() * 4); e != cudaSuccess) return e;
-    if (!shell.empty()) cudaMemcpy(s->dShell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice);
-    if (!seed.empty()) cudaMemcpy(s->dSeed, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
+    if (auto e = s->cellList(s->fine, FCFD_FLAG_INTERFACE, true, &s->dShell, &s->shellCount); e != cudaSuccess)
+        return e;
+    if (auto e = s->cellList(s->fine, FCFD_FLAG_SOLID, false, &s->dSeed, &s->seedCount); e != cudaSuccess) return e;
     s->updateForcesFromFine();
     if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return e;
     if (auto e = s->seedFine(); e != cudaSuccess) return e;
@@ -1389,7 +1440,15 @@ int fcfd_voxelize_airfoil(const fcfd_dims* dims, const float* xy, int npts, floa
     if (!dims || !xy || !flags) return -1;
     LevelDims d{dims->nx, dims->ny, dims->nz};
     if (n != static_cast<size_t>(d.cells())) return -1;
-    return voxelize_airfoil(d, xy, npts, aoa, chord, ax, ay, flags);
+    voxelize_airfoil(d, xy, npts, aoa, chord, ax, ay, flags);
+    return 0;
+}
+
+int fcfd_close_trailing_edge_gaps(const fcfd_dims* dims, uint8_t* flags, size_t n) {
+    if (!dims || !flags) return -1;
+    LevelDims d{dims->nx, dims->ny, dims->nz};
+    if (n != static_cast<size_t>(d.cells())) return -1;
+    return close_trailing_edge_gaps(d, flags);
 }
 
 int fcfd_stamp_interface_shell(const fcfd_dims* dims, uint8_t* flags, size_t n) {
@@ -1587,21 +1646,12 @@ int fcfd_q_link_info(fcfd_solver* s, int level, int* active, int* links, int* fa
 
 // ---- nested finer level (initFinerRefinement & co, lbm_solver.cpp:1916-2010)
 
-static int finer_lists(fcfd_solver* s, const uint8_t* ff, size_t n) {
-    std::vector<std::uint32_t> shell, seed;
-    for (size_t i = 0; i < n; ++i) {
-        if (ff[i] == FCFD_FLAG_INTERFACE) shell.push_back(static_cast<std::uint32_t>(i));
-        if (ff[i] != FCFD_FLAG_SOLID) seed.push_back(static_cast<std::uint32_t>(i));
-    }
-    dfree(s->dShellFiner);
-    dfree(s->dSeedFiner);
-    s->shellCountFiner = static_cast<int>(shell.size());
-    s->seedCountFiner = static_cast<int>(seed.size());
-    if (auto e = dalloc(&s->dShellFiner, shell.size() * 4); e != cudaSuccess) return e;
-    if (auto e = dalloc(&s->dSeedFiner, seed.size() * 4); e != cudaSuccess) return e;
-    if (!shell.empty()) cudaMemcpy(s->dShellFiner, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice);
-    if (!seed.empty()) cudaMemcpy(s->dSeedFiner, seed.data(), seed.size() * 4, cudaMemcpyHostToDevice);
-    return 0;
+/// Interface-shell and seed lists of the finer level (its flags uploaded).
+static int finer_lists(fcfd_solver* s) {
+    if (auto e = s->cellList(s->finer, FCFD_FLAG_INTERFACE, true, &s->dShellFiner, &s->shellCountFiner);
+        e != cudaSuccess)
+        return e;
+    return s->cellList(s->finer, FCFD_FLAG_SOLID, false, &s->dSeedFiner, &s->seedCountFiner);
 }
 
 int fcfd_init_finer_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor, const uint8_t* ff,
@@ -1649,7 +1699,7 @@ int fcfd_init_finer_refinement(fcfd_solver* s, const fcfd_patch_box* box, int fa
     };
     if (auto e = s->allocLevel(s->finer, fd); e != cudaSuccess) return fail("finer buffer allocation failed", e);
     if (auto e = s->uploadLevelFlags(s->finer, ff); e != cudaSuccess) return fail("finer flag upload failed", e);
-    if (auto e = static_cast<cudaError_t>(finer_lists(s, ff, n)); e != cudaSuccess)
+    if (auto e = static_cast<cudaError_t>(finer_lists(s)); e != cudaSuccess)
         return fail("finer target lists failed", e);
     s->finerActive = true;
     const long long sf = restrict_scratch_floats(s->geomFiner());
@@ -1673,7 +1723,7 @@ int fcfd_set_refined_finer_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {
     if (!s || !s->initialized || !s->finerActive || !ff || n != static_cast<size_t>(s->finer.n))
         return cudaErrorInvalidValue;
     if (auto e = s->uploadLevelFlags(s->finer, ff); e != cudaSuccess) return e;
-    if (auto e = finer_lists(s, ff, n); e != 0) return e;
+    if (auto e = finer_lists(s); e != 0) return e;
     if (auto e = s->buildWM(s->finer, kWallSampleFine); e != cudaSuccess) return e;
     return s->seedFiner();
 }
@@ -1682,7 +1732,7 @@ int fcfd_set_refined_finer_surface_reference(fcfd_solver* s, const uint8_t* clea
     if (!s || !s->initialized || !s->finerActive || !clean || n != static_cast<size_t>(s->finer.n))
         return cudaErrorInvalidValue;
     cudaStreamSynchronize(s->stream);
-    s->finer.surfaceRef.assign(clean, clean + n);
+    assign_flags(s->finer.surfaceRef, clean, n);
     return s->buildWM(s->finer, kWallSampleFine);
 }
 

@@ -15,6 +15,18 @@ import numpy as np
 from . import capi
 from .capi import ptr
 
+
+def _flags_arg(flags):
+    """(void* pointer, byte count, keep-alive) of a flag field given as host
+    bytes (anything numpy takes) or as a contiguous uint8 CUDA tensor (a
+    field built on the device; the C ABI detects device memory)."""
+    if getattr(flags, "is_cuda", False):
+        if flags.element_size() != 1 or not flags.is_contiguous():
+            raise SolverError("device flag field must be a contiguous uint8 tensor")
+        return C.c_void_p(flags.data_ptr()), flags.numel(), flags
+    a = np.ascontiguousarray(flags, np.uint8)
+    return ptr(a), a.size, a
+
 Q = 19
 FLAG = dict(fluid=0, solid=1, inlet=2, outlet=3, slip_top=4, slip_bottom=5, slip_front=6, slip_back=7,
             interface=8, outlet_eq=9)
@@ -99,13 +111,13 @@ class LBMSolver:
              les_cs: float | None = None, magic_lambda: float | None = None, kernel: str = "auto") -> None:
         """kernel: "auto", "cell" (one cell per thread) or "staged" (rows
         streamed through shared memory by bulk async copies)."""
-        flags = np.ascontiguousarray(flags, np.uint8)
+        fp, fn, _keep = _flags_arg(flags)
         d = capi.Dims(*dims)
         opt = capi.Options(STORE[storage], 0.0 if les_cs is None else (les_cs if les_cs > 0 else -1.0),
                            0.0 if magic_lambda is None else magic_lambda, 0,
                            {"auto": 0, "cell": 1, "staged": 2}[kernel])
         err = C.create_string_buffer(512)
-        rc = self._lib.fcfd_init(self._h, C.byref(d), C.byref(scaling), ptr(flags), flags.size, stream,
+        rc = self._lib.fcfd_init(self._h, C.byref(d), C.byref(scaling), fp, fn, stream,
                                  C.byref(opt), err, 512)
         if rc != 0:
             raise SolverError(err.value.decode() or f"init failed ({rc})")
@@ -121,16 +133,16 @@ class LBMSolver:
         self._lib.fcfd_reset(self._h)
 
     def set_flags(self, flags):
-        flags = np.ascontiguousarray(flags, np.uint8)
-        return self._lib.fcfd_set_flags(self._h, ptr(flags), flags.size)
+        fp, fn, _keep = _flags_arg(flags)
+        return self._lib.fcfd_set_flags(self._h, fp, fn)
 
     def apply_edited_flags(self, flags) -> int:
         """LBMSolver::applyEditedFlags (src/sim/lbm_solver.cpp:1086-1126):
         warm restart after a geometry edit; returns the number of cells whose
         solid state changed. Raises on a CUDA error."""
-        flags = np.ascontiguousarray(flags, np.uint8)
+        fp, fn, _keep = _flags_arg(flags)
         edited = C.c_longlong(0)
-        rc = self._lib.fcfd_apply_edited_flags(self._h, ptr(flags), flags.size, C.byref(edited))
+        rc = self._lib.fcfd_apply_edited_flags(self._h, fp, fn, C.byref(edited))
         if rc != 0:
             raise RuntimeError(f"fcfd_apply_edited_flags failed ({rc})")
         return int(edited.value)
@@ -231,12 +243,12 @@ class LBMSolver:
             raise SolverError(f"wall model setup failed ({rc})")
 
     def set_surface_reference(self, clean):
-        clean = np.ascontiguousarray(clean, np.uint8)
-        return self._lib.fcfd_set_surface_reference(self._h, ptr(clean), clean.size)
+        cp, cn, _keep = _flags_arg(clean)
+        return self._lib.fcfd_set_surface_reference(self._h, cp, cn)
 
     def set_refined_surface_reference(self, clean):
-        clean = np.ascontiguousarray(clean, np.uint8)
-        return self._lib.fcfd_set_refined_surface_reference(self._h, ptr(clean), clean.size)
+        cp, cn, _keep = _flags_arg(clean)
+        return self._lib.fcfd_set_refined_surface_reference(self._h, cp, cn)
 
     def wall_model_readout(self) -> capi.WMReadout:
         r = capi.WMReadout()
@@ -294,10 +306,10 @@ class LBMSolver:
 
     # ---- refinement ------------------------------------------------------
     def init_refinement(self, box: Box, factor: int, fine_flags) -> None:
-        ff = np.ascontiguousarray(fine_flags, np.uint8)
+        fp, fn, _keep = _flags_arg(fine_flags)
         err = C.create_string_buffer(512)
         b = box.as_c()
-        rc = self._lib.fcfd_init_refinement(self._h, C.byref(b), factor, ptr(ff), ff.size, err, 512)
+        rc = self._lib.fcfd_init_refinement(self._h, C.byref(b), factor, fp, fn, err, 512)
         if rc != 0:
             raise SolverError(err.value.decode() or f"initRefinement failed ({rc})")
 
@@ -320,10 +332,10 @@ class LBMSolver:
     # ---- nested finer level ----------------------------------------------
     def init_finer_refinement(self, box: Box, factor: int, finer_flags) -> None:
         """A patch inside the fine level (box in fine cells)."""
-        ff = np.ascontiguousarray(finer_flags, np.uint8)
+        fp, fn, _keep = _flags_arg(finer_flags)
         err = C.create_string_buffer(512)
         b = box.as_c()
-        rc = self._lib.fcfd_init_finer_refinement(self._h, C.byref(b), factor, ptr(ff), ff.size, err, 512)
+        rc = self._lib.fcfd_init_finer_refinement(self._h, C.byref(b), factor, fp, fn, err, 512)
         if rc != 0:
             raise SolverError(err.value.decode() or f"initFinerRefinement failed ({rc})")
 
@@ -331,8 +343,8 @@ class LBMSolver:
         self._lib.fcfd_shutdown_finer_refinement(self._h)
 
     def set_refined_finer_flags(self, finer_flags):
-        ff = np.ascontiguousarray(finer_flags, np.uint8)
-        return self._lib.fcfd_set_refined_finer_flags(self._h, ptr(ff), ff.size)
+        fp, fn, _keep = _flags_arg(finer_flags)
+        return self._lib.fcfd_set_refined_finer_flags(self._h, fp, fn)
 
     def finer_refinement_info(self) -> capi.FinerInfo:
         r = capi.FinerInfo()
@@ -360,8 +372,8 @@ class LBMSolver:
         self._lib.fcfd_shutdown_refinement(self._h)
 
     def set_refined_flags(self, fine_flags):
-        ff = np.ascontiguousarray(fine_flags, np.uint8)
-        return self._lib.fcfd_set_refined_flags(self._h, ptr(ff), ff.size)
+        fp, fn, _keep = _flags_arg(fine_flags)
+        return self._lib.fcfd_set_refined_flags(self._h, fp, fn)
 
     def refinement_info(self) -> capi.RefineInfo:
         r = capi.RefineInfo()
@@ -468,11 +480,39 @@ def naca4(digits: str, points_per_surface: int = 200) -> np.ndarray:
     return xy[: 2 * n].reshape(n, 2).copy()
 
 
-def voxelize_airfoil(dims, flags, xy, aoa_deg, chord_cells, anchor_x, anchor_y) -> int:
+def voxelize_airfoil(dims, flags, xy, aoa_deg, chord_cells, anchor_x, anchor_y, close_gaps: bool = True) -> int:
+    """voxelizeAirfoil into `flags` (in place), then, by default, the
+    trailing-edge gap closure; returns the cells closed."""
     xy = np.ascontiguousarray(xy, np.float32)
     d = capi.Dims(*dims)
-    return capi.load().fcfd_voxelize_airfoil(C.byref(d), ptr(xy), xy.shape[0], aoa_deg, chord_cells, anchor_x,
-                                             anchor_y, ptr(flags), flags.size)
+    lib = capi.load()
+    if lib.fcfd_voxelize_airfoil(C.byref(d), ptr(xy), xy.shape[0], aoa_deg, chord_cells, anchor_x, anchor_y,
+                                 ptr(flags), flags.size) != 0:
+        raise SolverError("bad voxelizer arguments")
+    return close_trailing_edge_gaps(dims, flags) if close_gaps else 0
+
+
+def layout_anchor(dims, frac=(0.3, 0.5)):
+    """DomainLayout::anchorX/anchorY (src/geom/voxelizer.h:71-83): the
+    quarter-chord anchor as FP32 fractions of nx, ny, in FP32 arithmetic."""
+    return (float(np.float32(frac[0]) * np.float32(dims[0])), float(np.float32(frac[1]) * np.float32(dims[1])))
+
+
+def fine_anchor(anchor, box, factor):
+    """makeFineLayout (voxelizer.cpp:203-223): the coarse anchor moved to the
+    patch origin and scaled by the factor, in FP32 arithmetic."""
+    f = np.float32(factor)
+    return (float(f * (np.float32(anchor[0]) - np.float32(box.x0))),
+            float(f * (np.float32(anchor[1]) - np.float32(box.y0))))
+
+
+def close_trailing_edge_gaps(dims, flags) -> int:
+    """closeTrailingEdgeGaps in place; returns the cells closed."""
+    d = capi.Dims(*dims)
+    n = capi.load().fcfd_close_trailing_edge_gaps(C.byref(d), ptr(flags), flags.size)
+    if n < 0:
+        raise SolverError("bad flag field")
+    return n
 
 
 def stamp_interface_shell(dims, flags):

@@ -18,7 +18,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .solver import (Box, boundary_flags, derive_patch_box, naca4, stamp_interface_shell, voxelize_airfoil)
+from .solver import (Box, boundary_flags, derive_patch_box, fine_anchor, layout_anchor, naca4, stamp_interface_shell,
+                     voxelize_airfoil)
 
 
 @dataclass
@@ -76,27 +77,30 @@ def square_cylinder(nx=384, ny=128, nz=64, side=24, cx=96, u_lat=0.08, outlet_eq
     return Tunnel("square_cylinder", dims, f.ravel().copy(), side, u_lat)
 
 
+def widen_box(box: Box, nx: int) -> Box:
+    """Widen a patch box to a multiple of 4 coarse cells so fine rows are
+    16-byte multiples in both storage precisions (bulk-copy staging)."""
+    extra = (-(box.x1 - box.x0)) % 4
+    grow_right = min(extra, nx - 3 - box.x1)
+    return Box(box.x0 - (extra - grow_right), box.y0, box.x1 + grow_right, box.y1)
+
+
 def airfoil_tunnel(nx=640, ny=192, nz=192, chord=256, aoa=6.0, digits="0012", margin_chord=0.1, factor=2,
                    u_lat=0.08, patch=True, anchor=(0.3, 0.5)):
     dims = (nx, ny, nz)
     flags = boundary_flags(dims)
     xy = naca4(digits, 200)
-    ax, ay = anchor[0] * nx, anchor[1] * ny
+    ax, ay = layout_anchor(dims, anchor)
     voxelize_airfoil(dims, flags, xy, aoa, chord, ax, ay)
     t = Tunnel(f"naca{digits}_{aoa:g}deg_{nx}x{ny}x{nz}", dims, flags, chord, u_lat, factor=factor)
     t.extra = dict(xy=xy, anchor=(ax, ay), aoa=aoa)
     if patch:
         m = int(round(margin_chord * chord))
-        box = derive_patch_box(dims, flags, m, m, m, m, 3)
-        # Widen the box to a multiple of 4 coarse cells so fine rows are
-        # 16-byte multiples in both storage precisions (bulk-copy staging).
-        extra = (-(box.x1 - box.x0)) % 4
-        grow_right = min(extra, nx - 3 - box.x1)
-        box = Box(box.x0 - (extra - grow_right), box.y0, box.x1 + grow_right, box.y1)
+        box = widen_box(derive_patch_box(dims, flags, m, m, m, m, 3), nx)
         t.box = box
         fd = t.fine_dims
         ff = np.zeros(int(np.prod(fd)), np.uint8)
-        voxelize_airfoil(fd, ff, xy, aoa, factor * chord, factor * (ax - box.x0), factor * (ay - box.y0))
+        voxelize_airfoil(fd, ff, xy, aoa, factor * chord, *fine_anchor((ax, ay), box, factor))
         stamp_interface_shell(fd, ff)
         t.fine_flags = ff
     return t

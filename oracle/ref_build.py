@@ -34,7 +34,8 @@ FLAGS = ["-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fas
 
 
 def available() -> bool:
-    return all((SIM / src).exists() for src, _ in UNITS.values()) and (SIM / "wall_model.cpp").exists()
+    return (all((SIM / src).exists() for src, _ in UNITS.values()) and (SIM / "wall_model.cpp").exists()
+            and (REFERENCE / "src" / "geom" / "voxelizer.cpp").exists())
 
 
 def _kernel_section(path: Path) -> str:
@@ -79,6 +80,19 @@ def build(force: bool = False) -> dict:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference wall_model.cpp build failed:\n{r.stderr[-4000:]}")
+    # The host geometry builders (NACA outline, voxeliser, patch flags) are
+    # plain C++ too; vg.cpp and platform.cpp only resolve their symbols.
+    so = OUT / "libref_geom.so"
+    libs["geom"] = so
+    if force or not so.exists():
+        geom = REFERENCE / "src" / "geom"
+        cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+               str(geom / "voxelizer.cpp"), str(geom / "airfoil.cpp"), str(geom / "vg.cpp"),
+               str(REFERENCE / "src" / "platform" / "platform.cpp"), str(HERE / "ref_geom_driver.cpp"),
+               "-I", str(geom), "-I", str(SIM), "-I", _cuda_include(), "-o", str(so)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference geometry build failed:\n{r.stderr[-4000:]}")
     return libs
 
 

@@ -25,6 +25,17 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def mg():
+    """The golden-vector generator's case definitions (geometries, layouts);
+    importing it needs no reference tree."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="session")
 def oracle_mod():
     from oracle import oracle
     oracle.build()

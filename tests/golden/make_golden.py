@@ -52,6 +52,17 @@ def load():
     return core, wall, refine, wl
 
 
+def load_geom():
+    geom = C.CDLL(str(ref_build.build()["geom"]))
+    geom.ref_naca4.argtypes = [C.c_char_p, I, P, I]
+    geom.ref_clean_foil_flags.argtypes = [C.c_char_p, I, F, I, I, I, I, F, F, P]
+    geom.ref_fine_patch_flags.argtypes = [C.c_char_p, I, F, I, I, I, I, F, F, I, I, I, I, I, P]
+    geom.ref_derive_patch_box.argtypes = [I, I, I, P, I, I, I, I, I, P]
+    geom.ref_voxelize_points.argtypes = [P, I, F, I, I, I, I, F, F, P]
+    geom.ref_close_te.argtypes = [I, I, I, P]
+    return geom
+
+
 def open_flags(nx, ny, nz):
     """Inlet x=0, outlet x=nx-1, slip y faces (tests/lbm_test_util.h:34-54)."""
     fl = np.zeros((nz, ny, nx), np.uint8)
@@ -358,6 +369,62 @@ def case_edits(core):
                         fB=fB, outA=outA, outB=outB)
 
 
+FOIL_CASES = [((160, 64, 4), 64, 6.0, "0012"), ((200, 96, 3), 80, -5.0, "2412"), ((301, 111, 2), 97, 12.3, "4415")]
+PATCH_CASES = [(0, (6, 9, 5, 7, 3), 2), (1, (4, 4, 4, 4, 3), 3)]
+
+
+def wedge_outline(n=24):
+    """A thin closed wedge (chord 1, 2 % thick at the nose, zero at the tail)
+    whose voxelised tail leaves single-cell gaps."""
+    x = np.linspace(0.0, 1.0, n // 2, dtype=np.float32)
+    t = 0.01 * (1.0 - x)
+    up = np.stack([x[::-1], t[::-1]], 1)
+    lo = np.stack([x[1:], -t[1:]], 1)
+    return np.ascontiguousarray(np.concatenate([up, lo]), np.float32)
+
+
+def case_geometry(geom):
+    """Host geometry builders (src/geom/voxelizer.cpp, airfoil.cpp): NACA
+    outlines, clean-foil flags, patch boxes and fine-patch flags, an
+    arbitrary outline into an existing field, and the trailing-edge closure."""
+    rng = np.random.default_rng(20261206)
+    out = {}
+    for digits in ("0012", "2412", "4415", "6409"):
+        for pps in (200, 50):
+            xy = np.zeros(2 * 2 * pps, np.float32)
+            n = geom.ref_naca4(digits.encode(), pps, p(xy), 2 * pps)
+            out[f"naca_{digits}_{pps}"] = xy[: 2 * n].reshape(n, 2).copy()
+    for i, (dims, chord, aoa, digits) in enumerate(FOIL_CASES):
+        f = np.zeros(int(np.prod(dims)), np.uint8)
+        closed = geom.ref_clean_foil_flags(digits.encode(), 200, aoa, *dims, chord, 0.3, 0.5, p(f))
+        out[f"foil{i}"] = f
+        out[f"foil{i}_closed"] = np.array(closed)
+    for k, (i, margins, factor) in enumerate(PATCH_CASES):
+        dims, chord, aoa, digits = FOIL_CASES[i]
+        box = np.zeros(4, np.int32)
+        geom.ref_derive_patch_box(*dims, p(out[f"foil{i}"]), *margins, p(box))
+        fd = (factor * int(box[2] - box[0]), factor * int(box[3] - box[1]), factor * dims[2])
+        ff = np.zeros(int(np.prod(fd)), np.uint8)
+        geom.ref_fine_patch_flags(digits.encode(), 200, aoa, *dims, chord, 0.3, 0.5, *[int(v) for v in box], factor,
+                                  p(ff))
+        out[f"patch{k}_box"] = box
+        out[f"patch{k}"] = ff
+    # Arbitrary outline over a field that already holds other flags; the
+    # wedge is placed to run off the top face.
+    dims = (90, 40, 3)
+    base = rng.choice(np.array([0, 0, 0, 0, 0, 0, 1, 2, 3, 4, 5], np.uint8), size=int(np.prod(dims)))
+    xy = wedge_outline()
+    vox = base.copy()
+    geom.ref_voxelize_points(p(xy), xy.shape[0], 20.0, *dims, 70, 30.0, 30.0, p(vox))
+    out.update(wedge_xy=xy, wedge_base=base, wedge_vox=vox)
+    te_dims = (40, 30, 3)
+    te_in = rng.choice(np.array([0, 1, 1, 2], np.uint8), size=int(np.prod(te_dims)))
+    te_out = te_in.copy()
+    out["te_closed"] = np.array(geom.ref_close_te(*te_dims, p(te_out)))
+    out.update(te_in=te_in, te_out=te_out)
+    np.savez_compressed(OUT / "geometry.npz", **out)
+
+
 def main(cases=None):
     """All cases, or the named ones (e.g. `qlibb`) to leave the others'
     fixtures untouched."""
@@ -368,6 +435,8 @@ def main(cases=None):
                 case_qlibb(core)
             elif c == "edits":
                 case_edits(core)
+            elif c == "geometry":
+                case_geometry(load_geom())
             else:
                 raise SystemExit(f"unknown case {c}")
         return
@@ -380,6 +449,7 @@ def main(cases=None):
     case_refine(core, refine, rng)
     case_qlibb(core)
     case_edits(core)
+    case_geometry(load_geom())
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -137,6 +137,59 @@ def test_voxelize_airfoil_area(fc):
     assert ys[xs.argmax()] < 40 < ys[xs.argmin()] + 1
 
 
+@pytest.mark.parametrize("digits", ["0012", "2412", "4415", "6409"])
+@pytest.mark.parametrize("pps", [200, 50])
+def test_naca4_matches_reference(fc, golden, digits, pps):
+    """generateNACA4 (src/geom/airfoil.cpp:177-266): every outline point."""
+    assert np.array_equal(fc.naca4(digits, pps), golden("geometry")[f"naca_{digits}_{pps}"])
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_clean_foil_flags_match_reference(fc, golden, mg, case):
+    """buildCleanFoilFlags: boundary flags, voxelised foil, closure."""
+    from foil_cfd_gb300.solver import layout_anchor
+    g = golden("geometry")
+    dims, chord, aoa, digits = mg.FOIL_CASES[case]
+    f = fc.boundary_flags(dims)
+    closed = fc.voxelize_airfoil(dims, f, fc.naca4(digits, 200), aoa, chord, *layout_anchor(dims))
+    assert closed == int(g[f"foil{case}_closed"])
+    assert np.array_equal(f, g[f"foil{case}"])
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_patch_box_and_fine_flags_match_reference(fc, golden, mg, k):
+    """derivePatchBox + buildFinePatchFlags (makeFineLayout anchor)."""
+    from foil_cfd_gb300.solver import fine_anchor, layout_anchor
+    g = golden("geometry")
+    i, margins, factor = mg.PATCH_CASES[k]
+    dims, chord, aoa, digits = mg.FOIL_CASES[i]
+    box = fc.derive_patch_box(dims, g[f"foil{i}"], *margins)
+    assert [box.x0, box.y0, box.x1, box.y1] == list(g[f"patch{k}_box"])
+    fd = (factor * (box.x1 - box.x0), factor * (box.y1 - box.y0), factor * dims[2])
+    ff = np.zeros(int(np.prod(fd)), np.uint8)
+    fc.voxelize_airfoil(fd, ff, fc.naca4(digits, 200), aoa, factor * chord,
+                        *fine_anchor(layout_anchor(dims), box, factor))
+    fc.stamp_interface_shell(fd, ff)
+    assert np.array_equal(ff, g[f"patch{k}"])
+
+
+def test_voxelize_outline_and_closure_match_reference(fc, golden):
+    """voxelizeAirfoil of an arbitrary outline over a field holding other
+    flags (only fluid becomes solid, faces untouched), and
+    closeTrailingEdgeGaps on a random field (closures do not cascade)."""
+    g = golden("geometry")
+    f = g["wedge_base"].copy()
+    assert fc.voxelize_airfoil((90, 40, 3), f, g["wedge_xy"], 20.0, 70, 30.0, 30.0, close_gaps=False) == 0
+    assert np.array_equal(f, g["wedge_vox"])
+    t = g["te_in"].copy()
+    assert fc.close_trailing_edge_gaps((40, 30, 3), t) == int(g["te_closed"])
+    assert np.array_equal(t, g["te_out"])
+    # An outline under 20 points is not a section: nothing is stamped.
+    f2 = g["wedge_base"].copy()
+    fc.voxelize_airfoil((90, 40, 3), f2, g["wedge_xy"][:19], 20.0, 70, 30.0, 30.0, close_gaps=False)
+    assert np.array_equal(f2, g["wedge_base"])
+
+
 def test_interface_shell_and_patch_box(fc):
     d = (20, 12, 2)
     f = np.zeros(int(np.prod(d)), np.uint8)
