@@ -1,7 +1,8 @@
 """ctypes binding of include/foilcfd_step.h (the solver step's C ABI),
 include/foilcfd_wallnet.h (the learned u_tau seed),
-include/foilcfd_batch.h (the batched multi-tunnel step) and
-include/foilcfd_geom.h (the on-device geometry builders).
+include/foilcfd_batch.h (the batched multi-tunnel step),
+include/foilcfd_geom.h (the on-device geometry builders) and
+include/foilcfd_snapshot.h (warm-start snapshots and the disk cache).
 
 Loading fails loudly when the compiled library is missing: there is no CPU
 fallback for the solver step. Build it with ``foil_cfd_gb300.build_lib``
@@ -33,6 +34,12 @@ class Options(C.Structure):
 
 class PatchBox(C.Structure):
     _fields_ = [("x0", C.c_int), ("y0", C.c_int), ("x1", C.c_int), ("y1", C.c_int)]
+
+
+class SnapshotKey(C.Structure):
+    """fcfd_snapshot_key (foilcfd_snapshot.h)."""
+    _fields_ = [("geometry_id", C.c_char_p), ("aoa_bucket", C.c_int), ("u_lat", C.c_float), ("dims", Dims),
+                ("solver_version", C.c_int)]
 
 
 class Foil(C.Structure):
@@ -154,6 +161,39 @@ _SIGS = {
     "fcfd_build_wall_list": (C.c_longlong, [C.POINTER(Dims), P, P, C.c_int, P, P, P, P, P, P, P, C.c_longlong, P]),
     "fcfd_boundary_flags": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
     "fcfd_naca4": (C.c_int, [C.c_char_p, C.c_int, P, C.c_int]),
+    # include/foilcfd_snapshot.h
+    "fcfd_aoa_bucket": (C.c_int, [C.c_float]),
+    "fcfd_snapshot_key_hash": (C.c_uint64, [C.POINTER(SnapshotKey)]),
+    "fcfd_snapshot_key_string": (C.c_int, [C.POINTER(SnapshotKey), C.c_char_p, C.c_size_t]),
+    "fcfd_hash_flags": (C.c_uint64, [P, C.c_size_t]),
+    "fcfd_vram_snapshot_create": (P, []),
+    "fcfd_vram_snapshot_destroy": (None, [P]),
+    "fcfd_vram_snapshot_capture": (C.c_int, [P, P, C.POINTER(SnapshotKey), C.c_char_p, C.c_size_t]),
+    "fcfd_vram_snapshot_restore": (C.c_int, [P, P]),
+    "fcfd_vram_snapshot_has_data": (C.c_int, [P]),
+    "fcfd_vram_snapshot_flags_hash": (C.c_uint64, [P]),
+    "fcfd_vram_snapshot_bytes": (C.c_size_t, [P]),
+    "fcfd_vram_snapshot_key": (C.c_int, [P, C.POINTER(SnapshotKey)]),
+    "fcfd_vram_snapshot_release": (None, [P]),
+    "fcfd_compact_snapshot_create": (P, []),
+    "fcfd_compact_snapshot_destroy": (None, [P]),
+    "fcfd_compact_snapshot_capture": (C.c_int, [P, P, C.POINTER(SnapshotKey), C.c_char_p, C.c_size_t]),
+    "fcfd_compact_snapshot_restore": (C.c_int, [P, P]),
+    "fcfd_compact_snapshot_save": (C.c_int, [P, C.c_char_p, C.c_char_p, C.c_size_t]),
+    "fcfd_compact_snapshot_load": (C.c_int, [P, C.c_char_p, C.c_char_p, C.c_size_t]),
+    "fcfd_compact_snapshot_has_data": (C.c_int, [P]),
+    "fcfd_compact_snapshot_flags_hash": (C.c_uint64, [P]),
+    "fcfd_compact_snapshot_key": (C.c_int, [P, C.POINTER(SnapshotKey)]),
+    "fcfd_compact_snapshot_scaling": (C.c_int, [P, C.POINTER(Scaling)]),
+    "fcfd_compact_snapshot_fields": (C.c_int, [P, P, P, P, P, P]),
+    "fcfd_disk_cache_open": (P, [C.c_char_p, C.c_uint64]),
+    "fcfd_disk_cache_close": (None, [P]),
+    "fcfd_disk_cache_find": (C.c_int, [P, C.POINTER(SnapshotKey), C.c_char_p, C.c_size_t]),
+    "fcfd_disk_cache_store": (C.c_int, [P, P, C.c_char_p, C.c_size_t]),
+    "fcfd_disk_cache_store_async": (C.c_int, [P, P]),
+    "fcfd_disk_cache_wait": (None, [P]),
+    "fcfd_disk_cache_set_budget": (None, [P, C.c_uint64]),
+    "fcfd_disk_cache_used_bytes": (C.c_uint64, [P]),
     "fcfd_close_trailing_edge_gaps": (C.c_int, [C.POINTER(Dims), P, C.c_size_t]),
     "fcfd_device_build_flags": (C.c_int, [C.POINTER(Dims), C.c_int, P, P, C.c_int, C.c_int, P, P, P]),
     "fcfd_device_derive_patch_box": (C.c_int, [C.POINTER(Dims), P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P,

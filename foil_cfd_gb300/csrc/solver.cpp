@@ -11,6 +11,7 @@
 #include "../../include/foilcfd_wallnet.h"
 #include "host_geom.h"
 #include "kernels.h"
+#include "snapshot_internal.h"
 
 #include <cuda_runtime.h>
 
@@ -1757,4 +1758,35 @@ int fcfd_import_finer_f32(fcfd_solver* s, const float* f, size_t count) {
 int fcfd_export_finer_f32(fcfd_solver* s, float* f, size_t count) {
     if (!s || !s->initialized || !s->finerActive || !f) return cudaErrorInvalidValue;
     return s->exportF32(s->finer, f, count);
+}
+
+int fcfd::solver_field_view(fcfd_solver* s, SolverFieldView* v) {
+    if (!s || !s->initialized || !v) return cudaErrorNotReady;
+    *v = SolverFieldView{};
+    const size_t pop = s->storage == Storage::F32 ? 4 : 2;
+    const Level* levels[3] = {&s->coarse, s->fineActive ? &s->fine : nullptr,
+                                           s->finerActive ? &s->finer : nullptr};
+    for (const auto* L : levels) {
+        if (!L) break;
+        const int l = v->levels;
+        v->f[l] = L->f[L->src];
+        v->bytes[l] = static_cast<size_t>(L->n) * 19 * pop;
+        v->dims[l] = L->d;
+        if (L->wm.active) {
+            v->wm[l][0] = L->wm.dUTau;
+            v->wmBytes[l][0] = static_cast<size_t>(L->wm.count) * 4;
+            void* slip[3] = {L->wm.dUwx, L->wm.dUwy, L->wm.dUwz};
+            for (int k = 0; k < 3; ++k) {
+                v->wm[l][k + 1] = slip[k];
+                v->wmBytes[l][k + 1] = static_cast<size_t>(L->n) * 2;
+            }
+        }
+        ++v->levels;
+    }
+    v->storage = s->storage == Storage::F32 ? FCFD_STORE_FP32 : FCFD_STORE_FP16;
+    v->stream = s->stream;
+    v->flags = s->coarse.hostFlags.data();
+    v->nFlags = s->coarse.hostFlags.size();
+    v->scaling = s->scaling;
+    return 0;
 }

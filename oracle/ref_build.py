@@ -35,7 +35,7 @@ FLAGS = ["-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fas
 
 def available() -> bool:
     return (all((SIM / src).exists() for src, _ in UNITS.values()) and (SIM / "wall_model.cpp").exists()
-            and (REFERENCE / "src" / "geom" / "voxelizer.cpp").exists())
+            and (REFERENCE / "src" / "geom" / "voxelizer.cpp").exists() and (SIM / "snapshot.cpp").exists())
 
 
 def _kernel_section(path: Path) -> str:
@@ -93,6 +93,20 @@ def build(force: bool = False) -> dict:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference geometry build failed:\n{r.stderr[-4000:]}")
+    # The snapshot code (keys, flag hash, FCS1 reader/writer); the solver
+    # methods it names are stubbed by the driver.
+    so = OUT / "libref_snapshot.so"
+    libs["snapshot"] = so
+    if force or not so.exists():
+        cuda = Path(_cuda_include()).parent
+        lib64 = next((str(p) for p in (cuda / "lib64", cuda / "lib") if p.exists()), str(cuda / "lib64"))
+        cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-w", "-pthread",
+               str(SIM / "snapshot.cpp"), str(REFERENCE / "src" / "platform" / "platform.cpp"),
+               str(HERE / "ref_snapshot_driver.cpp"), "-I", str(SIM), "-I", _cuda_include(),
+               "-L", lib64, "-lcudart", "-Wl,-rpath," + lib64, "-o", str(so)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference snapshot build failed:\n{r.stderr[-4000:]}")
     return libs
 
 

@@ -41,6 +41,7 @@ def load():
     core.ref_apply_flag_edits.argtypes = [I, I, I, P, P, P, P]
     core.ref_force.argtypes = [I, I, I, P, P, P, P, P, P]
     core.ref_init.argtypes = [I, I, I, P, P, F, F, C.c_uint, I]
+    core.ref_init_from_macro.argtypes = [I, I, I, P, P, P, P, P, P]
     wall = C.CDLL(str(libs["wall"]))
     wall.ref_wall_update.argtypes = [I, I, I, P, I, P, P, P, P, P, P, P, P, P, P, P, F, F, F, P]
     refine = C.CDLL(str(libs["refine"]))
@@ -50,6 +51,111 @@ def load():
     wl.ref_build_wall_list.argtypes = [I, I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P]
     wl.ref_build_wall_list.restype = C.c_longlong
     return core, wall, refine, wl
+
+
+def load_snapshot():
+    snap = C.CDLL(str(ref_build.build()["snapshot"]))
+    snap.ref_key_hash.argtypes = [C.c_char_p, I, F, I, I, I, I]
+    snap.ref_key_hash.restype = C.c_ulonglong
+    snap.ref_key_string.argtypes = [C.c_char_p, I, F, I, I, I, I, C.c_char_p, I]
+    snap.ref_bucket.argtypes = [F]
+    snap.ref_hash_flags.argtypes = [P, C.c_ulonglong]
+    snap.ref_hash_flags.restype = C.c_ulonglong
+    snap.ref_fcs_roundtrip.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, I]
+    return snap
+
+
+SNAPSHOT_KEYS = [("naca:2412", 12, 0.08, (768, 320, 96), 1), ("naca:0012", -10, 0.05, (64, 32, 8), 1),
+                 ("dat:e387.dat", 31, 0.1, (256, 128, 4), 1), ("stl:00ff12ab34cd56ef", 0, 0.0125, (48, 40, 40), 1),
+                 ("", 1, 0.08, (1, 1, 1), 2)]
+SNAPSHOT_AOA = [0.0, 0.24, 0.25, 0.26, -0.25, -0.75, 6.0, 12.3, 25.0, -5.1]
+SNAPSHOT_SCALING = dict(chord_m=1.2, airspeed_ms=30.0, nu_m2s=1.48e-5, chord_cells=64, u_lat=0.08, dx=0.01875,
+                        dt=5.0e-5, nu_lat_target=1.97e-6, nu_lat=1.5e-4, tau=0.50045, tau_clamped=1,
+                        re_target=2.43e6, re_effective=34133.3)
+
+
+def fcs_bytes(key, flags_hash, scaling, fields):
+    """An FCS1 file assembled field by field from the published layout
+    (little-endian; magic, format 1, key, flags hash, scaling echo, raw
+    payload tag, cell count, rho/u/v/w)."""
+    import struct
+    gid, bucket, u, dims, ver = key
+    b = struct.pack("<III", 0x31534346, 1, len(gid.encode())) + gid.encode()
+    b += struct.pack("<ifiiii", bucket, u, *dims, ver) + struct.pack("<Q", flags_hash)
+    sc = scaling
+    b += struct.pack("<fffiffffffBff", sc["chord_m"], sc["airspeed_ms"], sc["nu_m2s"], sc["chord_cells"],
+                     sc["u_lat"], sc["dx"], sc["dt"], sc["nu_lat_target"], sc["nu_lat"], sc["tau"],
+                     sc["tau_clamped"], sc["re_target"], sc["re_effective"])
+    n = int(np.prod(dims))
+    b += struct.pack("<IQ", 0, n)
+    for a in fields:
+        b += np.ascontiguousarray(a, "<f4").tobytes()
+    return b
+
+
+def case_macro_init(core):
+    """Compact-snapshot restore: f = feq(rho, u) of stored macroscopic
+    fields (initFromMacroKernel), rest state on solid cells."""
+    rng = np.random.default_rng(20261208)
+    dims = (16, 12, 4)
+    n = int(np.prod(dims))
+    fl = open_flags(*dims)
+    fl[:, 4:7, 5:8] = 1
+    flags = fl.ravel().copy()
+    rho = (1 + 0.02 * rng.standard_normal(n)).astype(np.float32)
+    u = (0.05 + 0.02 * rng.standard_normal(n)).astype(np.float32)
+    v = (0.02 * rng.standard_normal(n)).astype(np.float32)
+    w = (0.02 * rng.standard_normal(n)).astype(np.float32)
+    f = np.zeros(19 * n, np.float32)
+    core.ref_init_from_macro(*dims, p(f), p(flags), p(rho), p(u), p(v), p(w))
+    np.savez_compressed(OUT / "macro_init.npz", dims=np.array(dims), flags=flags, rho=rho, u=u, v=v, w=w, f=f)
+
+
+def case_snapshot(snap):
+    """Snapshot keys (hash, name), AoA buckets, the flag hash, and an FCS1
+    file read and written back by the reference's CompactSnapshot."""
+    import tempfile
+    rng = np.random.default_rng(20261207)
+    out = {}
+    hashes, names = [], []
+    for gid, bucket, u, dims, ver in SNAPSHOT_KEYS:
+        hashes.append(snap.ref_key_hash(gid.encode(), bucket, u, *dims, ver))
+        buf = C.create_string_buffer(512)
+        snap.ref_key_string(gid.encode(), bucket, u, *dims, ver, buf, 512)
+        names.append(buf.value.decode())
+    out["key_hash"] = np.array(hashes, np.uint64)
+    out["key_name"] = np.array(names)
+    out["aoa"] = np.array(SNAPSHOT_AOA, np.float32)
+    out["aoa_bucket"] = np.array([snap.ref_bucket(float(a)) for a in np.array(SNAPSHOT_AOA, np.float32)], np.int32)
+    flags = rng.integers(0, 10, 3000).astype(np.uint8)
+    out["flags"] = flags
+    out["flags_hash"] = np.array(snap.ref_hash_flags(p(flags), flags.size), np.uint64)
+    dims = (12, 7, 5)
+    n = int(np.prod(dims))
+    fields = [rng.standard_normal(n).astype(np.float32) for _ in range(4)]
+    key = ("naca:4412", 13, 0.08, dims, 1)
+    raw = fcs_bytes(key, 0x0123456789ABCDEF, SNAPSHOT_SCALING, fields)
+    with tempfile.TemporaryDirectory() as d:
+        src, dst = Path(d) / "in.fcs", Path(d) / "out.fcs"
+        src.write_bytes(raw)
+        err = C.create_string_buffer(512)
+        if snap.ref_fcs_roundtrip(str(src).encode(), str(dst).encode(), err, 512):
+            raise SystemExit(f"reference rejected the FCS1 file: {err.value.decode()}")
+        out["fcs"] = np.frombuffer(dst.read_bytes(), np.uint8).copy()
+        # Rejections: the reference's reason for each corrupted variant.
+        bad = {"magic": b"XCS1" + raw[4:], "format": raw[:4] + b"\x02" + raw[5:],
+               "truncated": raw[: len(raw) - 7], "version": None}
+        kv = fcs_bytes(("naca:4412", 13, 0.08, dims, 2), 0x0123456789ABCDEF, SNAPSHOT_SCALING, fields)
+        bad["version"] = kv
+        reasons = []
+        for name in ("magic", "format", "truncated", "version"):
+            src.write_bytes(bad[name])
+            rc = snap.ref_fcs_roundtrip(str(src).encode(), None, err, 512)
+            reasons.append(err.value.decode().split(":")[0] if rc else "")
+        out["reject_reason"] = np.array(reasons)
+    out["fcs_fields"] = np.stack(fields)
+    out["fcs_dims"] = np.array(dims)
+    np.savez_compressed(OUT / "snapshot.npz", **out)
 
 
 def load_geom():
@@ -437,6 +543,10 @@ def main(cases=None):
                 case_edits(core)
             elif c == "geometry":
                 case_geometry(load_geom())
+            elif c == "snapshot":
+                case_snapshot(load_snapshot())
+            elif c == "macro_init":
+                case_macro_init(core)
             else:
                 raise SystemExit(f"unknown case {c}")
         return
@@ -450,6 +560,8 @@ def main(cases=None):
     case_qlibb(core)
     case_edits(core)
     case_geometry(load_geom())
+    case_snapshot(load_snapshot())
+    case_macro_init(core)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 
