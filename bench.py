@@ -619,6 +619,52 @@ def geometry_leg(t, reps=3):
             "identical": same}
 
 
+def snapshot_leg(sol, t, reps=3):
+    """Warm-start snapshots of the timed solver: the exact VRAM snapshot
+    (device copies of both levels' populations and wall-model state) and the
+    compact FCS1 snapshot (macroscopic download, file write and read,
+    equilibrium re-init)."""
+    import tempfile
+    from foil_cfd_gb300 import snapshot as sn
+    key = sn.SnapshotKey("naca:0012", sn.aoa_bucket(t.extra.get("aoa", 0.0)), t.u_lat, t.dims)
+    v = sn.VramSnapshot()
+    cap, res = [], []
+    for _ in range(reps):
+        sol.synchronize()
+        a = time.perf_counter()
+        v.capture(sol, key)
+        sol.synchronize()
+        b = time.perf_counter()
+        assert v.restore(sol)
+        sol.synchronize()
+        cap.append(b - a)
+        res.append(time.perf_counter() - b)
+    nb = v.nbytes
+    v.close()
+    out = {"vram_bytes": nb, "vram_capture_ms": round(min(cap) * 1e3, 2), "vram_restore_ms": round(min(res) * 1e3, 2),
+           "vram_copy_gbs": round(2 * nb / min(min(cap), min(res)) / 1e9, 1)}
+    c = sn.CompactSnapshot()
+    with tempfile.TemporaryDirectory() as d:
+        path = Path(d) / f"{key.hash():016x}.fcs"
+        a = time.perf_counter()
+        c.capture(sol, key)
+        b = time.perf_counter()
+        c.save(path)
+        e = time.perf_counter()
+        back = sn.CompactSnapshot()
+        back.load(path)
+        f = time.perf_counter()
+        ok = back.restore(sol)
+        sol.synchronize()
+        g = time.perf_counter()
+        out.update({"fcs_bytes": path.stat().st_size, "compact_capture_ms": round((b - a) * 1e3, 1),
+                    "fcs_save_ms": round((e - b) * 1e3, 1), "fcs_load_ms": round((f - e) * 1e3, 1),
+                    "compact_restore_ms": round((g - f) * 1e3, 1), "compact_restored": bool(ok)})
+        back.close()
+    c.close()
+    return out
+
+
 def cpu_host():
     try:
         model = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -760,6 +806,8 @@ def main():
             "gpu_launches": int(r32["launches"]), "clocks": r32["clocks"],
             "force_lattice": r32["force"], "nan": bool(r32["nan"])}
     line["e2e"] = e2e(t, r32, args.steps)
+    if ws == 1 and not args.no_geometry:
+        line["snapshot"] = snapshot_leg(r32["solver"], t)
     if not args.no_wallnet and ws == 1:
         r32["snapshot"].restore(r32["solver"])
         line["wall_seed"] = wall_seed_leg(r32["solver"], t)

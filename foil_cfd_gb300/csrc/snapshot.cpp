@@ -89,6 +89,8 @@ struct Key {
 
 // ---- keys and hashes -----------------------------------------------------------
 
+std::uint64_t fcfd::fnv1a64(const void* p, size_t n) { return fnv(p, n); }
+
 extern "C" int fcfd_aoa_bucket(float aoa_deg) { return static_cast<int>(std::lround(aoa_deg * 2.0f)); }
 
 extern "C" uint64_t fcfd_snapshot_key_hash(const fcfd_snapshot_key* key) { return Key::of(key).hash(); }
@@ -181,7 +183,7 @@ extern "C" int fcfd_vram_snapshot_capture(fcfd_vram_snapshot* v, fcfd_solver* s,
     v->levels = fv.levels;
     v->storage = fv.storage;
     v->key = Key::of(key);
-    v->flagsHash = fcfd_hash_flags(fv.flags, fv.nFlags);
+    v->flagsHash = fv.flagsHash;
     v->hasData = true;
     say(err, errlen, "");
     return 0;
@@ -371,7 +373,7 @@ extern "C" int fcfd_compact_snapshot_capture(fcfd_compact_snapshot* c, fcfd_solv
     }
     c->key = Key::of(key);
     c->scaling = fv.scaling;
-    c->flagsHash = fcfd_hash_flags(fv.flags, fv.nFlags);
+    c->flagsHash = fv.flagsHash;
     c->hasData = true;
     say(err, errlen, "");
     return 0;

@@ -26,12 +26,13 @@ struct SolverFieldView {
     size_t wmBytes[3][4] = {};
     int storage = FCFD_STORE_FP32;
     cudaStream_t stream = nullptr;
-    const std::uint8_t* flags = nullptr;  ///< host copy of the coarse flags
-    size_t nFlags = 0;
+    std::uint64_t flagsHash = 0;    ///< FNV-1a of the coarse flags (cached)
     fcfd_scaling scaling{};
 };
 
 /// 0, or cudaErrorNotReady when the solver is not initialised.
 int solver_field_view(fcfd_solver* s, SolverFieldView* v);
+/// FNV-1a 64 of a byte array (the snapshot flag hash).
+std::uint64_t fnv1a64(const void* p, size_t n);
 
 } // namespace fcfd

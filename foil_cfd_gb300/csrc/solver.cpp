@@ -207,6 +207,8 @@ struct fcfd_solver {
     fcfd_patch_box finerBox{};
     std::uint32_t *dShellFiner = nullptr, *dSeedFiner = nullptr;
     int shellCountFiner = 0, seedCountFiner = 0;
+    std::uint64_t flagsHashCache = 0;   // FNV-1a of coarse.hostFlags
+    bool flagsHashValid = false;
     float* dScratchFiner = nullptr;
     std::uint32_t* dShell = nullptr;
     int shellCount = 0;
@@ -329,6 +331,7 @@ struct fcfd_solver {
     /// host copy (edit diffs), the cell classes, the kind bytes and the
     /// force-link list, the last two built on the device.
     cudaError_t uploadLevelFlags(Level& L, const std::uint8_t* flags) {
+        if (&L == &coarse) flagsHashValid = false;
         L.hostFlags.resize(static_cast<size_t>(L.n));
         const size_t nb = static_cast<size_t>(L.n);
         if (on_device(flags)) {
@@ -1785,8 +1788,12 @@ int fcfd::solver_field_view(fcfd_solver* s, SolverFieldView* v) {
     }
     v->storage = s->storage == Storage::F32 ? FCFD_STORE_FP32 : FCFD_STORE_FP16;
     v->stream = s->stream;
-    v->flags = s->coarse.hostFlags.data();
-    v->nFlags = s->coarse.hostFlags.size();
+    // The flag hash is cached until the coarse flags change.
+    if (!s->flagsHashValid) {
+        s->flagsHashCache = fnv1a64(s->coarse.hostFlags.data(), s->coarse.hostFlags.size());
+        s->flagsHashValid = true;
+    }
+    v->flagsHash = s->flagsHashCache;
     v->scaling = s->scaling;
     return 0;
 }
