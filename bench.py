@@ -323,12 +323,24 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10, fixed=None):
     step (FP16 storage, graph-replayed chunks, autotuned shape) from a uniform
     start; against 24 sequential single-tunnel FP32 runs (the drop-in)."""
     import foil_cfd_gb300 as fc
+    import torch
     from foil_cfd_gb300 import batch
+    t0 = time.perf_counter()
     tunnels = batch.polar_tunnels()
+    host_build_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev_tunnels = batch.polar_tunnels(device=True)
+    torch.cuda.synchronize()
+    dev_build_s = time.perf_counter() - t0
+    same = all(np.array_equal(d.flags.cpu().numpy(), h.flags) for d, h in zip(dev_tunnels, tunnels))
+    del dev_tunnels
     upd = float(sum(t.cells for t in tunnels))
     out = {"tunnels": len(tunnels), "cells": int(upd), "steps": steps,
            "sections": "NACA 0012/2412/4412, -4..16 deg by 2.5 (first 24), chord 96-192 cells, 2.5 x 1.5 chords, "
-                       "span 16 periodic, Re 1000 on the chord, uniform-flow start"}
+                       "span 16 periodic, Re 1000 on the chord, uniform-flow start",
+           "geometry_build_ms": {"host": round(host_build_s * 1e3, 1), "device": round(dev_build_s * 1e3, 1),
+                                 "identical": same}}
     res = {}
     for storage in ("fp16", "fp32"):
         b = batch.BatchSolver()

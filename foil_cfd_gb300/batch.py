@@ -34,9 +34,14 @@ class PolarTunnel:
 
 
 def polar_tunnels(count: int = 24, seed: int = 0, span: int = 16, u_lat: float = 0.08, chord_range=(96, 192),
-                  cambers=(0, 2, 4), aoas=None, reynolds: float = 1000.0, outlet_eq: bool = True):
+                  cambers=(0, 2, 4), aoas=None, reynolds: float = 1000.0, outlet_eq: bool = True,
+                  device: bool = False):
     """The polar's tunnels in (camber, angle) order; chord cells seeded.
-    Reynolds number on the chord (tau = 1/2 + 3 u c / Re)."""
+    Reynolds number on the chord (tau = 1/2 + 3 u c / Re). With `device`
+    the flag fields are built by the device geometry kernels (uint8 CUDA
+    tensors, the same bytes) instead of the host builders."""
+    if device:
+        from . import geometry
     aoas = [-4.0 + 2.5 * k for k in range(9)] if aoas is None else list(aoas)
     pairs = [(m, a) for m in cambers for a in aoas][:count]
     rng = np.random.default_rng(seed)
@@ -46,10 +51,16 @@ def polar_tunnels(count: int = 24, seed: int = 0, span: int = 16, u_lat: float =
         c = int(c)
         digits = f"{m}{4 if m else 0}12"
         dims = (int(round(2.5 * c)), int(round(1.5 * c)), span)
-        flags = boundary_flags(dims)
-        if outlet_eq:
-            flags[flags == FLAG_OUTLET] = FLAG_OUTLET_EQ
-        voxelize_airfoil(dims, flags, naca4(digits, 200), aoa, c, *layout_anchor(dims))
+        if device:
+            placed = geometry.foil(naca4(digits, 200), aoa, c, *layout_anchor(dims))
+            flags = geometry.build_flags(dims, "boundary", placed, True, 0)[0]
+            if outlet_eq:   # voxels and closures never touch the outlet column
+                flags[flags == FLAG_OUTLET] = FLAG_OUTLET_EQ
+        else:
+            flags = boundary_flags(dims)
+            if outlet_eq:
+                flags[flags == FLAG_OUTLET] = FLAG_OUTLET_EQ
+            voxelize_airfoil(dims, flags, naca4(digits, 200), aoa, c, *layout_anchor(dims))
         tau = float(np.float32(0.5 + 3.0 * u_lat * c / reynolds))
         out.append(PolarTunnel(digits, aoa, c, dims, flags, tau, u_lat))
     return out
@@ -74,10 +85,13 @@ class BatchSolver:
     def init(self, tunnels, storage: str = "fp16", les_cs: float = 0.1, magic_lambda: float = 0.0,
              force_every: int = 100, stream=None):
         self.tunnels = list(tunnels)
-        self._flags = [np.ascontiguousarray(t.flags, np.uint8) for t in self.tunnels]
+        # Host bytes, or uint8 CUDA tensors (device-built flags).
+        self._flags = [t.flags if getattr(t.flags, "is_cuda", False) else np.ascontiguousarray(t.flags, np.uint8)
+                       for t in self.tunnels]
         arr = (capi.BatchTunnel * len(self.tunnels))()
         for i, (t, f) in enumerate(zip(self.tunnels, self._flags)):
-            arr[i] = capi.BatchTunnel(capi.Dims(*t.dims), f.ctypes.data_as(C.c_void_p), t.tau, t.u_lat, t.chord)
+            fp = C.c_void_p(f.data_ptr()) if getattr(f, "is_cuda", False) else f.ctypes.data_as(C.c_void_p)
+            arr[i] = capi.BatchTunnel(capi.Dims(*t.dims), fp, t.tau, t.u_lat, t.chord)
         err = C.create_string_buffer(512)
         rc = self._lib.fcfd_batch_init(self._h, arr, len(self.tunnels), STORE[storage],
                                        les_cs if les_cs > 0 else -1.0, magic_lambda, force_every, stream, err, 512)

@@ -4,7 +4,7 @@
 // launch-shape autotuner.
 //
 // Per tunnel the set-up follows the single-tunnel solver: flags -> kind
-// bytes (launch_classify), compact force-link list (build_force_links),
+// bytes (launch_classify), compact force-link list (device compaction),
 // uniform-flow reset feq(1, u) + the reference's speck perturbation
 // (src/sim/lbm_solver.cpp:49, 896-935) on both buffers.
 #include "../../include/foilcfd_batch.h"
@@ -331,18 +331,20 @@ int fcfd_batch_init(fcfd_batch* b, const fcfd_batch_tunnel* tunnels, int count, 
         for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMalloc(&y.f[k], static_cast<size_t>(y.n) * 19 * esz);
         if (e == cudaSuccess) e = cudaMalloc(&y.flags, static_cast<size_t>(y.n));
         if (e == cudaSuccess) e = cudaMalloc(&y.kind, static_cast<size_t>(y.n) + 64);
-        if (e == cudaSuccess) e = cudaMemcpy(y.flags, in.flags, static_cast<size_t>(y.n), cudaMemcpyHostToDevice);
+        // Flags from host or device memory (a polar built on the device);
+        // the link list is compacted on the device either way.
+        if (e == cudaSuccess)
+            e = cudaMemcpy(y.flags, in.flags, static_cast<size_t>(y.n),
+                           is_device_pointer(in.flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = launch_classify(y.flags, y.kind, y.d, b->stream);
-        std::vector<std::uint32_t> cells, masks;
-        if (e == cudaSuccess) build_force_links(y.d, in.flags, cells, masks);
-        y.linkCount = static_cast<int>(cells.size());
+        long long links = 0, again = 0;
+        if (e == cudaSuccess) e = device_force_links(y.d, y.flags, nullptr, nullptr, 0, &links, b->stream);
+        y.linkCount = static_cast<int>(links);
         maxLinks = std::max(maxLinks, y.linkCount);
-        if (e == cudaSuccess) e = cudaMalloc(&y.linkCells, std::max<size_t>(4, cells.size() * 4));
-        if (e == cudaSuccess) e = cudaMalloc(&y.linkMasks, std::max<size_t>(4, masks.size() * 4));
-        if (e == cudaSuccess && !cells.empty()) {
-            e = cudaMemcpy(y.linkCells, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice);
-            if (e == cudaSuccess) e = cudaMemcpy(y.linkMasks, masks.data(), masks.size() * 4, cudaMemcpyHostToDevice);
-        }
+        if (e == cudaSuccess) e = cudaMalloc(&y.linkCells, std::max<size_t>(4, static_cast<size_t>(links) * 4));
+        if (e == cudaSuccess) e = cudaMalloc(&y.linkMasks, std::max<size_t>(4, static_cast<size_t>(links) * 4));
+        if (e == cudaSuccess && links > 0)
+            e = device_force_links(y.d, y.flags, y.linkCells, y.linkMasks, links, &again, b->stream);
     }
     if (e == cudaSuccess) e = cudaMalloc(&b->dPartials, std::max(1, force_blocks(maxLinks)) * 3 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&b->dForceCur, 3 * count * sizeof(double));

@@ -558,6 +558,15 @@ cudaError_t compact_into(const P& p, Grid3 g, long long cap, long long* count, i
 
 // ---- host entry points ---------------------------------------------------------
 
+bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice;
+}
+
 cudaError_t device_build_flags(LevelDims d, int base, const std::uint8_t* in, const FoilRaster* foil, int closeGaps,
                                int shell, std::uint8_t* out, cudaStream_t st, int* closedOut) {
     const long long n = d.cells();

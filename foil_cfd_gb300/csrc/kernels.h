@@ -220,6 +220,8 @@ cudaError_t device_build_flags(LevelDims d, int base, const std::uint8_t* in, co
 cudaError_t device_solid_bbox(LevelDims d, const std::uint8_t* flags, cudaStream_t st, int box[4]);
 /// Cells whose flag is read and written / inlet / neither.
 cudaError_t device_flag_classes(LevelDims d, const std::uint8_t* flags, cudaStream_t st, long long out[3]);
+/// True for a pointer into device memory (cudaPointerGetAttributes).
+bool is_device_pointer(const void* p);
 /// Ordered cell lists. *count <- the list length; nothing is written when it
 /// exceeds cap (size with a first call of capacity 0). All synchronise.
 cudaError_t device_force_links(LevelDims d, const std::uint8_t* flags, std::uint32_t* cells, std::uint32_t* masks,

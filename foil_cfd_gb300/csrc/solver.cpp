@@ -44,14 +44,7 @@ void set_err(char* err, size_t len, const std::string& m) {
 }
 
 /// True for a pointer into device memory (a flag field built on the GPU).
-bool on_device(const void* p) {
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        (void)cudaGetLastError();
-        return false;
-    }
-    return a.type == cudaMemoryTypeDevice;
-}
+bool on_device(const void* p) { return is_device_pointer(p); }
 
 /// Host copy of a flag field given in host or device memory.
 void assign_flags(std::vector<std::uint8_t>& v, const std::uint8_t* p, size_t n) {

@@ -39,8 +39,9 @@ extern "C" {
 
 typedef struct fcfd_batch fcfd_batch;
 
-/* One tunnel: dims, host flags (nx*ny*nz CellFlag bytes, copied), lattice
- * relaxation time, inlet speed, and the chord in cells (force coefficients). */
+/* One tunnel: dims, flags (nx*ny*nz CellFlag bytes, copied; host memory or
+ * device memory, e.g. built by fcfd_device_build_flags), lattice relaxation
+ * time, inlet speed, and the chord in cells (force coefficients). */
 typedef struct fcfd_batch_tunnel {
     fcfd_dims dims;
     const uint8_t* flags;

@@ -129,3 +129,21 @@ def test_health_reads_speeds(fc):
     assert b.step_n(40) == 0
     speed, bad = b.health()
     assert (bad == 0).all() and (speed > 0.05).all() and (speed < 0.285).all()
+
+
+def test_device_built_polar_matches_host_built(fc):
+    """Polar tunnels whose flags the device geometry kernels build (CUDA
+    tensors handed to the batch) are the host builders' bytes and step bit
+    for bit like the host-built batch."""
+    from foil_cfd_gb300 import batch
+    kw = dict(count=4, seed=5, span=4, chord_range=(28, 44), aoas=[-4.0, 6.0, 13.5], cambers=(0, 4))
+    host = batch.polar_tunnels(**kw)
+    dev = batch.polar_tunnels(device=True, **kw)
+    for h, d in zip(host, dev):
+        assert d.flags.is_cuda and np.array_equal(d.flags.cpu().numpy(), h.flags)
+    bh, bd = make_batch(host, "fp16"), make_batch(dev, "fp16")
+    assert bh.step_n(40) == 0 and bd.step_n(40) == 0
+    for i in range(len(host)):
+        assert np.array_equal(bh.export_f32(i), bd.export_f32(i))
+    assert np.array_equal(np.asarray(bh.forces_now()), np.asarray(bd.forces_now()))
+
