@@ -328,6 +328,7 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10, fixed=None):
     t0 = time.perf_counter()
     tunnels = batch.polar_tunnels()
     host_build_s = time.perf_counter() - t0
+    batch.polar_tunnels(count=1, device=True)   # first use loads the geometry kernels
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     dev_tunnels = batch.polar_tunnels(device=True)

@@ -53,9 +53,9 @@ def polar_tunnels(count: int = 24, seed: int = 0, span: int = 16, u_lat: float =
         dims = (int(round(2.5 * c)), int(round(1.5 * c)), span)
         if device:
             placed = geometry.foil(naca4(digits, 200), aoa, c, *layout_anchor(dims))
-            flags = geometry.build_flags(dims, "boundary", placed, True, 0)[0]
+            flags = geometry.build_flags(dims, "boundary", placed, True, 0, count_closed=False)[0]
             if outlet_eq:   # voxels and closures never touch the outlet column
-                flags[flags == FLAG_OUTLET] = FLAG_OUTLET_EQ
+                flags.masked_fill_(flags == FLAG_OUTLET, FLAG_OUTLET_EQ)
         else:
             flags = boundary_flags(dims)
             if outlet_eq:

@@ -606,11 +606,12 @@ cudaError_t device_build_flags(LevelDims d, int base, const std::uint8_t* in, co
         e = cudaGetLastError();
     }
     int h[2] = {0, 0};
-    if (e == cudaSuccess && closedOut) {
+    // A rasterised outline is checked for the row-crossing limit.
+    if (e == cudaSuccess && (closedOut || mask)) {
         e = cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e == cudaSuccess && h[1]) e = cudaErrorInvalidValue;   // a row with > 64 crossings
-        if (e == cudaSuccess) *closedOut = h[0];
+        if (e == cudaSuccess && closedOut) *closedOut = h[0];
     }
     cudaFreeAsync(work, st);
     return e;

@@ -48,9 +48,12 @@ def foil(xy, aoa_deg, chord_cells, anchor_x, anchor_y):
             float(anchor_y))
 
 
-def build_flags(dims, base="boundary", placed=None, close_gaps=True, shell=0, inp=None, out=None, stream=None):
+def build_flags(dims, base="boundary", placed=None, close_gaps=True, shell=0, inp=None, out=None, stream=None,
+                count_closed=True):
     """Flag field of `dims` in device memory; returns (uint8 tensor, closed).
-    base: "boundary" (domain faces), "fluid" or "input" (the tensor `inp`)."""
+    base: "boundary" (domain faces), "fluid" or "input" (the tensor `inp`).
+    count_closed=False skips the closure count (and its synchronisation);
+    closed is then None."""
     torch = _torch()
     n = int(np.prod(dims))
     if out is None:
@@ -65,10 +68,10 @@ def build_flags(dims, base="boundary", placed=None, close_gaps=True, shell=0, in
     closed = C.c_int(0)
     rc = capi.load().fcfd_device_build_flags(C.byref(d), BASE[base], _dev(inp), C.byref(fp) if fp else None,
                                              int(close_gaps), int(shell), _dev(out), _stream(stream),
-                                             C.byref(closed))
+                                             C.byref(closed) if count_closed else None)
     del keep
     _check(rc, "device flag build")
-    return out, closed.value
+    return out, (closed.value if count_closed else None)
 
 
 def derive_patch_box(dims, flags, mx0, mx1, my0, my1, clearance=3, stream=None) -> Box:

@@ -17,8 +17,10 @@
  * field in device memory as well: the solver then copies it on the device and
  * builds its force-link, wall-model, shell and seed lists with these kernels.
  *
- * Return convention: 0 or a cudaError_t value. Every call synchronises the
- * stream before it returns.
+ * Return convention: 0 or a cudaError_t value. The list builders and the
+ * patch box synchronise the stream before they return; the flag builder
+ * does when it rasterises an outline (row-crossing check) or reports the
+ * closure count.
  */
 #ifndef FOILCFD_GEOM_H
 #define FOILCFD_GEOM_H
