@@ -35,9 +35,11 @@ namespace {
 
 constexpr int kRefineBlock = 128;
 // Resident 128-thread blocks per SM the fill and the restriction are
-// compiled for (64 and 48 registers; measured 3-12 % and 17 % faster than
-// the unconstrained 72 and 54).
-constexpr int kFillMinBlocks = 8;
+// compiled for, as measured on GB300: the FP16 fill at 64 registers is 5 %
+// faster than at 72 (the FP32 fill 3 % slower, so it is left free); the
+// restriction at 48 registers is 17 % faster than at 54.
+template <class S> struct FillMinBlocks { static constexpr int value = 1; };
+template <> struct FillMinBlocks<StoreF16> { static constexpr int value = 8; };
 constexpr int kRestrictMinBlocks = 10;
 constexpr int kRestrictBand = 2;   // coarse band skipped by the restriction
 constexpr int kRestrictBlend = 3;  // edge-blend ramp width (coarse cells)
@@ -68,7 +70,7 @@ __device__ __forceinline__ void regularize(float (&fneq)[kQ]) {
 
 
 template <class S>
-__global__ void __launch_bounds__(kRefineBlock, kFillMinBlocks)
+__global__ void __launch_bounds__(kRefineBlock, FillMinBlocks<S>::value)
 fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restrict__ cT1,
             const std::uint8_t* __restrict__ ckind, typename S::T* __restrict__ ff,
             const std::uint32_t* __restrict__ targets, int count, RefineGeom g, float invFactor,
