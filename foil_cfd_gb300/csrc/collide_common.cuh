@@ -424,14 +424,19 @@ cudaError_t launch_apply_flag_edits_impl(void* fA, void* fB, const std::uint8_t*
 // ---- last fine sub-step with the restriction's child averages fused in --------
 // Factor-2 patches only. A thread owns one fine x column of a 2 x 2 (y, z)
 // cell group and updates its four cells in the children's summation order
-// (z, then y); after each cell the even lane (child x offset 0) takes its
-// odd partner's stored values with a warp shuffle and adds its own, then the
-// partner's -- the stand-alone pass's order (z, y, x; solid children
-// skipped) -- into its own column of a shared-memory accumulator (private to
-// the lane: no block barrier, and no extra registers during the collide). The values used are the stored ones, exactly as a later
-// load would return them. The even lane then writes the scratch record. This
-// saves the stand-alone pass's full re-read of the fine populations.
+// (z, then y); the x partner of each child pair is the neighbouring lane.
+// The child sums stay in registers split across the lane pair (even lane:
+// directions 0..9, odd lane: 10..18): per cell one shuffle per direction
+// pair hands each lane the partner's value it needs, and each lane adds the
+// two children in the stand-alone pass's order (z, y, x; solid children
+// skipped). The values summed are the stored ones, exactly as a later load
+// would return them. The even lane then collects the odd lane's sums and
+// writes the scratch record. This saves the stand-alone pass's full re-read
+// of the fine populations (measured 3 % faster than accumulating in shared
+// memory).
 constexpr int kFuseX = 128;
+
+constexpr int kSplit = 10;   // directions summed by the even lane
 
 template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kFuseX, S::kChildMinBlocks)
@@ -441,13 +446,12 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
     const bool inX = x < a.nx;
     const bool even = (threadIdx.x & 1) == 0;
     const int lx = cf.boxX0 + (x >> 1) - cf.rx0, ly = cf.boxY0 + static_cast<int>(blockIdx.y) - cf.ry0;
-    const bool record = even && x + 1 < a.nx && lx >= 0 && lx < cf.rw && ly >= 0 && ly < cf.rh;
-    __shared__ float acc[kQ][kFuseX / 2];
-    const int col = threadIdx.x >> 1;
-    if (record) {
+    // Both lanes of a pair take the record decision of the even lane.
+    const int xe = x & ~1;
+    const bool record = xe + 1 < a.nx && lx >= 0 && lx < cf.rw && ly >= 0 && ly < cf.rh;
+    float acc[kSplit];
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) acc[q][col] = 0.0f;
-    }
+    for (int k = 0; k < kSplit; ++k) acc[k] = 0.0f;
     int nFluid = 0;
     for (int kz = 0; kz < 2; ++kz)
         for (int jy = 0; jy < 2; ++jy) {
@@ -481,25 +485,37 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                     }
                 }
             }
+            if (!solid) ++nFluid;
             const bool partnerSolid = __shfl_xor_sync(0xffffffffu, static_cast<int>(solid), 1) != 0;
-            if (record && !solid) {
-                ++nFluid;
+            // Children in order: the even lane's first, then the odd lane's.
+            const bool skipFirst = even ? solid : partnerSolid;
+            const bool skipSecond = even ? partnerSolid : solid;
 #pragma unroll
-                for (int q = 0; q < kQ; ++q) acc[q][col] += v[q];
+            for (int k = 0; k < kSplit; ++k) {
+                const int qo = k + kSplit < kQ ? k + kSplit : kQ - 1;   // odd lane's direction
+                const float send = even ? v[qo] : v[k];
+                const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+                const float own = even ? v[k] : v[qo];
+                const float first = even ? own : recv, second = even ? recv : own;
+                if (k + kSplit < kQ || even) {
+                    float t = acc[k];
+                    if (!skipFirst) t += first;
+                    if (!skipSecond) t += second;
+                    acc[k] = t;
+                }
             }
-#pragma unroll
-            for (int q = 0; q < kQ; ++q) {
-                const float pv = __shfl_xor_sync(0xffffffffu, v[q], 1);
-                if (record && !partnerSolid) acc[q][col] += pv;
-            }
-            if (record && !partnerSolid) ++nFluid;
         }
-    if (!record) return;
+    // The even lane gathers the odd lane's sums (directions 10..18) and the
+    // child count, then writes the record.
+    const int nOdd = __shfl_xor_sync(0xffffffffu, nFluid, 1);
     float fi[kQ];
 #pragma unroll
-    for (int q = 0; q < kQ; ++q) fi[q] = acc[q][col];
+    for (int k = 0; k < kSplit; ++k) fi[k] = acc[k];
+#pragma unroll
+    for (int k = 0; k + kSplit < kQ; ++k) fi[k + kSplit] = __shfl_xor_sync(0xffffffffu, acc[k], 1);
+    if (!record || !even) return;
     const long long t = lx + static_cast<long long>(cf.rw) * (ly + static_cast<long long>(cf.rh) * blockIdx.z);
-    write_child_record(fi, nFluid, reinterpret_cast<float4*>(cf.scratch) + t * (kScratchVals / 4));
+    write_child_record(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t * (kScratchVals / 4));
 }
 
 template <class S, bool EXACT>
