@@ -34,13 +34,6 @@ namespace fcfd {
 namespace {
 
 constexpr int kRefineBlock = 128;
-// Resident 128-thread blocks per SM the fill and the restriction are
-// compiled for, as measured on GB300: the FP16 fill at 64 registers is 5 %
-// faster than at 72 (the FP32 fill 3 % slower, so it is left free); the
-// restriction at 48 registers is 17 % faster than at 54.
-template <class S> struct FillMinBlocks { static constexpr int value = 1; };
-template <> struct FillMinBlocks<StoreF16> { static constexpr int value = 8; };
-constexpr int kRestrictMinBlocks = 10;
 constexpr int kRestrictBand = 2;   // coarse band skipped by the restriction
 constexpr int kRestrictBlend = 3;  // edge-blend ramp width (coarse cells)
 
@@ -70,7 +63,7 @@ __device__ __forceinline__ void regularize(float (&fneq)[kQ]) {
 
 
 template <class S>
-__global__ void __launch_bounds__(kRefineBlock, FillMinBlocks<S>::value)
+__global__ void __launch_bounds__(kRefineBlock)
 fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restrict__ cT1,
             const std::uint8_t* __restrict__ ckind, typename S::T* __restrict__ ff,
             const std::uint32_t* __restrict__ targets, int count, RefineGeom g, float invFactor,
@@ -177,7 +170,7 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
 constexpr int kRestrictTX = 32, kRestrictTY = 2, kRestrictTZ = 2;
 
 template <class S>
-__global__ void __launch_bounds__(kRestrictTX * kRestrictTY * kRestrictTZ, kRestrictMinBlocks)
+__global__ void __launch_bounds__(kRestrictTX * kRestrictTY * kRestrictTZ)
 restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__ ckind,
                 RefineGeom g, int rx0, int ry0, int rw, int rh, float neqScaleInv,
                 const float* __restrict__ scratch, float* __restrict__ mRho,
