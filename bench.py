@@ -34,6 +34,7 @@ METRIC = "GLUPS, 23.6M-cell wall-modeled tunnel: FP16-store vs FP32, % of HBM pe
 UNIT = "GLUPS"
 BYTES_PER_LUP = {"fp32": 153.0, "fp16": 77.0}  # 19 loads + 19 stores + 1 kind byte
 BATCH = 50
+DIST = None   # torch.distributed when launched as replicas under torchrun
 # Measured DRAM traffic of the collide kernel over its algorithmic bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum of one coarse and one fine
 # launch, divided by the class-based algorithmic bytes of those launches) from
@@ -174,7 +175,11 @@ def measure(t, storage, steps, warmup, clocks=None):
     l0 = sol.kernel_launches()
     if clocks:
         clocks.start()
+    sol.synchronize()
+    barrier()
     ms = timed_steps(sol, steps)
+    sol.synchronize()
+    barrier()
     clk = clocks.stop() if clocks else None
     if sol.nan_detected():
         raise RuntimeError("the solver latched its watchdog inside the timed steps: no valid timing")
@@ -715,6 +720,9 @@ def cpu_reference(t, steps):
 
 
 def dist_setup():
+    """One process per GPU under torchrun (RANK/LOCAL_RANK/WORLD_SIZE from the
+    environment): NCCL with GPUs, gloo on a host without them."""
+    global DIST
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return None, 0, 1
@@ -722,9 +730,34 @@ def dist_setup():
     import torch.distributed as dist
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    DIST = dist
     return dist, rank, ws
+
+
+def barrier():
+    """Barrier of all replicas (no-op on one process)."""
+    if DIST is not None:
+        DIST.barrier()
+
+
+def max_over_ranks(dist, value: float) -> float:
+    """The slowest replica's time: all-reduce MAX (NCCL on the GPU, gloo on
+    the host)."""
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def aggregate_glups(world: int, updates_per_step: float, steps: int, ms: float) -> float:
+    """Whole-job throughput: every replica's updates over the slowest time."""
+    return world * updates_per_step * steps / (ms * 1e-3) / 1e9
 
 
 def main():
@@ -801,13 +834,8 @@ def main():
                           "roofline": roofline("fp16", r16["collide"]), "clocks": r16["clocks"]}))
         return
     r32 = measure(t, "fp32", args.steps, warmup, clocks)
-    ms = r32["ms"]
-    if dist is not None:
-        import torch
-        tt = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = ws * t.updates_per_step() * args.steps / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(dist, r32["ms"])
+    value = aggregate_glups(ws, t.updates_per_step(), args.steps, ms)
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
