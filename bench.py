@@ -683,6 +683,60 @@ def snapshot_leg(sol, t, reps=3):
     return out
 
 
+HEADLINE = dict(nx=768, ny=320, nz=96, chord=256, aoa=6.0, tau=0.52, u=0.08)
+
+
+def headline_tunnel():
+    """The reference's own headline configuration (its --selftest grid:
+    768x320x96, plain half-way bounce-back, no patch, no wall model, FP32),
+    here with a NACA 0012 at 6 deg, chord 256 cells."""
+    from foil_cfd_gb300 import tunnels
+    h = HEADLINE
+    return tunnels.airfoil_tunnel(h["nx"], h["ny"], h["nz"], chord=h["chord"], aoa=h["aoa"], patch=False)
+
+
+def headline_leg(warmup=100, steps=100):
+    """This library's step on the reference's headline configuration, timed
+    like the reference's --selftest (stepN(100) warm-up, stepN(100) timed)."""
+    import foil_cfd_gb300 as fc
+    t = headline_tunnel()
+    sol = fc.LBMSolver()
+    sol.init(t.dims, fc.scaling_direct(HEADLINE["tau"], HEADLINE["u"], t.chord_cells), t.flags, storage="fp32")
+    sol.set_startup_ramp_enabled(False)
+    sol.reset()
+    assert sol.step_n(warmup) == 0
+    ms = timed_steps(sol, steps)
+    cells = float(np.prod(t.dims))
+    return {"workload": "768x320x96 plain tunnel (the reference's --selftest grid), NACA 0012 at 6 deg, chord 256, "
+                        "FP32, no wall model, no patch, tau 0.52, u 0.08",
+            "glups": round(cells * steps / (ms * 1e-3) / 1e9, 3), "ms_per_step": round(ms / steps, 4),
+            "steps": steps, "warmup": warmup, "latched": bool(sol.nan_detected())}
+
+
+def reference_cuda_leg(warmup=100, steps=100):
+    """The reference's own CUDA stream-collide (+ its per-step ghost-plane
+    refresh) on this GPU and the same configuration: compiled from the
+    reference tree as it builds it (nvcc -O3, sm_103a) into a cubin in the
+    build container, launched through the driver-API harness."""
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "reference cubin not built (the reference tree is only in the build container) "
+                               "or nvcc missing"}
+    from oracle import oracle
+    t = headline_tunnel()
+    n = int(np.prod(t.dims))
+    # Uniform start feq(1, u_in) everywhere (the oracle's equilibrium).
+    f0 = oracle.equilibrium(np.ones(n), np.full(n, HEADLINE["u"]), np.zeros(n), np.zeros(n), np.float32)
+    _, ms = ref_gpu.run(t.dims, t.flags, f0, HEADLINE["tau"], HEADLINE["u"], cs=0.1733, warmup=warmup, steps=steps,
+                        batch=100)
+    cells = float(np.prod(t.dims))
+    return {"workload": "768x320x96 plain tunnel, NACA 0012 at 6 deg, chord 256, FP32, tau 0.52, u 0.08",
+            "kernel": "streamCollideKernel<false,false> + refreshGhostZKernel (src/sim/lbm_core.cu), nvcc -O3 "
+                      "sm_103a, launched per step as the reference's stepN does",
+            "glups": round(cells * steps / (ms * 1e-3) / 1e9, 3), "ms_per_step": round(ms / steps, 4),
+            "steps": steps, "warmup": warmup}
+
+
 def cpu_host():
     try:
         model = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -809,6 +863,11 @@ def main():
                 "data": "synthetic", "config": cfg,
                 "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": ref["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if not args.small:
+            try:
+                line["reference_cuda_kernel"] = reference_cuda_leg()
+            except Exception as ex:   # a GPU-side failure must not hide the CPU line
+                line["reference_cuda_kernel"] = {"unavailable": str(ex)[:200]}
         print(json.dumps(line))
         return
 
@@ -858,6 +917,7 @@ def main():
         line["batched_polar"] = polar_leg(args.polar_steps)
     if not args.no_geometry and ws == 1 and not args.small:
         line["geometry_build"] = geometry_leg(t)
+        line["headline_plain_tunnel"] = headline_leg()
     if args.precision and ws == 1:
         line["precision"] = precision_leg()
     del r32

@@ -17,6 +17,7 @@ and to generate the golden fixtures under tests/golden/.
 from __future__ import annotations
 
 import os
+import shutil
 import subprocess
 import sys
 from pathlib import Path
@@ -93,6 +94,21 @@ def build(force: bool = False) -> dict:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference geometry build failed:\n{r.stderr[-4000:]}")
+    # The reference's CUDA stream-collide as an sm_103a cubin (device code
+    # only, loaded through the driver API by ref_gpu_harness.cu), built as
+    # the reference builds it (C++20, default contraction).
+    # A second one without contraction is the exact-parity twin of the CPU
+    # build (the check that the harness passes the parameters right).
+    for key, name, extra in (("cubin", "ref_core_sm103a.cubin", []),
+                             ("cubin_nofma", "ref_core_sm103a_nofma.cubin", ["--fmad=false"])):
+        cubin = OUT / name
+        libs[key] = cubin
+        if (force or not cubin.exists()) and shutil.which("nvcc"):
+            cmd = ["nvcc", "-cubin", "-std=c++20", "-O3", *extra, "-gencode", "arch=compute_103a,code=sm_103a",
+                   "-I", str(SIM), str(SIM / "lbm_core.cu"), "-o", str(cubin)]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"reference cubin build failed:\n{r.stderr[-4000:]}")
     # The snapshot code (keys, flag hash, FCS1 reader/writer); the solver
     # methods it names are stubbed by the driver.
     so = OUT / "libref_snapshot.so"
