@@ -99,13 +99,16 @@ def build(force: bool = False) -> dict:
     # the reference builds it (C++20, default contraction).
     # A second one without contraction is the exact-parity twin of the CPU
     # build (the check that the harness passes the parameters right).
-    for key, name, extra in (("cubin", "ref_core_sm103a.cubin", []),
-                             ("cubin_nofma", "ref_core_sm103a_nofma.cubin", ["--fmad=false"])):
+    for key, src, name, extra in (("cubin", "lbm_core.cu", "ref_core_sm103a.cubin", []),
+                                  ("cubin_nofma", "lbm_core.cu", "ref_core_sm103a_nofma.cubin", ["--fmad=false"]),
+                                  ("cubin_refine", "lbm_refine.cu", "ref_refine_sm103a.cubin", []),
+                                  ("cubin_refine_nofma", "lbm_refine.cu", "ref_refine_sm103a_nofma.cubin",
+                                   ["--fmad=false"])):
         cubin = OUT / name
         libs[key] = cubin
         if (force or not cubin.exists()) and shutil.which("nvcc"):
             cmd = ["nvcc", "-cubin", "-std=c++20", "-O3", *extra, "-gencode", "arch=compute_103a,code=sm_103a",
-                   "-I", str(SIM), str(SIM / "lbm_core.cu"), "-o", str(cubin)]
+                   "-I", str(SIM), str(SIM / src), "-o", str(cubin)]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError(f"reference cubin build failed:\n{r.stderr[-4000:]}")

@@ -43,3 +43,48 @@ def test_reference_cuda_kernel_matches_ours(fc, oracle_mod):
     assert s.step_n(25) == 0
     m = written_mask(flags)
     assert np.array_equal(s.export_f32().reshape(19, -1)[:, m], ref.reshape(19, -1)[:, m])
+
+
+def uniform_feq(u):
+    """feq(1, u, 0, 0) per direction in FP32 arithmetic, in the expression
+    order the harness uses for its uniform start (the reference's
+    equilibrium19: (w rho)(1 + cu + cu cu / 2 - usq))."""
+    f32 = np.float32
+    u = f32(u)
+    usq = f32(1.5) * (u * u)
+    cx = [0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0]
+    out = np.empty(19, np.float32)
+    for q in range(19):
+        w = f32(1.0) / f32(3.0) if q == 0 else (f32(1.0) / f32(18.0) if q <= 6 else f32(1.0) / f32(36.0))
+        cu = f32(3.0) * (f32(cx[q]) * u)
+        out[q] = (w * f32(1.0)) * (((f32(1.0) + cu) + (f32(0.5) * cu) * cu) - usq)
+    return out
+
+
+def test_reference_cuda_refined_step_matches_ours(fc):
+    """The reference's refined step (its collide, fill and restriction
+    kernels from the reference tree, no contraction) against this library's
+    step with the 2:1 patch: coarse and fine fluid populations equal after
+    ten coarse steps from the same uniform state."""
+    from oracle import ref_gpu
+    from foil_cfd_gb300.tunnels import airfoil_tunnel
+    if not (ref_gpu.CUBIN_NOFMA.exists() and ref_gpu.CUBIN_REFINE_NOFMA.exists()):
+        pytest.skip("reference cubins not built (needs the reference tree in the build container)")
+    t = airfoil_tunnel(160, 64, 16, chord=64, aoa=6.0)
+    nc, nf = int(np.prod(t.dims)), int(np.prod(t.fine_dims))
+    feq = uniform_feq(t.u_lat)
+    _, rc, rf = ref_gpu.run_refined(t.dims, t.flags, t.fine_dims, t.fine_flags, t.box, t.factor, 0.52, t.u_lat,
+                                    cs=0.1, wall_model=False, warmup=0, steps=10, batch=50,
+                                    refine_cubin=ref_gpu.CUBIN_REFINE_NOFMA, states=True)
+    s = fc.LBMSolver()
+    s.init(t.dims, fc.scaling_direct(0.52, t.u_lat, t.chord_cells), t.flags, les_cs=0.1)
+    s.set_startup_ramp_enabled(False)
+    s.reset()
+    s.init_refinement(t.box, t.factor, t.fine_flags)
+    s.import_f32(np.repeat(feq, nc))
+    s.import_fine_f32(np.repeat(feq, nf))
+    assert s.step_n(10) == 0
+    mc = written_mask(t.flags)
+    assert np.array_equal(s.export_f32().reshape(19, -1)[:, mc], rc.reshape(19, -1)[:, mc])
+    mf = t.fine_flags == 0
+    assert np.array_equal(s.export_fine_f32().reshape(19, -1)[:, mf], rf.reshape(19, -1)[:, mf])
