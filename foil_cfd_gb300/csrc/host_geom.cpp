@@ -1,9 +1,10 @@
 // Host-side builders: the wall-model cell list (reference
-// src/sim/wall_model.cpp:55-236), the force-link list, and the geometry
-// fixtures of the tunnels (domain boundary flags, NACA 4-digit sections,
-// point-in-polygon airfoil voxelisation with trailing-edge gap closure, the
-// interface shell of a refinement patch, and the patch box), following
-// src/geom/voxelizer.cpp and src/geom/airfoil.cpp:177-266.
+// src/sim/wall_model.cpp:55-236) and the geometry of the tunnels (domain
+// boundary flags, NACA 4-digit sections, point-in-polygon airfoil
+// voxelisation, trailing-edge gap closure, the interface shell of a
+// refinement patch, and the patch box), following src/geom/voxelizer.cpp and
+// src/geom/airfoil.cpp:177-266. The device builders (geom_kernels.cu) produce
+// the same bytes.
 #include "host_geom.h"
 
 #include <algorithm>
@@ -126,30 +127,6 @@ WallList build_wall_list(const LevelDims& d, const std::uint8_t* active, const s
     }
     if (stats) *stats = tally;
     return merged;
-}
-
-void build_force_links(const LevelDims& d, const std::uint8_t* flags,
-                       std::vector<std::uint32_t>& cells, std::vector<std::uint32_t>& masks) {
-    cells.clear();
-    masks.clear();
-    for (int z = 0; z < d.nz; ++z)
-        for (int y = 0; y < d.ny; ++y)
-            for (int x = 0; x < d.nx; ++x) {
-                const long long c = idx(x, y, z, d);
-                if (flags[c] != kFlagFluidHost) continue;
-                std::uint32_t m = 0;
-                for (int q = 1; q < 19; ++q) {
-                    int X = x + kHostCx[q], Y = y + kHostCy[q], Z = z + kHostCz[q];
-                    X = X < 0 ? X + d.nx : (X >= d.nx ? X - d.nx : X);
-                    Y = Y < 0 ? Y + d.ny : (Y >= d.ny ? Y - d.ny : Y);
-                    Z = wrap_z(Z, d.nz);
-                    if (flags[idx(X, Y, Z, d)] == kFlagSolidHost) m |= 1u << q;
-                }
-                if (m) {
-                    cells.push_back(static_cast<std::uint32_t>(c));
-                    masks.push_back(m);
-                }
-            }
 }
 
 void boundary_flags(const LevelDims& d, std::uint8_t* f) {

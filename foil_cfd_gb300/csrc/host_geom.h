@@ -35,11 +35,6 @@ WallList build_wall_list(const LevelDims& d, const std::uint8_t* active,
                          const std::uint8_t* clean, int sampleCells,
                          WallListStats* stats);
 
-/// Fluid cells with a solid neighbour at +c_q (bit q of the mask).
-void build_force_links(const LevelDims& d, const std::uint8_t* flags,
-                       std::vector<std::uint32_t>& cells,
-                       std::vector<std::uint32_t>& masks);
-
 void boundary_flags(const LevelDims& d, std::uint8_t* flags);
 int naca4(const char* digits, int pointsPerSurface, std::vector<float>& xy);
 constexpr int kMinOutlinePoints = 20;  ///< smallest valid section outline
