@@ -342,7 +342,7 @@ __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ sr
 constexpr int kCellBlockX = 128;
 
 template <class S, bool WM, bool EXACT, bool QL>
-__global__ void __launch_bounds__(kCellBlockX)
+__global__ void __launch_bounds__(kCellBlockX, S::kCellMinBlocks)
 collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                     const std::uint8_t* __restrict__ kind, CollideArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
