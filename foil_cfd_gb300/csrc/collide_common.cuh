@@ -429,8 +429,10 @@ cudaError_t launch_apply_flag_edits_impl(void* fA, void* fB, const std::uint8_t*
 // directions 0..9, odd lane: 10..18): per cell one shuffle per direction
 // pair hands each lane the partner's value it needs, and each lane adds the
 // two children in the stand-alone pass's order (z, y, x; solid children
-// skipped). The values summed are the stored ones, exactly as a later load
-// would return them. The even lane then collects the odd lane's sums and
+// skipped). With FP32 storage the values summed are the stored ones, exactly
+// as a later load returns them (bit-identical to the separate pass); with
+// FP16 storage they are the collided FP32 values before the half rounding.
+// The even lane then collects the odd lane's sums and
 // writes the scratch record. This saves the stand-alone pass's full re-read
 // of the fine populations (measured 3 % faster than accumulating in shared
 // memory).
@@ -469,11 +471,11 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                     else gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, v);
                     float rr, ux, uy, uz;
                     collide_body<EXACT>(v, a, rr, ux, uy, uz);
+                    // FP32: the sums see the stored values exactly. FP16:
+                    // the collided FP32 values (not their half round trip),
+                    // the more accurate child average.
 #pragma unroll
-                    for (int q = 0; q < kQ; ++q) {
-                        S::st(dst + q * a.n, cell, v[q], wgt(q));
-                        v[q] = S::rt(v[q], wgt(q));
-                    }
+                    for (int q = 0; q < kQ; ++q) S::st(dst + q * a.n, cell, v[q], wgt(q));
                     solid = false;
                 } else {
                     boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
