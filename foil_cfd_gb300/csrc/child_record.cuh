@@ -1,7 +1,7 @@
 // Restriction pass 1 per coarse cell: the averaged children's moments with
 // the density floor and the |u| <= 0.3 limiter, their non-equilibrium part,
-// and the 96-byte scratch record the restriction filter reads (fneq[19],
-// valid flag, rho, ux, uy, uz as six float4). Shared by the stand-alone
+// and the scratch record the restriction filter reads (fneq[19], valid
+// flag, rho, ux, uy, uz; 96 B with FP32 storage, 64 B with FP16). Shared by the stand-alone
 // child-average kernel and the fine collide that fuses it. Every multiply
 // and add is an explicit round-to-nearest intrinsic in the reference's
 // operation order, so the record rounds the same in a translation unit built
@@ -10,6 +10,8 @@
 #pragma once
 
 #include "d3q19.cuh"
+
+#include <cuda_fp16.h>
 
 namespace fcfd {
 
@@ -52,10 +54,121 @@ __device__ __forceinline__ float feq_q_rn(int q, float rho, float ux, float uy, 
     return rn_mul(rn_mul(wgt(q), rho), poly);
 }
 
+/// Layout of a coarse cell's record by storage. FP32 storage: fneq[19] in
+/// FP32, the valid flag, rho, ux, uy, uz -- six float4 (96 B), so the
+/// restriction is bit-identical to the reference's. FP16 storage: fneq[19]
+/// as halves (the precision of the stored deviations), the valid flag and
+/// rho, ux, uy, uz in FP32 -- four float4 (64 B); the restriction's 19
+/// neighbour reads per coarse cell then move 48 B each instead of 80 B.
+template <class S> struct ChildRecord;
+
+template <> struct ChildRecord<StoreF32> {
+    static constexpr int kVec = kScratchVals / 4;
+    __device__ __forceinline__ static void write(float4* rec, const float (&fneq)[kQ], float rho, float ux,
+                                                 float uy, float uz) {
+        float r[kScratchVals];
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) r[q] = fneq[q];
+        r[kScratchValid] = 1.0f;
+        r[kScratchRho] = rho; r[kScratchRho + 1] = ux; r[kScratchRho + 2] = uy; r[kScratchRho + 3] = uz;
+#pragma unroll
+        for (int k = 0; k < kVec; ++k) rec[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+    }
+    __device__ __forceinline__ static void write_invalid(float4* rec) {
+        rec[kScratchValid / 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    /// fneq of the record into out; false (out untouched) when not valid.
+    __device__ __forceinline__ static bool load(const float4* rec, float (&out)[kQ]) {
+        const float4 v4 = __ldg(rec + kScratchValid / 4);   // fneq[16..18], valid
+        if (v4.w == 0.0f) return false;
+        out[16] = v4.x; out[17] = v4.y; out[18] = v4.z;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 a = __ldg(rec + k);
+            out[4 * k] = a.x; out[4 * k + 1] = a.y; out[4 * k + 2] = a.z; out[4 * k + 3] = a.w;
+        }
+        return true;
+    }
+    /// acc[q] += fneq[q] for every q when the record is valid.
+    __device__ __forceinline__ static bool add(const float4* rec, float (&acc)[kQ]) {
+        const float4 last = __ldg(rec + kScratchValid / 4);
+        if (last.w == 0.0f) return false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 a = __ldg(rec + k);
+            acc[4 * k] += a.x; acc[4 * k + 1] += a.y; acc[4 * k + 2] += a.z; acc[4 * k + 3] += a.w;
+        }
+        acc[16] += last.x; acc[17] += last.y; acc[18] += last.z;
+        return true;
+    }
+    __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + kScratchRho / 4); }
+};
+
+template <> struct ChildRecord<StoreF16> {
+    static constexpr int kVec = 4;   // halves 0-7 | halves 8-15 | halves 16-18, valid | rho, u, v, w
+    __device__ __forceinline__ static unsigned pack(float a, float b) {
+        const __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<const unsigned*>(&h);
+    }
+    __device__ __forceinline__ static float2 unpack(unsigned u) {
+        const __half2 h = *reinterpret_cast<const __half2*>(&u);
+        return __half22float2(h);
+    }
+    __device__ __forceinline__ static void write(float4* rec, const float (&fneq)[kQ], float rho, float ux,
+                                                 float uy, float uz) {
+        uint4* r = reinterpret_cast<uint4*>(rec);
+        r[0] = make_uint4(pack(fneq[0], fneq[1]), pack(fneq[2], fneq[3]), pack(fneq[4], fneq[5]),
+                          pack(fneq[6], fneq[7]));
+        r[1] = make_uint4(pack(fneq[8], fneq[9]), pack(fneq[10], fneq[11]), pack(fneq[12], fneq[13]),
+                          pack(fneq[14], fneq[15]));
+        r[2] = make_uint4(pack(fneq[16], fneq[17]), pack(fneq[18], 0.0f), __float_as_uint(1.0f), 0u);
+        rec[3] = make_float4(rho, ux, uy, uz);
+    }
+    __device__ __forceinline__ static void write_invalid(float4* rec) {
+        reinterpret_cast<uint4*>(rec)[2] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __device__ __forceinline__ static bool load(const float4* rec, float (&out)[kQ]) {
+        const uint4 c2 = __ldg(reinterpret_cast<const uint4*>(rec) + 2);
+        if (__uint_as_float(c2.z) == 0.0f) return false;
+        const float2 p16 = unpack(c2.x), p18 = unpack(c2.y);
+        out[16] = p16.x; out[17] = p16.y; out[18] = p18.x;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint4 c = __ldg(reinterpret_cast<const uint4*>(rec) + k);
+            const unsigned w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 p = unpack(w[j]);
+                out[8 * k + 2 * j] = p.x; out[8 * k + 2 * j + 1] = p.y;
+            }
+        }
+        return true;
+    }
+    __device__ __forceinline__ static bool add(const float4* rec, float (&acc)[kQ]) {
+        const uint4 c2 = __ldg(reinterpret_cast<const uint4*>(rec) + 2);
+        if (__uint_as_float(c2.z) == 0.0f) return false;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint4 c = __ldg(reinterpret_cast<const uint4*>(rec) + k);
+            const unsigned w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 p = unpack(w[j]);
+                acc[8 * k + 2 * j] += p.x; acc[8 * k + 2 * j + 1] += p.y;
+            }
+        }
+        const float2 p16 = unpack(c2.x), p18 = unpack(c2.y);
+        acc[16] += p16.x; acc[17] += p16.y; acc[18] += p18.x;
+        return true;
+    }
+    __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + 3); }
+};
+
 /// Record of a coarse cell from the sum fi of its nFluid fluid children.
+template <class S>
 __device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, float4* rec) {
     if (nFluid == 0) {
-        rec[kScratchValid / 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ChildRecord<S>::write_invalid(rec);
         return;
     }
     const float invN = 1.0f / static_cast<float>(nFluid);
@@ -64,13 +177,10 @@ __device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, 
     float rho, ux, uy, uz;
     limited_moments(fi, rho, ux, uy, uz);
     const float usq = rn_mul(1.5f, rn_add(rn_add(rn_mul(ux, ux), rn_mul(uy, uy)), rn_mul(uz, uz)));
-    float r[kScratchVals];
+    float fneq[kQ];
 #pragma unroll
-    for (int q = 0; q < kQ; ++q) r[q] = rn_sub(fi[q], feq_q_rn(q, rho, ux, uy, uz, usq));
-    r[kScratchValid] = 1.0f;
-    r[kScratchRho] = rho; r[kScratchRho + 1] = ux; r[kScratchRho + 2] = uy; r[kScratchRho + 3] = uz;
-#pragma unroll
-    for (int k = 0; k < kScratchVals / 4; ++k) rec[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+    for (int q = 0; q < kQ; ++q) fneq[q] = rn_sub(fi[q], feq_q_rn(q, rho, ux, uy, uz, usq));
+    ChildRecord<S>::write(rec, fneq, rho, ux, uy, uz);
 }
 
 } // namespace fcfd

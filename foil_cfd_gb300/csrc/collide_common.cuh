@@ -517,7 +517,7 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
     for (int k = 0; k + kSplit < kQ; ++k) fi[k + kSplit] = __shfl_xor_sync(0xffffffffu, acc[k], 1);
     if (!record || !even) return;
     const long long t = lx + static_cast<long long>(cf.rw) * (ly + static_cast<long long>(cf.rh) * blockIdx.z);
-    write_child_record(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t * (kScratchVals / 4));
+    write_child_record<S>(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t * ChildRecord<S>::kVec);
 }
 
 template <class S, bool EXACT>

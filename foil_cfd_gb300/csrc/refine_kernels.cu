@@ -164,7 +164,7 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
 #pragma unroll
                 for (int q = 0; q < kQ; ++q) fi[q] += S::ld(ff + q * fn, c, wgt(q));
             }
-    write_child_record(fi, nFluid, reinterpret_cast<float4*>(scratch) + t * (kScratchVals / 4));
+    write_child_record<S>(fi, nFluid, reinterpret_cast<float4*>(scratch) + t * ChildRecord<S>::kVec);
 }
 
 constexpr int kRestrictTX = 32, kRestrictTY = 2, kRestrictTZ = 2;
@@ -187,16 +187,9 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
                         * (static_cast<unsigned>(yc) + static_cast<unsigned>(g.coarse.ny) * zc);
     if ((ckind[cell] & kFlagMask) != kFluid) return;
     const float4* rec = reinterpret_cast<const float4*>(scratch);
-    constexpr int kRec = kScratchVals / 4;
+    constexpr int kRec = ChildRecord<S>::kVec;
     float fneq[kQ];
-    float4 v4 = __ldg(rec + t * kRec + kScratchValid / 4);  // fneq[16..18], valid
-    if (v4.w == 0.0f) return;
-    fneq[16] = v4.x; fneq[17] = v4.y; fneq[18] = v4.z;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float4 a = __ldg(rec + t * kRec + k);
-        fneq[4 * k] = a.x; fneq[4 * k + 1] = a.y; fneq[4 * k + 2] = a.z; fneq[4 * k + 3] = a.w;
-    }
+    if (!ChildRecord<S>::load(rec + t * kRec, fneq)) return;
 
     const int dEdge = min(min(lx, rw - 1 - lx), min(ly, rh - 1 - ly));
     const float blend = fminf(1.0f, static_cast<float>(dEdge + 1) / static_cast<float>(kRestrictBlend + 1));
@@ -208,22 +201,15 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
         if (nlx < 0 || nlx >= rw || nly < 0 || nly >= rh) continue;
         const int nzw = wrapi(zc + cz(nb), nz);
         const long long tn = nlx + static_cast<long long>(rw) * (nly + static_cast<long long>(rh) * nzw);
-        const float4 last = __ldg(rec + tn * kRec + kScratchValid / 4);
-        if (last.w == 0.0f) continue;
         // Same per-q accumulation order as summing slot by slot.
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float4 a = __ldg(rec + tn * kRec + k);
-            fneq[4 * k] += a.x; fneq[4 * k + 1] += a.y; fneq[4 * k + 2] += a.z; fneq[4 * k + 3] += a.w;
-        }
-        fneq[16] += last.x; fneq[17] += last.y; fneq[18] += last.z;
+        if (!ChildRecord<S>::add(rec + tn * kRec, fneq)) continue;
         ++nStencil;
     }
     const float invS = 1.0f / static_cast<float>(nStencil);
 #pragma unroll
     for (int q = 0; q < kQ; ++q) fneq[q] *= invS;
     regularize(fneq);
-    const float4 m4 = __ldg(rec + t * kRec + kScratchRho / 4);
+    const float4 m4 = ChildRecord<S>::moments(rec + t * kRec);
     const float rho = m4.x, ux = m4.y, uy = m4.z, uz = m4.w;
     const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
     float br = 0.f, bjx = 0.f, bjy = 0.f, bjz = 0.f;
