@@ -23,9 +23,9 @@
 namespace fcfd {
 namespace {
 
-// Register cap: at least 32 resident warps per SM (64 registers).
+// Register cap per storage: S::kBatchThreads resident threads per SM.
 template <class S, bool EXACT, int BX, int ROWS>
-__global__ void __launch_bounds__(BX, 1024 / BX)
+__global__ void __launch_bounds__(BX, S::kBatchThreads / BX)
 batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, unsigned nItems, int parity) {
     using T = typename S::T;
     const unsigned itemEnd = itemBase + nItems;

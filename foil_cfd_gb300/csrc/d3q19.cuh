@@ -114,6 +114,10 @@ struct StoreF32 {
     /// for: 51 registers (the fine-level launch measured 1.7 % faster than
     /// with the compiler's own 56).
     static constexpr int kCellMinBlocks = 10;
+    /// Resident threads per SM the batched collide is compiled for: 64
+    /// registers (the FP16 batched polar measured 15 % slower at 1536
+    /// threads, 40 registers).
+    static constexpr int kBatchThreads = 1024;
     /// Same for the fine collide with the restriction's child sums fused in
     /// (64 registers).
     static constexpr int kChildMinBlocks = 8;
@@ -138,6 +142,7 @@ struct StoreF16 {
     static constexpr int kBytes = 2;
     /// 42 registers: the fine-level launch measured 7 % faster than at 56.
     static constexpr int kCellMinBlocks = 12;
+    static constexpr int kBatchThreads = 1024;
     static constexpr int kChildMinBlocks = 8;
     __device__ __forceinline__ static float ld(const T* __restrict__ p, long long i, float w) {
         return w + __half2float(__ldg(p + i));
