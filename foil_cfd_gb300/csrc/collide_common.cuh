@@ -44,6 +44,42 @@ struct CollideArgs {
     const std::uint32_t* ffMask; // q-LIBB two-node bits [cell]
 };
 
+/// Byte offsets of the pulls of an interior cell (no periodic wrap on any
+/// axis), from the cell's own slot in direction slice 0: pull[q] reaches the
+/// source x - c_q in slice q, slice[q] the cell itself in slice q. Passed as
+/// a __grid_constant__ kernel parameter, so each load and store of such a cell
+/// is one 64-bit add of a constant-bank operand to the cell's base pointer
+/// instead of a wrapped 3-D index and a slice product per direction.
+struct PullOffsets {
+    long long pull[kQ];
+    long long slice[kQ];
+};
+
+template <class T>
+__host__ PullOffsets pull_offsets(int nx, int ny, long long n) {
+    PullOffsets o;
+    const long long sx = nx, sxy = static_cast<long long>(nx) * ny;
+    for (int q = 0; q < kQ; ++q) {
+        o.slice[q] = q * n * static_cast<long long>(sizeof(T));
+        o.pull[q] = (q * n - (cx(q) + sx * cy(q) + sxy * cz(q))) * static_cast<long long>(sizeof(T));
+    }
+    return o;
+}
+
+template <class T>
+__device__ __forceinline__ const T* byte_add(const T* p, long long b) {
+    return reinterpret_cast<const T*>(reinterpret_cast<const char*>(p) + b);
+}
+template <class T>
+__device__ __forceinline__ T* byte_add(T* p, long long b) {
+    return reinterpret_cast<T*>(reinterpret_cast<char*>(p) + b);
+}
+
+/// True when no pull of (x, y, z) wraps around a periodic axis.
+__device__ __forceinline__ bool interior(int x, int y, int z, const CollideArgs& a) {
+    return x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1 && z > 0 && z < a.nz - 1;
+}
+
 // ---- equilibrium in the reference expression order ------------------------
 __device__ __forceinline__ float dot_c(int q, float ux, float uy, float uz) {
     // (cx ux + cy uy) + cz uz with zero terms dropped and +-1 folded.
@@ -248,6 +284,30 @@ __device__ __forceinline__ void gather_bulk(const typename S::T* __restrict__ sr
         f[q] = S::ld(src + q * a.n, b.sx[1 + cx(q)] + unx * (b.sy[1 + cy(q)] + uny * b.sz[1 + cz(q)]), wgt(q));
 }
 
+/// Bulk fluid cell away from the periodic faces: the same 19 pulls through
+/// the constant offsets.
+template <class S>
+__device__ __forceinline__ void gather_interior(const typename S::T* __restrict__ src, const PullOffsets& o,
+                                                unsigned cell, float (&f)[kQ]) {
+    const typename S::T* base = src + cell;
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) f[q] = S::ld(byte_add(base, o.pull[q]), 0, wgt(q));
+}
+
+/// Store the 19 populations of `cell` (slice offsets when given).
+template <class S>
+__device__ __forceinline__ void store_cell(typename S::T* __restrict__ dst, const CollideArgs& a, unsigned cell,
+                                           const float (&f)[kQ], const PullOffsets* o) {
+    if (o) {
+        typename S::T* base = dst + cell;
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) S::st(byte_add(base, o->slice[q]), 0, f[q], wgt(q));
+    } else {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) S::st(dst + q * a.n, cell, f[q], wgt(q));
+    }
+}
+
 /// Near-wall fluid cell: the upstream flag picks the (slot, cell) pair per
 /// link; the wall-model Ladd term 6 w_q (c_q . u_w) on solid links.
 template <class S, bool WM, bool QL = false>
@@ -309,12 +369,27 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
 
 template <class S, bool EXACT>
 __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, const CollideArgs& a, unsigned cell,
-                                            float (&f)[kQ]) {
+                                            float (&f)[kQ], const PullOffsets* o = nullptr) {
     float r, ux, uy, uz;
     collide_body<EXACT>(f, a, r, ux, uy, uz);
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) S::st(dst + q * a.n, cell, f[q], wgt(q));
+    store_cell<S>(dst, a, cell, f, o);
     if (a.writeMacro) { a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz; }
+}
+
+/// The 19 post-streaming populations of fluid cell (x, y, z): bulk cells by
+/// plain pulls (constant offsets away from the periodic faces when `o` is
+/// given), near-wall cells through their neighbours' flags.
+template <class S, bool WM, bool QL>
+__device__ __forceinline__ void gather_fluid(const typename S::T* __restrict__ src,
+                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a,
+                                             std::uint8_t k, unsigned cell, int x, int y, int z, float (&f)[kQ],
+                                             const PullOffsets* o) {
+    if (!(k & kNearWall)) {
+        if (o && interior(x, y, z, a)) gather_interior<S>(src, *o, cell, f);
+        else gather_bulk<S>(src, a, neighbours(x, y, z, a.nx, a.ny, a.nz), f);
+    } else {
+        gather_wall<S, WM, QL>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
+    }
 }
 
 /// One full cell update at (x, y, z): boundary cells by flag, fluid cells
@@ -322,7 +397,7 @@ __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, con
 template <class S, bool WM, bool EXACT, bool QL = false>
 __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a, int x, int y,
-                                            int z) {
+                                            int z, const PullOffsets* o = nullptr) {
     const unsigned cell = static_cast<unsigned>(x)
                         + static_cast<unsigned>(a.nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z);
     const std::uint8_t k = kind[cell];
@@ -331,11 +406,9 @@ __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ sr
         boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
         return;
     }
-    const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
     float f[kQ];
-    if (!(k & kNearWall)) gather_bulk<S>(src, a, b, f);
-    else gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, f);
-    finish_cell<S, EXACT>(dst, a, cell, f);
+    gather_fluid<S, WM, QL>(src, kind, a, k, cell, x, y, z, f, o);
+    finish_cell<S, EXACT>(dst, a, cell, f, o);
 }
 
 // ---- one cell per thread -----------------------------------------------------
@@ -344,10 +417,10 @@ constexpr int kCellBlockX = 128;
 template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kCellBlockX, S::kCellMinBlocks)
 collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
-                    const std::uint8_t* __restrict__ kind, CollideArgs a) {
+                    const std::uint8_t* __restrict__ kind, CollideArgs a, const __grid_constant__ PullOffsets off) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= a.nx) return;
-    collide_one<S, WM, EXACT, QL>(src, dst, kind, a, x, blockIdx.y, blockIdx.z);
+    collide_one<S, WM, EXACT, QL>(src, dst, kind, a, x, blockIdx.y, blockIdx.z, &off);
 }
 
 // ---- warm-restart flag edits (applyFlagEditsKernel, lbm_core.cu:644-717) -----
@@ -443,7 +516,8 @@ constexpr int kSplit = 10;   // directions summed by the even lane
 template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kFuseX, S::kChildMinBlocks)
 collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
-                     const std::uint8_t* __restrict__ kind, CollideArgs a, ChildFuse cf) {
+                     const std::uint8_t* __restrict__ kind, CollideArgs a, ChildFuse cf,
+                     const __grid_constant__ PullOffsets off) {
     const int x = blockIdx.x * kFuseX + threadIdx.x;
     const bool inX = x < a.nx;
     const bool even = (threadIdx.x & 1) == 0;
@@ -466,23 +540,21 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                 const std::uint8_t k = kind[cell];
                 const int flag = k & kFlagMask;
                 if (flag == kFluid) {
-                    const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
-                    if (!(k & kNearWall)) gather_bulk<S>(src, a, b, v);
-                    else gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, v);
+                    gather_fluid<S, WM, QL>(src, kind, a, k, cell, x, y, z, v, &off);
                     float rr, ux, uy, uz;
                     collide_body<EXACT>(v, a, rr, ux, uy, uz);
                     // FP32: the sums see the stored values exactly. FP16:
                     // the collided FP32 values (not their half round trip),
                     // the more accurate child average.
-#pragma unroll
-                    for (int q = 0; q < kQ; ++q) S::st(dst + q * a.n, cell, v[q], wgt(q));
+                    store_cell<S>(dst, a, cell, v, &off);
                     solid = false;
                 } else {
                     boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
                     if (flag != kSolid) {
                         // Written or untouched, the child average sees what dst holds.
+                        const typename S::T* base = dst + cell;
 #pragma unroll
-                        for (int q = 0; q < kQ; ++q) v[q] = S::ld(dst + q * a.n, cell, wgt(q));
+                        for (int q = 0; q < kQ; ++q) v[q] = S::ld(byte_add(base, off.slice[q]), 0, wgt(q));
                         solid = false;
                     }
                 }
@@ -540,12 +612,13 @@ cudaError_t launch_collide_child_impl(const void* srcv, void* dstv, const std::u
     const T* src = static_cast<const T*>(srcv);
     T* dst = static_cast<T*>(dstv);
     const bool ql = a.qFrac != nullptr;
+    const PullOffsets off = pull_offsets<T>(d.nx, d.ny, a.n);
     if (slip.active())
         (ql ? collide_child_kernel<S, true, EXACT, true> : collide_child_kernel<S, true, EXACT, false>)
-            <<<grid, block, 0, st>>>(src, dst, kind, a, cf);
+            <<<grid, block, 0, st>>>(src, dst, kind, a, cf, off);
     else
         (ql ? collide_child_kernel<S, false, EXACT, true> : collide_child_kernel<S, false, EXACT, false>)
-            <<<grid, block, 0, st>>>(src, dst, kind, a, cf);
+            <<<grid, block, 0, st>>>(src, dst, kind, a, cf, off);
     return cudaGetLastError();
 }
 
@@ -844,12 +917,13 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     const int bx = d.nx >= kCellBlockX ? kCellBlockX : ((d.nx + 31) / 32) * 32;
     const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),
                     static_cast<unsigned>(d.nz));
+    const PullOffsets off = pull_offsets<T>(d.nx, d.ny, a.n);
     if (a.qFrac) {
-        if (wm) collide_cell_kernel<S, true, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a);
-        else collide_cell_kernel<S, false, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a);
+        if (wm) collide_cell_kernel<S, true, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a, off);
+        else collide_cell_kernel<S, false, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a, off);
     } else {
-        if (wm) collide_cell_kernel<S, true, EXACT, false><<<grid, bx, 0, st>>>(src, dst, kind, a);
-        else collide_cell_kernel<S, false, EXACT, false><<<grid, bx, 0, st>>>(src, dst, kind, a);
+        if (wm) collide_cell_kernel<S, true, EXACT, false><<<grid, bx, 0, st>>>(src, dst, kind, a, off);
+        else collide_cell_kernel<S, false, EXACT, false><<<grid, bx, 0, st>>>(src, dst, kind, a, off);
     }
     return cudaGetLastError();
 }
