@@ -164,8 +164,9 @@ template <> struct ChildRecord<StoreF16> {
     __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + 3); }
 };
 
-/// Record of a coarse cell from the sum fi of its nFluid fluid children.
-template <class S>
+/// Record of a coarse cell from the sum fi of its nFluid fluid children
+/// (sums of the deviations f - w_q when DEV).
+template <class S, bool DEV = false>
 __device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, float4* rec) {
     if (nFluid == 0) {
         ChildRecord<S>::write_invalid(rec);
@@ -173,7 +174,7 @@ __device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, 
     }
     const float invN = 1.0f / static_cast<float>(nFluid);
 #pragma unroll
-    for (int q = 0; q < kQ; ++q) fi[q] = rn_mul(fi[q], invN);
+    for (int q = 0; q < kQ; ++q) fi[q] = DEV ? rn_mul(fi[q], invN) + wgt(q) : rn_mul(fi[q], invN);
     float rho, ux, uy, uz;
     limited_moments(fi, rho, ux, uy, uz);
     const float usq = rn_mul(1.5f, rn_add(rn_add(rn_mul(ux, ux), rn_mul(uy, uy)), rn_mul(uz, uz)));

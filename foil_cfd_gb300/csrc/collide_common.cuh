@@ -15,9 +15,17 @@
 //    386-467) with zero-coefficient terms skipped (an exact identity). It is
 //    bit-identical to the reference only in a translation unit compiled with
 //    --fmad=false (collide_f32.cu), where no multiply-add is contracted.
-//  * collide_fast: moments, stress and TRT formed from opposite-pair
-//    sums/differences with the equilibrium's second moment in closed form
-//    (rho/3 I + rho u u); fewer instructions, FP32-rounding-level different.
+//  * collide_dev: the same TRT + Smagorinsky update on the deviations
+//    g_q = f_q - w_q (the FP16 storage format), with moments, stress and
+//    TRT formed from opposite-pair sums/differences and the equilibrium's
+//    second moment in closed form (rho/3 I + rho u u); reciprocals and square
+//    roots by the hardware approximations. Fewer instructions, no weight add
+//    per load or subtract per store, FP32-rounding-level different.
+// Population access follows the body: Pop<S, DEV> loads and stores f (exact
+// body) or g (deviation body); a bounce-back or mirrored slot has the weight
+// of the link it replaces and the Ladd and interpolated bounce-back terms are
+// affine with unit coefficient sum, so every gather path is the same in both
+// forms.
 //
 // This header is included by exactly one translation unit per instantiation
 // set; the kernels live in an anonymous namespace.
@@ -78,6 +86,35 @@ __device__ __forceinline__ T* byte_add(T* p, long long b) {
 /// True when no pull of (x, y, z) wraps around a periodic axis.
 __device__ __forceinline__ bool interior(int x, int y, int z, const CollideArgs& a) {
     return x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1 && z > 0 && z < a.nz - 1;
+}
+
+/// Population access in f (DEV false) or deviation g = f - w_q (DEV true).
+template <class S, bool DEV>
+struct Pop {
+    using T = typename S::T;
+    __device__ __forceinline__ static float ld(const T* __restrict__ p, long long i, float w) {
+        if constexpr (DEV) return S::ld_dev(p, i, w);
+        else return S::ld(p, i, w);
+    }
+    __device__ __forceinline__ static void st(T* __restrict__ p, long long i, float v, float w) {
+        if constexpr (DEV) S::st_dev(p, i, v, w);
+        else S::st(p, i, v, w);
+    }
+    __device__ __forceinline__ static float lds(unsigned row, int i, float w) {
+        if constexpr (DEV) return S::lds_dev(row, i, w);
+        else return S::lds(row, i, w);
+    }
+};
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 // ---- equilibrium in the reference expression order ------------------------
@@ -155,22 +192,27 @@ __device__ __forceinline__ void collide_exact(float (&f)[kQ], float tau0, float 
     rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
 }
 
-__device__ __forceinline__ void collide_fast(float (&f)[kQ], float tau0, float lambda, float smagPre,
-                                             float& rhoO, float& uxO, float& uyO, float& uzO) {
+__device__ __forceinline__ void collide_dev(float (&g)[kQ], float tau0, float lambda, float smagPre,
+                                            float& rhoO, float& uxO, float& uyO, float& uzO) {
+    // Pair sums of f are s[p] + 2 w_p, differences d[p] as for f. The
+    // update needs only these (symmetric and antisymmetric parts), so the
+    // pair's own values are not kept.
     float s[10], d[10];
 #pragma unroll
     for (int p = 1; p <= 9; ++p) {
-        s[p] = f[2 * p - 1] + f[2 * p];
-        d[p] = f[2 * p - 1] - f[2 * p];
+        s[p] = g[2 * p - 1] + g[2 * p];
+        d[p] = g[2 * p - 1] - g[2 * p];
     }
     // Pair p has velocity c_{2p-1}: p1 (1,0,0) p2 (0,1,0) p3 (0,0,1)
     // p4 (1,1,0) p5 (1,0,1) p6 (0,1,1) p7 (1,-1,0) p8 (1,0,-1) p9 (0,1,-1).
-    float rho = f[0] + ((s[1] + s[2]) + (s[3] + s[4])) + ((s[5] + s[6]) + (s[7] + s[8])) + s[9];
+    const float dr = g[0] + ((s[1] + s[2]) + (s[3] + s[4])) + ((s[5] + s[6]) + (s[7] + s[8])) + s[9];
     const float jx = (d[1] + d[4]) + (d[5] + d[7]) + d[8];
     const float jy = (d[2] + d[4]) + (d[6] - d[7]) + d[9];
     const float jz = (d[3] + d[5]) + (d[6] - d[8]) - d[9];
-    rho = fmaxf(rho, kRhoFloor);
-    const float inv = __frcp_rn(rho);
+    const bool floored = 1.0f + dr < kRhoFloor;
+    const float rho = floored ? kRhoFloor : 1.0f + dr;
+    const float rm1 = floored ? kRhoFloor - 1.0f : dr;   // rho - 1
+    const float inv = rcp_approx(rho);
     float ux = jx * inv, uy = jy * inv, uz = jz * inv;
     float u2 = ux * ux + uy * uy + uz * uz;
     if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
@@ -178,47 +220,50 @@ __device__ __forceinline__ void collide_fast(float (&f)[kQ], float tau0, float l
         ux *= sc; uy *= sc; uz *= sc;
         u2 = ux * ux + uy * uy + uz * uz;
     }
+    const float rux = rho * ux, ruy = rho * uy;
     float tauEff = tau0;
     if (smagPre > 0.0f) {
-        const float pxx = (s[1] + s[4]) + (s[5] + s[7]) + s[8];
-        const float pyy = (s[2] + s[4]) + (s[6] + s[7]) + s[9];
-        const float pzz = (s[3] + s[5]) + (s[6] + s[8]) + s[9];
-        const float r3 = rho * (1.0f / 3.0f);
-        const float rux = rho * ux, ruy = rho * uy;
-        const float nxx = pxx - r3 - rux * ux;
-        const float nyy = pyy - r3 - ruy * uy;
-        const float nzz = pzz - r3 - rho * uz * uz;
+        // Non-equilibrium stress: the weights' share of the diagonal
+        // (sum of w_q over c_a != 0 = 1/3) cancels against rho/3 up to rho - 1.
+        const float r3 = rm1 * (1.0f / 3.0f);
+        const float nxx = ((s[1] + s[4]) + (s[5] + s[7]) + s[8]) - r3 - rux * ux;
+        const float nyy = ((s[2] + s[4]) + (s[6] + s[7]) + s[9]) - r3 - ruy * uy;
+        const float nzz = ((s[3] + s[5]) + (s[6] + s[8]) + s[9]) - r3 - rho * uz * uz;
         const float nxy = (s[4] - s[7]) - rux * uy;
         const float nxz = (s[5] - s[8]) - rux * uz;
         const float nyz = (s[6] - s[9]) - ruy * uz;
-        const float qbar = sqrtf(nxx * nxx + nyy * nyy + nzz * nzz + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz));
-        tauEff = 0.5f * (tau0 + sqrtf(tau0 * tau0 + smagPre * qbar * inv));
+        const float qbar = sqrt_approx(nxx * nxx + nyy * nyy + nzz * nzz + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz));
+        tauEff = 0.5f * (tau0 + sqrt_approx(tau0 * tau0 + smagPre * qbar * inv));
     }
-    const float omP = __frcp_rn(tauEff);
-    const float omM = __frcp_rn(0.5f + __fdiv_rn(lambda, tauEff - 0.5f));
-    const float base = 1.0f - 1.5f * u2;
-    const float r1 = rho * (1.0f / 18.0f), r2 = rho * (1.0f / 36.0f);
-    f[0] = f[0] - omP * (f[0] - rho * (1.0f / 3.0f) * base);
+    const float omP = rcp_approx(tauEff);
+    const float omM = rcp_approx(0.5f + lambda * rcp_approx(tauEff - 0.5f));
+    // feq_q - w_q = w_q (A + 4.5 rho (c_q.u)^2) + 3 w_q rho (c_q.u), A = rho - 1 - 1.5 rho u^2.
+    const float A = rm1 - 1.5f * rho * u2;
+    const float r45 = 4.5f * rho;
+    g[0] = g[0] - omP * (g[0] - (1.0f / 3.0f) * A);
 #pragma unroll
     for (int p = 1; p <= 9; ++p) {
         const int a = 2 * p - 1;
-        const float wr = p <= 3 ? r1 : r2;
+        const float w = wgt(a);
         const float cu = cx(a) * ux + cy(a) * uy + cz(a) * uz;
-        const float es = wr * (base + 4.5f * cu * cu);
-        const float ea = (3.0f * wr) * cu;
-        const float t1 = omP * (0.5f * s[p] - es);
-        const float t2 = omM * (0.5f * d[p] - ea);
-        f[a] = f[a] - t1 - t2;
-        f[a + 1] = f[a + 1] - t1 + t2;
+        const float es = w * (A + r45 * cu * cu);
+        const float ea = (3.0f * w * rho) * cu;
+        const float hs = 0.5f * s[p], hd = 0.5f * d[p];
+        const float sym = hs - omP * (hs - es);
+        const float asym = hd - omM * (hd - ea);
+        g[a] = sym + asym;
+        g[a + 1] = sym - asym;
     }
     rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
 }
 
+/// The collision of a cell's 19 populations: f with the exact body, the
+/// deviations g with the fast one.
 template <bool EXACT>
 __device__ __forceinline__ void collide_body(float (&f)[kQ], const CollideArgs& a, float& r, float& ux, float& uy,
                                              float& uz) {
     if constexpr (EXACT) collide_exact(f, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
-    else collide_fast(f, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
+    else collide_dev(f, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
 }
 
 // ---- per-cell pieces ---------------------------------------------------------
@@ -275,42 +320,43 @@ __device__ __forceinline__ void boundary_cell(const typename S::T* __restrict__ 
 }
 
 /// Bulk fluid cell: 19 plain pulls from global memory.
-template <class S>
+template <class S, bool DEV>
 __device__ __forceinline__ void gather_bulk(const typename S::T* __restrict__ src, const CollideArgs& a,
                                             const Nbr& b, float (&f)[kQ]) {
     const unsigned unx = a.nx, uny = a.ny;
 #pragma unroll
     for (int q = 0; q < kQ; ++q)
-        f[q] = S::ld(src + q * a.n, b.sx[1 + cx(q)] + unx * (b.sy[1 + cy(q)] + uny * b.sz[1 + cz(q)]), wgt(q));
+        f[q] = Pop<S, DEV>::ld(src + q * a.n, b.sx[1 + cx(q)] + unx * (b.sy[1 + cy(q)] + uny * b.sz[1 + cz(q)]),
+                               wgt(q));
 }
 
 /// Bulk fluid cell away from the periodic faces: the same 19 pulls through
 /// the constant offsets.
-template <class S>
+template <class S, bool DEV>
 __device__ __forceinline__ void gather_interior(const typename S::T* __restrict__ src, const PullOffsets& o,
                                                 unsigned cell, float (&f)[kQ]) {
     const typename S::T* base = src + cell;
 #pragma unroll
-    for (int q = 0; q < kQ; ++q) f[q] = S::ld(byte_add(base, o.pull[q]), 0, wgt(q));
+    for (int q = 0; q < kQ; ++q) f[q] = Pop<S, DEV>::ld(byte_add(base, o.pull[q]), 0, wgt(q));
 }
 
 /// Store the 19 populations of `cell` (slice offsets when given).
-template <class S>
+template <class S, bool DEV>
 __device__ __forceinline__ void store_cell(typename S::T* __restrict__ dst, const CollideArgs& a, unsigned cell,
                                            const float (&f)[kQ], const PullOffsets* o) {
     if (o) {
         typename S::T* base = dst + cell;
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) S::st(byte_add(base, o->slice[q]), 0, f[q], wgt(q));
+        for (int q = 0; q < kQ; ++q) Pop<S, DEV>::st(byte_add(base, o->slice[q]), 0, f[q], wgt(q));
     } else {
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) S::st(dst + q * a.n, cell, f[q], wgt(q));
+        for (int q = 0; q < kQ; ++q) Pop<S, DEV>::st(dst + q * a.n, cell, f[q], wgt(q));
     }
 }
 
 /// Near-wall fluid cell: the upstream flag picks the (slot, cell) pair per
 /// link; the wall-model Ladd term 6 w_q (c_q . u_w) on solid links.
-template <class S, bool WM, bool QL = false>
+template <class S, bool WM, bool QL, bool DEV>
 __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ src,
                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a,
                                             const Nbr& b, unsigned cell, int y, int z, float (&f)[kQ]) {
@@ -318,7 +364,8 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
     const long long n = a.n;
     float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
     bool uwLoaded = false;
-    f[0] = S::ld(src, cell, wgt(0));
+    using P = Pop<S, DEV>;
+    f[0] = P::ld(src, cell, wgt(0));
 #pragma unroll
     for (int q = 1; q < kQ; ++q) {
         const unsigned X = b.sx[1 + cx(q)], Y = b.sy[1 + cy(q)], Z = b.sz[1 + cz(q)];
@@ -331,7 +378,7 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
         const unsigned pZ = X + unx * (Y + uny * static_cast<unsigned>(z));
         const int qs = solid ? opp(q) : (slipY ? mir_y(q) : (slipZ ? mir_z(q) : q));
         const unsigned cs = solid ? cell : (slipY ? pY : (slipZ ? pZ : pn));
-        float fq = S::ld(src + static_cast<long long>(qs) * n, cs, wgt(q));
+        float fq = P::ld(src + static_cast<long long>(qs) * n, cs, wgt(q));
         // Interpolated bounce-back (Bouzidi 2001) on a solid link with an
         // analytic cut fraction, in the reference's expression order
         // (lbm_core.cu:332-364): the wall sits at q = byte/255 of the link.
@@ -339,14 +386,14 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
             const std::uint8_t qb = a.qFrac[static_cast<long long>(cell) * kQ + q];
             if (qb != 0) {
                 const float qf = static_cast<float>(qb) * (1.0f / 255.0f);
-                const float fOut = S::ld(src + static_cast<long long>(q) * n, cell, wgt(q));
+                const float fOut = P::ld(src + static_cast<long long>(q) * n, cell, wgt(q));
                 if (qf >= 0.5f) {
                     const float inv2q = 0.5f / qf;
                     fq = inv2q * fOut + (1.0f - inv2q) * fq;
                 } else if (a.ffMask[cell] & (1u << q)) {
                     // Second fluid node x + c_q (opposite the wall).
                     const unsigned pff = b.sx[1 - cx(q)] + unx * (b.sy[1 - cy(q)] + uny * b.sz[1 - cz(q)]);
-                    const float fOutFF = S::ld(src + static_cast<long long>(q) * n, pff, wgt(q));
+                    const float fOutFF = P::ld(src + static_cast<long long>(q) * n, pff, wgt(q));
                     fq = 2.0f * qf * fOut + (1.0f - 2.0f * qf) * fOutFF;
                 }
                 // else: x + c_q solid (thin vane): keep the half-way value.
@@ -372,23 +419,23 @@ __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, con
                                             float (&f)[kQ], const PullOffsets* o = nullptr) {
     float r, ux, uy, uz;
     collide_body<EXACT>(f, a, r, ux, uy, uz);
-    store_cell<S>(dst, a, cell, f, o);
+    store_cell<S, !EXACT>(dst, a, cell, f, o);
     if (a.writeMacro) { a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz; }
 }
 
 /// The 19 post-streaming populations of fluid cell (x, y, z): bulk cells by
 /// plain pulls (constant offsets away from the periodic faces when `o` is
 /// given), near-wall cells through their neighbours' flags.
-template <class S, bool WM, bool QL>
+template <class S, bool WM, bool QL, bool DEV>
 __device__ __forceinline__ void gather_fluid(const typename S::T* __restrict__ src,
                                              const std::uint8_t* __restrict__ kind, const CollideArgs& a,
                                              std::uint8_t k, unsigned cell, int x, int y, int z, float (&f)[kQ],
                                              const PullOffsets* o) {
     if (!(k & kNearWall)) {
-        if (o && interior(x, y, z, a)) gather_interior<S>(src, *o, cell, f);
-        else gather_bulk<S>(src, a, neighbours(x, y, z, a.nx, a.ny, a.nz), f);
+        if (o && interior(x, y, z, a)) gather_interior<S, DEV>(src, *o, cell, f);
+        else gather_bulk<S, DEV>(src, a, neighbours(x, y, z, a.nx, a.ny, a.nz), f);
     } else {
-        gather_wall<S, WM, QL>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
+        gather_wall<S, WM, QL, DEV>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
     }
 }
 
@@ -407,7 +454,7 @@ __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ sr
         return;
     }
     float f[kQ];
-    gather_fluid<S, WM, QL>(src, kind, a, k, cell, x, y, z, f, o);
+    gather_fluid<S, WM, QL, !EXACT>(src, kind, a, k, cell, x, y, z, f, o);
     finish_cell<S, EXACT>(dst, a, cell, f, o);
 }
 
@@ -540,13 +587,13 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                 const std::uint8_t k = kind[cell];
                 const int flag = k & kFlagMask;
                 if (flag == kFluid) {
-                    gather_fluid<S, WM, QL>(src, kind, a, k, cell, x, y, z, v, &off);
+                    gather_fluid<S, WM, QL, !EXACT>(src, kind, a, k, cell, x, y, z, v, &off);
                     float rr, ux, uy, uz;
                     collide_body<EXACT>(v, a, rr, ux, uy, uz);
                     // FP32: the sums see the stored values exactly. FP16:
                     // the collided FP32 values (not their half round trip),
                     // the more accurate child average.
-                    store_cell<S>(dst, a, cell, v, &off);
+                    store_cell<S, !EXACT>(dst, a, cell, v, &off);
                     solid = false;
                 } else {
                     boundary_cell<S>(src, dst, a, flag, cell, x, y, z);
@@ -554,7 +601,7 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                         // Written or untouched, the child average sees what dst holds.
                         const typename S::T* base = dst + cell;
 #pragma unroll
-                        for (int q = 0; q < kQ; ++q) v[q] = S::ld(byte_add(base, off.slice[q]), 0, wgt(q));
+                        for (int q = 0; q < kQ; ++q) v[q] = Pop<S, !EXACT>::ld(byte_add(base, off.slice[q]), 0, wgt(q));
                         solid = false;
                     }
                 }
@@ -589,7 +636,7 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
     for (int k = 0; k + kSplit < kQ; ++k) fi[k + kSplit] = __shfl_xor_sync(0xffffffffu, acc[k], 1);
     if (!record || !even) return;
     const long long t = lx + static_cast<long long>(cf.rw) * (ly + static_cast<long long>(cf.rh) * blockIdx.z);
-    write_child_record<S>(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t * ChildRecord<S>::kVec);
+    write_child_record<S, !EXACT>(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t * ChildRecord<S>::kVec);
 }
 
 template <class S, bool EXACT>
@@ -806,10 +853,10 @@ collide_staged_kernel(const typename S::T* __restrict__ src, typename S::T* __re
                 const int xs[3] = {wrap_inc(x, nx), x, wrap_dec(x, nx)};
                 const unsigned rowBytes = static_cast<unsigned>(nx) * sizeof(T);
 #pragma unroll
-                for (int q = 0; q < kQ; ++q) f[q] = S::lds(sbase + q * rowBytes, xs[1 + cx(q)], wgt(q));
+                for (int q = 0; q < kQ; ++q) f[q] = Pop<S, !EXACT>::lds(sbase + q * rowBytes, xs[1 + cx(q)], wgt(q));
             } else {
                 const Nbr b = neighbours(x, y, z, nx, a.ny, a.nz);
-                gather_wall<S, WM, QL>(src, kind, a, b, cell, y, z, f);
+                gather_wall<S, WM, QL, !EXACT>(src, kind, a, b, cell, y, z, f);
             }
             finish_cell<S, EXACT>(dst, a, cell, f);
         }

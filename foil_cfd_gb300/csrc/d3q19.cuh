@@ -136,6 +136,14 @@ struct StoreF32 {
         asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(row + 4u * static_cast<unsigned>(i)));
         return v;
     }
+    /// Deviation forms g = f - w_q of ld / st / lds.
+    __device__ __forceinline__ static float ld_dev(const T* __restrict__ p, long long i, float w) {
+        return __ldg(p + i) - w;
+    }
+    __device__ __forceinline__ static void st_dev(T* __restrict__ p, long long i, float g, float w) {
+        p[i] = g + w;
+    }
+    __device__ __forceinline__ static float lds_dev(unsigned row, int i, float w) { return lds(row, i, w) - w; }
 };
 struct StoreF16 {
     using T = __half;
@@ -152,9 +160,19 @@ struct StoreF16 {
     }
     __device__ __forceinline__ static float rt(float v, float w) { return w + __half2float(__float2half_rn(v - w)); }
     __device__ __forceinline__ static float lds(unsigned row, int i, float w) {
+        return w + lds_dev(row, i, w);
+    }
+    /// The stored deviation itself: no weight add on load or subtract on store.
+    __device__ __forceinline__ static float ld_dev(const T* __restrict__ p, long long i, float) {
+        return __half2float(__ldg(p + i));
+    }
+    __device__ __forceinline__ static void st_dev(T* __restrict__ p, long long i, float g, float) {
+        p[i] = __float2half_rn(g);
+    }
+    __device__ __forceinline__ static float lds_dev(unsigned row, int i, float) {
         unsigned short h;
         asm volatile("ld.shared.u16 %0, [%1];" : "=h"(h) : "r"(row + 2u * static_cast<unsigned>(i)));
-        return w + __half2float(__ushort_as_half(h));
+        return __half2float(__ushort_as_half(h));
     }
 };
 
