@@ -62,7 +62,11 @@ __device__ __forceinline__ void regularize(float (&fneq)[kQ]) {
 }
 
 
-template <class S>
+/// BLEND false: a time weight of 0, where s0 + 0 (s1 - s0) is s0 itself
+/// (the sign of a zero sum aside, for which s1 is read), so the second time
+/// level is not read. Identical to the blended form whenever the second
+/// level is finite.
+template <class S, bool BLEND>
 __global__ void __launch_bounds__(kRefineBlock)
 fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restrict__ cT1,
             const std::uint8_t* __restrict__ ckind, typename S::T* __restrict__ ff,
@@ -115,12 +119,23 @@ fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restri
 #pragma unroll
     for (int q = 0; q < kQ; ++q) {
         float s0 = 0.0f, s1 = 0.0f;
+        if constexpr (BLEND) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            s0 += w8[c] * S::ld(cT0 + q * cn, corner[c], wgt(q));
-            s1 += w8[c] * S::ld(cT1 + q * cn, corner[c], wgt(q));
+            for (int c = 0; c < 8; ++c) {
+                s0 += w8[c] * S::ld(cT0 + q * cn, corner[c], wgt(q));
+                s1 += w8[c] * S::ld(cT1 + q * cn, corner[c], wgt(q));
+            }
+            fi[q] = s0 + tw * (s1 - s0);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) s0 += w8[c] * S::ld(cT0 + q * cn, corner[c], wgt(q));
+            if (s0 == 0.0f) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) s1 += w8[c] * S::ld(cT1 + q * cn, corner[c], wgt(q));
+                s0 = s0 + tw * (s1 - s0);
+            }
+            fi[q] = s0;
         }
-        fi[q] = s0 + tw * (s1 - s0);
     }
     float rho, ux, uy, uz;
     limited_moments(fi, rho, ux, uy, uz);
@@ -246,12 +261,13 @@ cudaError_t launch_fill_c2f(Storage s, const void* cT0, const void* cT1,
     if (count <= 0) return cudaSuccess;
     const unsigned nb = static_cast<unsigned>((count + kRefineBlock - 1) / kRefineBlock);
     const float invF = 1.0f / static_cast<float>(g.factor);
+    const bool blend = timeWeight != 0.0f;
     if (s == Storage::F32)
-        fill_kernel<StoreF32><<<nb, kRefineBlock, 0, st>>>(
+        (blend ? fill_kernel<StoreF32, true> : fill_kernel<StoreF32, false>)<<<nb, kRefineBlock, 0, st>>>(
             static_cast<const float*>(cT0), static_cast<const float*>(cT1), coarseKind,
             static_cast<float*>(fineF), targets, count, g, invF, timeWeight, neqScale);
     else
-        fill_kernel<StoreF16><<<nb, kRefineBlock, 0, st>>>(
+        (blend ? fill_kernel<StoreF16, true> : fill_kernel<StoreF16, false>)<<<nb, kRefineBlock, 0, st>>>(
             static_cast<const __half*>(cT0), static_cast<const __half*>(cT1), coarseKind,
             static_cast<__half*>(fineF), targets, count, g, invF, timeWeight, neqScale);
     return cudaGetLastError();

@@ -567,7 +567,8 @@ struct fcfd_solver {
         restrict_sub_box(g, cf.rx0, cf.ry0, cf.rw, cf.rh);
         cudaEvent_t e2 = collideTiming
                              ? fuseT.begin(static_cast<double>(L.n),
-                                           L.collideBytes(storage) + 96.0 * static_cast<double>(cf.rw) * cf.rh * g.coarse.nz,
+                                           L.collideBytes(storage) + (storage == Storage::F32 ? 96.0 : 64.0)
+                                                   * static_cast<double>(cf.rw) * cf.rh * g.coarse.nz,
                                            stream)
                              : nullptr;
         ++launches;
