@@ -37,6 +37,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 namespace fcfd {
 namespace {
 
@@ -103,6 +105,12 @@ struct Pop {
     __device__ __forceinline__ static float lds(unsigned row, int i, float w) {
         if constexpr (DEV) return S::lds_dev(row, i, w);
         else return S::lds(row, i, w);
+    }
+    /// Coherent load, for a slot this kernel may have written.
+    __device__ __forceinline__ static float ld_coherent(const T* p, float w) {
+        const float v = static_cast<float>(*p);
+        if constexpr (DEV) return std::is_same_v<T, float> ? v - w : v;
+        else return std::is_same_v<T, float> ? v : w + v;
     }
 };
 
@@ -601,7 +609,8 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
                         // Written or untouched, the child average sees what dst holds.
                         const typename S::T* base = dst + cell;
 #pragma unroll
-                        for (int q = 0; q < kQ; ++q) v[q] = Pop<S, !EXACT>::ld(byte_add(base, off.slice[q]), 0, wgt(q));
+                        for (int q = 0; q < kQ; ++q)
+                            v[q] = Pop<S, !EXACT>::ld_coherent(byte_add(base, off.slice[q]), wgt(q));
                         solid = false;
                     }
                 }
