@@ -241,7 +241,12 @@ struct fcfd_solver {
     int nanKind = 0;
     bool wmEnabled = false;
     bool zSlipWalls = false;
-    bool fuseChild = true;              // child averages fused into the last fine sub-step
+    // Child averages fused into the last fine sub-step: -1 by storage (FP32
+    // fused: 3.73 vs 3.86 ms per config-3 step; FP16 separate: 3.02 vs 3.10
+    // ms, its issue-bound collide pays more for the fused sums than the
+    // separate pass's 1.6 GB re-read costs), 0 separate, 1 fused.
+    int fuseChild = -1;
+    bool fuseOn() const { return fuseChild < 0 ? storage == Storage::F32 : fuseChild != 0; }
     int wallMethod = 0;                 // FCFD_UTAU_* solve of the wall updates
     std::uint16_t* dNetW = nullptr;     // learned seed: solver-owned BF16 weights
     wallnet::NetDev netView{};
@@ -621,7 +626,7 @@ struct fcfd_solver {
                 // Factor 2: the last sub-step's collide also forms the
                 // restriction's child averages (no re-read of the fine level)
                 // -- unless a finer level rewrites the fine state after it.
-                const bool fuse = fuseChild && m == 2 && !finerActive;
+                const bool fuse = fuseOn() && m == 2 && !finerActive;
                 for (int k = 0; k < m; ++k) {
                     ++launches;
                     if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src],
@@ -641,7 +646,7 @@ struct fcfd_solver {
                         const float tr = fineTau(tf, m2);
                         CollideParams rp = fp;
                         rp.tau = tr;
-                        const bool fuseR = fuseChild && m2 == 2;
+                        const bool fuseR = fuseOn() && m2 == 2;
                         for (int q = 0; q < m2; ++q) {
                             ++launches;
                             if (auto e = launch_fill_c2f(storage, fine.f[fine.src], fine.f[1 - fine.src], fine.kind,
@@ -1601,7 +1606,7 @@ int fcfd_wall_update_timed(fcfd_solver* s, int level, int reps, float* ms, fcfd_
 
 int fcfd_set_fused_restriction(fcfd_solver* s, int enabled) {
     if (!s) return cudaErrorInvalidValue;
-    s->fuseChild = enabled != 0;
+    s->fuseChild = enabled < 0 ? -1 : (enabled != 0 ? 1 : 0);
     return 0;
 }
 

@@ -304,9 +304,11 @@ int fcfd_refinement_info(const fcfd_solver* s, fcfd_refine_info* out);
 int fcfd_import_fine_f32(fcfd_solver* s, const float* host_f, size_t count);
 int fcfd_export_fine_f32(fcfd_solver* s, float* host_f, size_t count);
 /* Factor-2 patches: form the restriction's child averages inside the last
- * fine sub-step's collide (default 1) instead of re-reading the fine level
- * (lbm_refine.cu:274-429 reads it in the restriction). Both settings give
- * the same populations bit for bit; 0 is kept for that comparison. */
+ * fine sub-step's collide (1) instead of re-reading the fine level in a
+ * separate pass (0; lbm_refine.cu:274-429 reads it in the restriction).
+ * Negative (the default): 1 with FP32 storage, 0 with FP16, the faster of
+ * the two for each. With FP32 storage both give the same populations bit
+ * for bit. */
 int fcfd_set_fused_restriction(fcfd_solver* s, int enabled);
 
 /* ---- nested finer level (lbm_solver.h:118-124, 207-243) ----------------- */

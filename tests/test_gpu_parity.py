@@ -371,6 +371,28 @@ def test_error_behaviour(fc):
         s.import_f32(np.zeros(5, np.float32))
 
 
+@pytest.mark.parametrize("storage,fused_default", [("fp32", True), ("fp16", False)])
+def test_fused_restriction_default_by_storage(fc, storage, fused_default):
+    """The default restriction path is the faster one per storage: the child
+    averages fused into the last fine sub-step with FP32 storage, the
+    separate pass with FP16; an explicit setting overrides it."""
+    from foil_cfd_gb300.tunnels import airfoil_tunnel
+    t = airfoil_tunnel(160, 64, 16, chord=64, aoa=6.0)
+    s = fc.LBMSolver()
+    s.init(t.dims, fc.scaling_direct(0.52, t.u_lat, t.chord_cells), t.flags, storage=storage, les_cs=0.1)
+    s.set_startup_ramp_enabled(False)
+    s.reset()
+    s.init_refinement(t.box, t.factor, t.fine_flags)
+    s.enable_collide_timing(True)
+    assert s.step_n(4) == 0
+    assert (s.fused_collide_time_ms()[1] > 0) == fused_default
+    s.set_fused_restriction(not fused_default)
+    s.enable_collide_timing(False)
+    s.enable_collide_timing(True)
+    assert s.step_n(4) == 0
+    assert (s.fused_collide_time_ms()[1] > 0) == (not fused_default)
+
+
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
 def test_fused_child_average_equals_separate_pass(fc, storage):
     """The last fine sub-step's collide with the restriction's child averages
