@@ -128,6 +128,8 @@ _SIGS = {
     "fcfd_f_bytes": (C.c_size_t, [P]),
     "fcfd_notify_restored": (None, [P, C.c_int]),
     "fcfd_import_f32": (C.c_int, [P, P, C.c_size_t]),
+    "fcfd_stage_f32": (C.c_int, [P, C.c_int, P, C.c_size_t]),
+    "fcfd_commit_staged": (C.c_int, [P]),
     "fcfd_export_f32": (C.c_int, [P, P, C.c_size_t]),
     "fcfd_restore_from_macro": (C.c_int, [P, P, P, P, P]),
     "fcfd_perf_stats": (C.c_int, [P, C.POINTER(Perf)]),

@@ -190,6 +190,14 @@ struct fcfd_solver {
     Level coarse;
     Level fine;
     bool fineActive = false;
+    // ---- staged FP32 import (fcfd_stage_f32 / fcfd_commit_staged) ----
+    struct Staged {
+        float* buf = nullptr;   // FP32 SoA of one level
+        size_t bytes = 0;
+        bool pending = false;
+    } staged[3];
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evStaged = nullptr, evCommitted = nullptr;
     int factor = 2;
     fcfd_patch_box box{};
     fcfd_scaling fineScaling{};
@@ -526,8 +534,83 @@ struct fcfd_solver {
         forcesFromFine = false;
     }
 
+    void freeStaged() {
+        if (copyStream) cudaStreamSynchronize(copyStream);
+        for (Staged& st : staged) {
+            dfree(st.buf);
+            st = Staged{};
+        }
+        for (cudaEvent_t* e : {&evStaged, &evCommitted})
+            if (*e) { cudaEventDestroy(*e); *e = nullptr; }
+        if (copyStream) { cudaStreamDestroy(copyStream); copyStream = nullptr; }
+    }
+
+    Level* levelAt(int level) {
+        if (level == 0) return &coarse;
+        if (level == 1 && fineActive) return &fine;
+        if (level == 2 && finerActive) return &finer;
+        return nullptr;
+    }
+
+    /// Queue the host -> device copy of one level's FP32 SoA state into its
+    /// staging buffer on the copy stream.
+    cudaError_t stageF32(int level, const float* host, size_t count) {
+        Level* L = levelAt(level);
+        if (!L || !host || count != static_cast<size_t>(L->n) * 19) return cudaErrorInvalidValue;
+        if (!copyStream) {
+            if (auto e = cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking); e != cudaSuccess) return e;
+            if (auto e = cudaEventCreateWithFlags(&evStaged, cudaEventDisableTiming); e != cudaSuccess) return e;
+            if (auto e = cudaEventCreateWithFlags(&evCommitted, cudaEventDisableTiming); e != cudaSuccess) return e;
+        }
+        Staged& st = staged[level];
+        const size_t bytes = count * sizeof(float);
+        if (st.bytes != bytes) {
+            cudaStreamSynchronize(copyStream);
+            dfree(st.buf);
+            st.bytes = 0;
+            if (auto e = cudaMalloc(&st.buf, bytes); e != cudaSuccess) return e;
+            st.bytes = bytes;
+        }
+        // A commit still reading the staging buffers finishes first.
+        if (auto e = cudaStreamWaitEvent(copyStream, evCommitted, 0); e != cudaSuccess) return e;
+        if (auto e = cudaMemcpyAsync(st.buf, host, bytes, cudaMemcpyHostToDevice, copyStream); e != cudaSuccess)
+            return e;
+        if (auto e = cudaEventRecord(evStaged, copyStream); e != cudaSuccess) return e;
+        st.pending = true;
+        return cudaSuccess;
+    }
+
+    /// The staged levels become the current state, ordered on the solver
+    /// stream after their copies.
+    cudaError_t commitStaged() {
+        bool any = false, coarseDone = false;
+        for (const Staged& st : staged) any |= st.pending;
+        if (!any) return cudaErrorNotReady;
+        if (auto e = cudaStreamWaitEvent(stream, evStaged, 0); e != cudaSuccess) return e;
+        for (int level = 0; level < 3; ++level) {
+            Staged& st = staged[level];
+            if (!st.pending) continue;
+            st.pending = false;
+            Level* L = levelAt(level);
+            if (!L || st.bytes != static_cast<size_t>(L->n) * 19 * sizeof(float)) return cudaErrorInvalidValue;
+            cudaError_t e;
+            if (storage == Storage::F32) {
+                e = cudaMemcpyAsync(L->f[L->src], st.buf, st.bytes, cudaMemcpyDeviceToDevice, stream);
+            } else {
+                ++launches;
+                e = launch_f32_to_store(storage, st.buf, L->f[L->src], L->n, stream);
+            }
+            if (e != cudaSuccess) return e;
+            coarseDone |= level == 0;
+        }
+        if (auto e = cudaEventRecord(evCommitted, stream); e != cudaSuccess) return e;
+        if (coarseDone) notifyRestored(true);
+        return cudaSuccess;
+    }
+
     void freeAll() {
         if (stream) cudaStreamSynchronize(stream);
+        freeStaged();
         freeFine();
         coarse.free_all();
         dfree(rho); dfree(u); dfree(v); dfree(w); dfree(dForce); dfree(dNan); dfree(dStatus);
@@ -1131,6 +1214,16 @@ int fcfd_import_f32(fcfd_solver* s, const float* f, size_t count) {
     if (auto e = s->importF32(s->coarse, f, count); e != cudaSuccess) return e;
     s->notifyRestored(true);
     return 0;
+}
+
+int fcfd_stage_f32(fcfd_solver* s, int level, const float* f, size_t count) {
+    if (!s || !s->initialized) return cudaErrorInvalidValue;
+    return s->stageF32(level, f, count);
+}
+
+int fcfd_commit_staged(fcfd_solver* s) {
+    if (!s || !s->initialized) return cudaErrorInvalidValue;
+    return s->commitStaged();
 }
 
 int fcfd_export_f32(fcfd_solver* s, float* f, size_t count) {

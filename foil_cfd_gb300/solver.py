@@ -206,6 +206,21 @@ class LBMSolver:
         if rc:
             raise SolverError(f"import failed ({rc})")
 
+    def stage_f32(self, level: int, f: np.ndarray):
+        """Queue the copy of one level's FP32 SoA state (0 coarse, 1 fine,
+        2 finer) on the solver's copy stream; `f` (float32, contiguous,
+        ideally a PinnedArray's array) must stay alive until commit_staged."""
+        if f.dtype != np.float32 or not f.flags["C_CONTIGUOUS"]:
+            raise SolverError("stage_f32 needs a contiguous float32 array that outlives the commit")
+        rc = self._lib.fcfd_stage_f32(self._h, int(level), ptr(f), f.size)
+        if rc:
+            raise SolverError(f"stage failed ({rc})")
+
+    def commit_staged(self) -> int:
+        """Make the staged levels the current state (0, or cudaErrorNotReady
+        when nothing is staged)."""
+        return self._lib.fcfd_commit_staged(self._h)
+
     def export_f32(self) -> np.ndarray:
         f = np.empty(Q * self.ncells, np.float32)
         rc = self._lib.fcfd_export_f32(self._h, ptr(f), f.size)

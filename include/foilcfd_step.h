@@ -237,6 +237,20 @@ void fcfd_notify_restored(fcfd_solver* s, int full_state);
  * tests/lbm_test_util.h:116-204). Import calls fcfd_notify_restored(s, 1). */
 int fcfd_import_f32(fcfd_solver* s, const float* host_f, size_t count);
 int fcfd_export_f32(fcfd_solver* s, float* host_f, size_t count);
+/* Two-phase FP32 import, so that the host copy of the next state overlaps
+ * the stepping of the current one (no reference counterpart: the reference
+ * restores with blocking copies). fcfd_stage_f32 queues the host -> device
+ * copy of one level's FP32 SoA state (level 0 coarse, 1 fine, 2 finer;
+ * 19*ncells floats, pinned host memory for the copy to be asynchronous) into
+ * a device staging buffer on a copy stream of the solver's own; the host
+ * buffer must stay valid until the commit. fcfd_commit_staged orders the
+ * solver stream after the staged copies and makes them the levels' current
+ * state: the same state as fcfd_import_f32 / fcfd_import_fine_f32 /
+ * fcfd_import_finer_f32 of that data (with fcfd_notify_restored(s, 1) when
+ * the coarse level was staged). A stage issued after a commit waits for the
+ * commit to have read the staging buffer. cudaErrorNotReady: nothing staged. */
+int fcfd_stage_f32(fcfd_solver* s, int level, const float* host_f, size_t count);
+int fcfd_commit_staged(fcfd_solver* s);
 /* restoreFromMacroscopic (lbm_solver.cpp:1773-1803), host arrays. */
 int fcfd_restore_from_macro(fcfd_solver* s, const float* rho, const float* u,
                             const float* v, const float* w);

@@ -371,6 +371,49 @@ def test_error_behaviour(fc):
         s.import_f32(np.zeros(5, np.float32))
 
 
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_staged_import_equals_import(fc, storage):
+    """fcfd_stage_f32 + fcfd_commit_staged give the state fcfd_import_f32 /
+    fcfd_import_fine_f32 give, with steps run between the stage and the
+    commit (the copy overlaps them); a commit with nothing staged is
+    cudaErrorNotReady."""
+    from foil_cfd_gb300.solver import PinnedArray
+    from foil_cfd_gb300.tunnels import airfoil_tunnel
+    t = airfoil_tunnel(160, 64, 16, chord=64, aoa=6.0)
+
+    def make():
+        s = fc.LBMSolver()
+        s.init(t.dims, fc.scaling_direct(0.52, t.u_lat, t.chord_cells), t.flags, storage=storage, les_cs=0.1)
+        s.set_startup_ramp_enabled(False)
+        s.reset()
+        s.init_refinement(t.box, t.factor, t.fine_flags)
+        return s
+
+    a = make()
+    assert a.commit_staged() == 600
+    assert a.step_n(5) == 0
+    kept = [PinnedArray(19 * int(np.prod(d))) for d in (t.dims, t.fine_dims)]
+    kept[0].array[:] = a.export_f32()
+    kept[1].array[:] = a.export_fine_f32()
+    assert a.step_n(5) == 0
+    a.stage_f32(0, kept[0].array)
+    a.stage_f32(1, kept[1].array)
+    assert a.step_n(3) == 0
+    assert a.commit_staged() == 0
+    assert a.commit_staged() == 600
+    b = make()
+    assert b.step_n(2) == 0
+    b.import_f32(kept[0].array)
+    b.import_fine_f32(kept[1].array)
+    assert np.array_equal(a.export_f32(), b.export_f32())
+    assert np.array_equal(a.export_fine_f32(), b.export_fine_f32())
+    assert a.step_n(4) == 0 and b.step_n(4) == 0
+    assert np.array_equal(a.export_f32(), b.export_f32())
+    assert np.array_equal(a.export_fine_f32(), b.export_fine_f32())
+    for k in kept:
+        k.close()
+
+
 @pytest.mark.parametrize("storage,fused_default", [("fp32", True), ("fp16", False)])
 def test_fused_restriction_default_by_storage(fc, storage, fused_default):
     """The default restriction path is the faster one per storage: the child
