@@ -30,6 +30,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 namespace fcfd {
 namespace {
 
@@ -116,10 +118,22 @@ fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restri
 
     const long long cn = g.coarse.cells(), fn = g.fine.cells();
     float fi[kQ];
+    // FP16 storage sums the stored deviations and adds w_q once: with the
+    // corner weights summing to one, sum w8 (w_q + g) = w_q + sum w8 g up to
+    // rounding, without a weight add per corner load. FP32 keeps the
+    // reference's expression.
+    constexpr bool kDev = std::is_same_v<S, StoreF16>;
 #pragma unroll
     for (int q = 0; q < kQ; ++q) {
         float s0 = 0.0f, s1 = 0.0f;
-        if constexpr (BLEND) {
+        if constexpr (kDev) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                s0 += w8[c] * S::ld_dev(cT0 + q * cn, corner[c], wgt(q));
+                if constexpr (BLEND) s1 += w8[c] * S::ld_dev(cT1 + q * cn, corner[c], wgt(q));
+            }
+            fi[q] = wgt(q) + (BLEND ? s0 + tw * (s1 - s0) : s0);
+        } else if constexpr (BLEND) {
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 s0 += w8[c] * S::ld(cT0 + q * cn, corner[c], wgt(q));
