@@ -381,6 +381,10 @@ class LBMSolver:
             raise SolverError(f"finer import failed ({rc})")
 
     def set_fused_restriction(self, enabled: bool):
+        """Form the restriction's child averages inside the last fine
+        sub-step's collide (True) or in a separate pass (False). Until called,
+        the faster one per storage is used: fused with FP32, separate with
+        FP16."""
         self._lib.fcfd_set_fused_restriction(self._h, int(enabled))
 
     def shutdown_refinement(self):
