@@ -44,6 +44,7 @@ constexpr int kTileCells = kTileThreads * kTileRun;
 /// Periodic index for any offset (a sample search can step several
 /// periods on a thin span); equals the single wrap wherever that is in range.
 __device__ __forceinline__ int wrapi(int v, int n) {
+    if (static_cast<unsigned>(v) < static_cast<unsigned>(n)) return v;
     const int r = v % n;
     return r < 0 ? r + n : r;
 }
@@ -242,7 +243,9 @@ struct ForceLinkPred {
 #pragma unroll
         for (int q = 1; q < kQ; ++q) {
             const int X = wrapi(x + cx(q), g.nx), Y = wrapi(y + cy(q), g.ny), Z = wrapi(z + cz(q), g.nz);
-            if (f[X + static_cast<long long>(g.nx) * (Y + static_cast<long long>(g.ny) * Z)] == kSolidB) m |= 1u << q;
+            const unsigned nb = static_cast<unsigned>(X)
+                              + static_cast<unsigned>(g.nx) * (static_cast<unsigned>(Y) + static_cast<unsigned>(g.ny) * Z);
+            if (f[nb] == kSolidB) m |= 1u << q;
         }
         return m;
     }
@@ -272,17 +275,23 @@ struct FlagNePred {     // flag != value (non-solid seed list)
     }
 };
 
-// Wall-model cell list (wall_model.cpp:55-236).
-struct WallPred {
+// Wall-model cell list (wall_model.cpp:55-236), in two compactions so that
+// the 5^3 occupancy gradient runs one candidate per thread instead of on
+// the one lane of a warp that meets a wall cell:
+//  1. WallCandPred over the lattice: fluid cells with a pull link that is
+//     solid in the active field and none that is solid only there (a vane
+//     link: the cell is excluded and counted);
+//  2. WallListPred over the candidate list: the gradient normal (degenerate
+//     ones dropped and counted), the sample cell along it, the entry.
+// Both compactions keep order, so the entries are in ascending cell order,
+// as the host builder's.
+struct WallGeom {
     Grid3 g;
     const std::uint8_t* active;
     const std::uint8_t* clean;
-    int sampleCells;
-    std::uint32_t *cell, *sample, *mask;
-    float *nX, *nY, *nZ, *ys;
-
-    __device__ __forceinline__ long long at(int x, int y, int z) const {
-        return x + static_cast<long long>(g.nx) * (y + static_cast<long long>(g.ny) * z);
+    __device__ __forceinline__ unsigned at(int x, int y, int z) const {
+        return static_cast<unsigned>(x) + static_cast<unsigned>(g.nx) * (static_cast<unsigned>(y)
+                                                                         + static_cast<unsigned>(g.ny) * z);
     }
     // Solid with x/y out of range = not solid, z periodic.
     __device__ __forceinline__ bool solid(const std::uint8_t* f, int x, int y, int z) const {
@@ -293,6 +302,7 @@ struct WallPred {
         gx = gy = gz = 0.0f;
         for (int dz = -2; dz <= 2; ++dz)
             for (int dy = -2; dy <= 2; ++dy)
+#pragma unroll
                 for (int dx = -2; dx <= 2; ++dx)
                     if (solid(clean, x + dx, y + dy, z + dz)) {
                         gx += static_cast<float>(dx);
@@ -300,58 +310,93 @@ struct WallPred {
                         gz += static_cast<float>(dz);
                     }
     }
-    // 0 = not listed; otherwise the link mask. stats (count pass only):
-    // [0] listed, [1] vane-excluded, [2] degenerate normal.
+};
+
+struct WallCandPred {
+    WallGeom w;
+    std::uint32_t *cells, *masks;
+    // 0 = not a candidate; otherwise the link mask. stats (count pass only):
+    // [1] vane-excluded.
     __device__ std::uint32_t eval(long long c, int x, int y, int z, int* stats) const {
-        if (active[c] != kFluidB) return 0;
+        if (w.active[c] != kFluidB) return 0;
         std::uint32_t m = 0;
         bool vgOnly = false;
 #pragma unroll
         for (int q = 1; q < kQ; ++q) {
             const int sx = x - cx(q), sy = y - cy(q), sz = z - cz(q);
-            if (!solid(active, sx, sy, sz)) continue;
+            if (!w.solid(w.active, sx, sy, sz)) continue;
             m |= 1u << q;
-            if (!solid(clean, sx, sy, sz)) vgOnly = true;
+            if (!w.solid(w.clean, sx, sy, sz)) vgOnly = true;
         }
         if (m == 0) return 0;
         if (vgOnly) {
             if (stats) atomicAdd(stats + 1, 1);
             return 0;
         }
+        return m;
+    }
+    __device__ void emit(long long slot, long long c, int, int, int, std::uint32_t m) const {
+        cells[slot] = static_cast<std::uint32_t>(c);
+        masks[slot] = m;
+    }
+};
+
+struct WallListPred {
+    WallGeom w;
+    int sampleCells;
+    const std::uint32_t *candCell, *candMask;
+    std::uint32_t *cell, *sample, *mask;
+    float *nX, *nY, *nZ, *ys;
+
+    __device__ __forceinline__ void decode(std::uint32_t c, int& x, int& y, int& z) const {
+        const unsigned nxy = static_cast<unsigned>(w.g.nx) * static_cast<unsigned>(w.g.ny);
+        z = static_cast<int>(c / nxy);
+        const unsigned r = c - static_cast<unsigned>(z) * nxy;
+        y = static_cast<int>(r / static_cast<unsigned>(w.g.nx));
+        x = static_cast<int>(r - static_cast<unsigned>(y) * static_cast<unsigned>(w.g.nx));
+    }
+    // i = candidate index. 0 = dropped; otherwise the link mask. stats
+    // (count pass only): [0] listed, [2] degenerate normal.
+    __device__ std::uint32_t eval(long long i, int, int, int, int* stats) const {
+        int x, y, z;
+        decode(candCell[i], x, y, z);
         float gx, gy, gz;
-        gradient(x, y, z, gx, gy, gz);
+        w.gradient(x, y, z, gx, gy, gz);
         const float gm = sqrtf(gx * gx + gy * gy + gz * gz);
         if (gm < 1e-3f) {
             if (stats) atomicAdd(stats + 2, 1);
             return 0;
         }
         if (stats) atomicAdd(stats + 0, 1);
-        return m;
+        return candMask[i];
     }
-    __device__ void emit(long long slot, long long c, int x, int y, int z, std::uint32_t m) const {
+    __device__ void emit(long long slot, long long i, int, int, int, std::uint32_t m) const {
+        const std::uint32_t c = candCell[i];
+        int x, y, z;
+        decode(c, x, y, z);
         float gx, gy, gz;
-        gradient(x, y, z, gx, gy, gz);
+        w.gradient(x, y, z, gx, gy, gz);
         const float gm = sqrtf(gx * gx + gy * gy + gz * gz);
         const float nx_ = -gx / gm, ny_ = -gy / gm, nz_ = -gz / gm;
-        long long s = c;
+        std::uint32_t s = c;
         int sx = x, sy = y, sz = z;
         for (int k = sampleCells; k >= 1; --k) {
             const int tx = x + static_cast<int>(lroundf(nx_ * static_cast<float>(k)));
             const int ty = y + static_cast<int>(lroundf(ny_ * static_cast<float>(k)));
-            const int tz = wrapi(z + static_cast<int>(lroundf(nz_ * static_cast<float>(k))), g.nz);
-            if (tx < 0 || tx >= g.nx || ty < 0 || ty >= g.ny) continue;
-            const long long cand = at(tx, ty, tz);
-            if (active[cand] != kFluidB) continue;
+            const int tz = wrapi(z + static_cast<int>(lroundf(nz_ * static_cast<float>(k))), w.g.nz);
+            if (tx < 0 || tx >= w.g.nx || ty < 0 || ty >= w.g.ny) continue;
+            const std::uint32_t cand = w.at(tx, ty, tz);
+            if (w.active[cand] != kFluidB) continue;
             s = cand; sx = tx; sy = ty; sz = tz;
             break;
         }
         int dzw = sz - z;
-        if (dzw > g.nz / 2) dzw -= g.nz;
-        if (dzw < -g.nz / 2) dzw += g.nz;
+        if (dzw > w.g.nz / 2) dzw -= w.g.nz;
+        if (dzw < -w.g.nz / 2) dzw += w.g.nz;
         const float proj = static_cast<float>(sx - x) * nx_ + static_cast<float>(sy - y) * ny_
                          + static_cast<float>(dzw) * nz_;
-        cell[slot] = static_cast<std::uint32_t>(c);
-        sample[slot] = static_cast<std::uint32_t>(s);
+        cell[slot] = c;
+        sample[slot] = s;
         nX[slot] = nx_; nY[slot] = ny_; nZ[slot] = nz_;
         ys[slot] = 0.5f + fmaxf(proj, 0.0f);
         mask[slot] = m;
@@ -671,9 +716,41 @@ cudaError_t device_cells_where(LevelDims d, const std::uint8_t* flags, std::uint
 cudaError_t device_wall_list(LevelDims d, const std::uint8_t* active, const std::uint8_t* clean, int sampleCells,
                              const WallListOut& out, long long cap, long long* count, int stats[3],
                              cudaStream_t st) {
-    WallPred p{{d.nx, d.ny, d.nz}, active, clean ? clean : active, sampleCells, out.cell, out.sample, out.mask,
-               out.nX, out.nY, out.nZ, out.ys};
-    return compact_into(p, {d.nx, d.ny, d.nz}, cap, count, stats, st);
+    const Grid3 g{d.nx, d.ny, d.nz};
+    const long long n = d.cells();
+    if (n <= 0 || n >= (1LL << 31) || !count || !active) return cudaErrorInvalidValue;
+    const WallGeom w{g, active, clean ? clean : active};
+    // 1. Candidates, in cell order.
+    WallCandPred p1{w, nullptr, nullptr};
+    CompactScratch ws;
+    long long nc = 0;
+    int s1[3] = {0, 0, 0};
+    cudaError_t e = ws.alloc(tiles_for(n), st);
+    if (e == cudaSuccess) e = compact_count(p1, g, ws, &nc, s1, st);
+    void* cand = nullptr;
+    if (e == cudaSuccess && nc > 0) e = cudaMallocAsync(&cand, static_cast<size_t>(nc) * 8, st);
+    if (e == cudaSuccess && nc > 0) {
+        p1.cells = static_cast<std::uint32_t*>(cand);
+        p1.masks = p1.cells + nc;
+        e = compact_scatter(p1, g, ws, nc, st);
+    }
+    ws.release(st);
+    // 2. The listed entries among them.
+    int s2[3] = {0, 0, 0};
+    if (e == cudaSuccess) {
+        if (nc > 0) {
+            const std::uint32_t* cc = static_cast<const std::uint32_t*>(cand);
+            WallListPred p2{w, sampleCells, cc, cc + nc, out.cell, out.sample, out.mask, out.nX, out.nY, out.nZ,
+                            out.ys};
+            e = compact_into(p2, {static_cast<int>(nc), 1, 1}, cap, count, s2, st);
+        } else {
+            *count = 0;
+        }
+    }
+    if (cand) cudaFreeAsync(cand, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (stats) { stats[0] = s2[0]; stats[1] = s1[1]; stats[2] = s2[2]; }
+    return e;
 }
 
 } // namespace fcfd
