@@ -478,6 +478,41 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
     collide_one<S, WM, EXACT, QL>(src, dst, kind, a, x, blockIdx.y, blockIdx.z, &off);
 }
 
+// ---- one cell per thread over the flattened lattice -----------------------------
+// For levels whose rows are not a multiple of 32 cells (the 616-cell fine
+// rows of the airfoil patch), a row-per-block launch ends every row with a
+// partly idle warp; here consecutive threads take consecutive cells across
+// row boundaries. (x, y, z) come from two divisions by invariant integers
+// (Granlund & Montgomery 1994: q = (t + ((n - t) >> 1)) >> s, t = mulhi(m, n)).
+struct FastDiv {
+    unsigned d, m;
+    int s;
+};
+/// Divisor d >= 2: m = floor(2^32 (2^l - d) / d) + 1, s = l - 1, l = ceil(log2 d).
+inline FastDiv fast_div(unsigned d) {
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    const unsigned long long m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, static_cast<unsigned>(m), l - 1};
+}
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv& f) {
+    const unsigned t = __umulhi(n, f.m);
+    return (t + ((n - t) >> 1)) >> f.s;
+}
+
+template <class S, bool WM, bool EXACT, bool QL>
+__global__ void __launch_bounds__(kCellBlockX, S::kCellMinBlocks)
+collide_flat_kernel(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
+                    const std::uint8_t* __restrict__ kind, CollideArgs a, const __grid_constant__ PullOffsets off,
+                    FastDiv divX, FastDiv divY) {
+    const unsigned cell = blockIdx.x * kCellBlockX + threadIdx.x;
+    if (cell >= static_cast<unsigned long long>(a.n)) return;
+    const unsigned row = fdiv(cell, divX);
+    const unsigned z = fdiv(row, divY);
+    collide_one<S, WM, EXACT, QL>(src, dst, kind, a, static_cast<int>(cell - row * divX.d),
+                                  static_cast<int>(row - z * divY.d), static_cast<int>(z), &off);
+}
+
 // ---- warm-restart flag edits (applyFlagEditsKernel, lbm_core.cu:644-717) -----
 // mask 1: newly solid -> every population of both buffers zeroed; mask 2:
 // newly fluid -> equilibrium of the mean rho, u of the neighbours (x + c_q,
@@ -974,6 +1009,15 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),
                     static_cast<unsigned>(d.nz));
     const PullOffsets off = pull_offsets<T>(d.nx, d.ny, a.n);
+    if (d.nx % 32 != 0 && d.nx >= 2 && d.ny >= 2) {
+        const FastDiv fx = fast_div(static_cast<unsigned>(d.nx)), fy = fast_div(static_cast<unsigned>(d.ny));
+        const unsigned blocks = static_cast<unsigned>((a.n + kCellBlockX - 1) / kCellBlockX);
+        const bool ql = a.qFrac != nullptr;
+        auto kern = wm ? (ql ? collide_flat_kernel<S, true, EXACT, true> : collide_flat_kernel<S, true, EXACT, false>)
+                       : (ql ? collide_flat_kernel<S, false, EXACT, true> : collide_flat_kernel<S, false, EXACT, false>);
+        kern<<<blocks, kCellBlockX, 0, st>>>(src, dst, kind, a, off, fx, fy);
+        return cudaGetLastError();
+    }
     if (a.qFrac) {
         if (wm) collide_cell_kernel<S, true, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a, off);
         else collide_cell_kernel<S, false, EXACT, true><<<grid, bx, 0, st>>>(src, dst, kind, a, off);

@@ -391,6 +391,11 @@ def test_staged_import_equals_import(fc, storage):
 
     a = make()
     assert a.commit_staged() == 600
+    with pytest.raises(fc.SolverError):   # no finer level
+        a.stage_f32(2, np.zeros(19, np.float32))
+    with pytest.raises(fc.SolverError):   # wrong element count
+        a.stage_f32(0, np.zeros(19 * 8, np.float32))
+    assert a.commit_staged() == 600
     assert a.step_n(5) == 0
     kept = [PinnedArray(19 * int(np.prod(d))) for d in (t.dims, t.fine_dims)]
     kept[0].array[:] = a.export_f32()
