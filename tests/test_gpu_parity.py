@@ -5,8 +5,8 @@ the golden vectors the reference's own kernels produced, and the oracle
 The FP32 collide and the refinement coupling evaluate the reference's
 expression tree without FMA contraction, so their populations must be
 bit-identical to the reference (golden) and the oracle: the tests assert
-exact equality on every cell a step writes, and also report the north-star
-metric (<= 1e-6 relative in rho and u, max-norm normalised by the field's
+exact equality on every cell a step writes, and also report the parity
+target (<= 1e-6 relative in rho and u, max-norm normalised by the field's
 max, after 1000 steps). The wall model (fast __logf/__expf on the device),
 the FP64 force sums (summation order) and FP16 storage carry the tolerances
 stated in their tests."""
