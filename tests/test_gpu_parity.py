@@ -92,7 +92,7 @@ def test_collide_vs_reference_golden(fc, golden, case, steps, flags_key, slip, k
 
 
 def test_taylor_green_1000_steps_vs_reference(fc, golden):
-    """Spec bar: <= 1e-6 relative in rho and u after 1000 steps."""
+    """Parity bar: <= 1e-6 relative in rho and u after 1000 steps."""
     g = golden("taylor_green")
     dims = tuple(int(x) for x in g["dims"])
     tau, lam, cs, u_in = (float(x) for x in g["params"])
