@@ -16,7 +16,7 @@
  * u_tau (the fixed log u_par term only centres the target). One FP32 Newton
  * correction follows; when the relative Reichardt residual |g| / u_par after
  * it exceeds 1e-6, the cell falls back to full FP64 Newton (relative step
- * below 1e-8), which is also the judge of the seed's error.
+ * below 1e-8), which is also the reference the seed's error is measured against.
  *
  * The network is trained on the GPU by this library's own forward/backward
  * and Adam kernels from (u_par, y, nu, u_tau) samples: harvested from a
