@@ -102,6 +102,26 @@ template <> struct ChildRecord<StoreF32> {
         return true;
     }
     __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + kScratchRho / 4); }
+    /// As add, but every part of the record is read before the valid flag
+    /// decides (a select keeps acc when the record is invalid), so the loads
+    /// of successive neighbours do not wait on each other's flags.
+    __device__ __forceinline__ static bool add_sel(const float4* rec, float (&acc)[kQ]) {
+        float4 a[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) a[k] = __ldg(rec + k);
+        const bool ok = a[4].w != 0.0f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            acc[4 * k] = ok ? acc[4 * k] + a[k].x : acc[4 * k];
+            acc[4 * k + 1] = ok ? acc[4 * k + 1] + a[k].y : acc[4 * k + 1];
+            acc[4 * k + 2] = ok ? acc[4 * k + 2] + a[k].z : acc[4 * k + 2];
+            acc[4 * k + 3] = ok ? acc[4 * k + 3] + a[k].w : acc[4 * k + 3];
+        }
+        acc[16] = ok ? acc[16] + a[4].x : acc[16];
+        acc[17] = ok ? acc[17] + a[4].y : acc[17];
+        acc[18] = ok ? acc[18] + a[4].z : acc[18];
+        return ok;
+    }
 };
 
 template <> struct ChildRecord<StoreF16> {
@@ -162,6 +182,27 @@ template <> struct ChildRecord<StoreF16> {
         return true;
     }
     __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + 3); }
+    __device__ __forceinline__ static bool add_sel(const float4* rec, float (&acc)[kQ]) {
+        uint4 c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c[k] = __ldg(reinterpret_cast<const uint4*>(rec) + k);
+        const bool ok = __uint_as_float(c[2].z) != 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const unsigned w[4] = {c[k].x, c[k].y, c[k].z, c[k].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 p = unpack(w[j]);
+                acc[8 * k + 2 * j] = ok ? acc[8 * k + 2 * j] + p.x : acc[8 * k + 2 * j];
+                acc[8 * k + 2 * j + 1] = ok ? acc[8 * k + 2 * j + 1] + p.y : acc[8 * k + 2 * j + 1];
+            }
+        }
+        const float2 p16 = unpack(c[2].x), p18 = unpack(c[2].y);
+        acc[16] = ok ? acc[16] + p16.x : acc[16];
+        acc[17] = ok ? acc[17] + p16.y : acc[17];
+        acc[18] = ok ? acc[18] + p18.x : acc[18];
+        return ok;
+    }
 };
 
 /// Record of a coarse cell from the sum fi of its nFluid fluid children

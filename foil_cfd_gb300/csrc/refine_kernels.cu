@@ -231,8 +231,7 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
         const int nzw = wrapi(zc + cz(nb), nz);
         const long long tn = nlx + static_cast<long long>(rw) * (nly + static_cast<long long>(rh) * nzw);
         // Same per-q accumulation order as summing slot by slot.
-        if (!ChildRecord<S>::add(rec + tn * kRec, fneq)) continue;
-        ++nStencil;
+        nStencil += ChildRecord<S>::add_sel(rec + tn * kRec, fneq) ? 1 : 0;
     }
     const float invS = 1.0f / static_cast<float>(nStencil);
 #pragma unroll
