@@ -619,6 +619,18 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
 #pragma unroll
     for (int k = 0; k < kSplit; ++k) acc[k] = 0.0f;
     int nFluid = 0;
+    // The four cells' kind bytes, read up front (one byte each in a packed
+    // word), so no cell's update waits on a kind load after the previous one.
+    unsigned kinds = 0;
+    if (inX) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int y = 2 * blockIdx.y + (c & 1), z = 2 * blockIdx.z + (c >> 1);
+            kinds |= static_cast<unsigned>(kind[static_cast<unsigned>(x) + static_cast<unsigned>(a.nx)
+                                                * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z)])
+                   << (8 * c);
+        }
+    }
     for (int kz = 0; kz < 2; ++kz)
         for (int jy = 0; jy < 2; ++jy) {
             const int y = 2 * blockIdx.y + jy, z = 2 * blockIdx.z + kz;
@@ -627,7 +639,7 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
             if (inX) {
                 const unsigned cell = static_cast<unsigned>(x)
                                     + static_cast<unsigned>(a.nx) * (static_cast<unsigned>(y) + static_cast<unsigned>(a.ny) * z);
-                const std::uint8_t k = kind[cell];
+                const std::uint8_t k = static_cast<std::uint8_t>(kinds >> (8 * (2 * kz + jy)));
                 const int flag = k & kFlagMask;
                 if (flag == kFluid) {
                     gather_fluid<S, WM, QL, !EXACT>(src, kind, a, k, cell, x, y, z, v, &off);
