@@ -788,16 +788,121 @@ def reference_cuda_leg(warmup=100, steps=100):
             "glups": round(cells * steps / (ms * 1e-3) / 1e9, 3), "ms_per_step": round(ms / steps, 4),
             "steps": steps, "warmup": warmup}
     # The metric's own workload: the config-3 tunnel with its 2:1 patch and
-    # the wall model on (zero slip arrays: the same reads and arithmetic),
-    # the reference's refined step, counted as coarse + 2 x fine updates.
+    # the wall model on, the reference's whole refined stepN: per step the
+    # collides, fills, restriction and ghost refreshes; per batch of 50 the
+    # force reduction on the fine level and the wall-model update of both
+    # levels (wall lists from this library's host builder, byte-identical to
+    # the reference's buildWallCellList); the watchdog every 200 steps.
+    # Counted as coarse + 2 x fine updates.
+    import foil_cfd_gb300 as fc
     w = workload(False)
     sc = _scaling_of(w)
-    ms3 = ref_gpu.run_refined(w.dims, w.flags, w.fine_dims, w.fine_flags, w.box, w.factor, sc.tau, w.u_lat, cs=0.1,
-                              wall_model=True, warmup=10, steps=100, batch=BATCH)
+    wc = fc.build_wall_list(w.dims, w.flags, None, 2)
+    wf = fc.build_wall_list(w.fine_dims, w.fine_flags, None, 3)
+    r3 = ref_gpu.run_full(w.dims, w.flags, sc.tau, w.u_lat, cs=0.1, wall=wc,
+                          fine=dict(dims=w.fine_dims, flags=w.fine_flags, box=w.box, factor=w.factor, wall=wf),
+                          wm=True, warmup=10, steps=100, batch=BATCH, forces=True, watchdog=True,
+                          variant="asbuilt")
+    ms3 = r3["ms"]
     out["config3"] = {"workload": f"{w.name} + {w.fine_dims[0]}x{w.fine_dims[1]}x{w.fine_dims[2]} 2:1 patch, "
-                                  "wall-model kernels, FP32 (the reference's refined stepN launches)",
+                                  "wall model, FP32: the reference's refined stepN launches incl. the per-batch "
+                                  "force reduction and wall-model updates and the watchdog",
                       "glups": round(w.updates_per_step() * 100 / (ms3 * 1e-3) / 1e9, 3),
-                      "ms_per_step": round(ms3 / 100, 4)}
+                      "ms_per_step": round(ms3 / 100, 4), "steps": 100, "warmup": 10,
+                      "watchdog_trips": r3["trip_step"]}
+    return out
+
+
+def _uniform_feq(u):
+    """feq(1, u, 0, 0) per direction in FP32, in the reference's equilibrium19
+    expression order without contraction (the harness's uniform start)."""
+    f32 = np.float32
+    u = f32(u)
+    usq = f32(1.5) * (u * u)
+    cx = [0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0]
+    out = np.empty(19, np.float32)
+    for q in range(19):
+        w = f32(1.0) / f32(3.0) if q == 0 else (f32(1.0) / f32(18.0) if q <= 6 else f32(1.0) / f32(36.0))
+        cu = f32(3.0) * (f32(cx[q]) * u)
+        out[q] = (w * f32(1.0)) * (((f32(1.0) + cu) + (f32(0.5) * cu) * cu) - usq)
+    return out
+
+
+def _first_trip(sol, steps, batch=100):
+    """Step `sol` in stepN(batch) calls; the step count after the call whose
+    watchdog check latched, its verdict, or (0, 0)."""
+    done = 0
+    while done < steps:
+        n = min(batch, steps - done)
+        sol.step_n(n)
+        done += n
+        sol.synchronize()
+        if sol.nan_detected():
+            return done, int(sol.nan_kind())
+    return 0, 0
+
+
+def stability_leg(c3_steps=300, c2_steps=6000):
+    """Where the specified configurations first trip the speed/NaN watchdog
+    (every 200 steps, 1/4093 of the cells, lbm_core.cu:508-559): the
+    reference's own step (as-built cubins: collide, fills, restriction, ghost
+    refreshes, per-batch force reduction and wall-model updates, watchdog;
+    oracle/ref_gpu_harness.cu) and this library, both from the same uniform
+    feq(1, u_in) start in both A/B buffers, ramps off, stepN batches of 100.
+    Config 3: the 640x192x192 tunnel with its patch and the wall model, tau
+    0.5005; config 2: the 384x128x64 square cylinder (side 24, bounce-back
+    walls, zero-gradient outlet), Re 1000 (tau 0.50576), Cs 0.1. The
+    reference runs as it builds (asbuilt: contracted multiply-adds) and
+    without contraction (nofma, which this library equals bit for bit)."""
+    import foil_cfd_gb300 as fc
+    from foil_cfd_gb300 import tunnels
+    from oracle import ref_gpu
+    if not ref_gpu.available("asbuilt", ("core", "refine", "wall")):
+        return {"unavailable": "reference cubins not built (the reference tree is only in the build container)"}
+    out = {}
+    # config 3
+    t = workload(False)
+    sc = _scaling_of(t)
+    feq = _uniform_feq(t.u_lat)
+    nc, nf = int(np.prod(t.dims)), int(np.prod(t.fine_dims))
+    sol, _ = make_solver(t, "fp32")
+    sol.import_f32(np.repeat(feq, nc))
+    sol.import_fine_f32(np.repeat(feq, nf))
+    sol.mirror_buffers()
+    ours = _first_trip(sol, c3_steps)
+    sol = None
+    wc = fc.build_wall_list(t.dims, t.flags, None, 2)
+    wf = fc.build_wall_list(t.fine_dims, t.fine_flags, None, 3)
+    rec = {"workload": f"{t.name} + 2:1 patch, wall model, tau {sc.tau:.4f}, {c3_steps} steps",
+           "ours_first_trip_step": ours[0], "ours_verdict": ours[1]}
+    for variant in ("asbuilt", "nofma"):
+        r = ref_gpu.run_full(t.dims, t.flags, sc.tau, t.u_lat, cs=0.1, wall=wc,
+                             fine=dict(dims=t.fine_dims, flags=t.fine_flags, box=t.box, factor=t.factor, wall=wf),
+                             wm=True, steps=c3_steps, batch=100, forces=True, watchdog=True, variant=variant)
+        rec[f"reference_{variant}_first_trip_step"] = r["trip_step"]
+        rec[f"reference_{variant}_verdict"] = r["trip_flag"]
+    out["config3"] = rec
+    # config 2
+    c = tunnels.square_cylinder(384, 128, 64, side=24, u_lat=0.08)
+    tau2 = np.float32(0.5 + 3.0 * 0.08 * 24 / 1000.0)
+    feq = _uniform_feq(c.u_lat)
+    n2 = int(np.prod(c.dims))
+    sol = fc.LBMSolver()
+    sol.init(c.dims, fc.scaling_direct(float(tau2), c.u_lat, 24), c.flags, storage="fp32", les_cs=0.1)
+    sol.set_startup_ramp_enabled(False)
+    sol.reset()
+    sol.import_f32(np.repeat(feq, n2))
+    sol.mirror_buffers()
+    ours = _first_trip(sol, c2_steps)
+    sol = None
+    rec = {"workload": f"384x128x64 square cylinder, Re 1000, tau {float(tau2):.5f}, Cs 0.1, {c2_steps} steps",
+           "ours_first_trip_step": ours[0], "ours_verdict": ours[1]}
+    for variant in ("asbuilt", "nofma"):
+        r = ref_gpu.run_full(c.dims, c.flags, float(tau2), c.u_lat, cs=0.1, wm=False, steps=c2_steps, batch=100,
+                             forces=True, watchdog=True, variant=variant)
+        rec[f"reference_{variant}_first_trip_step"] = r["trip_step"]
+        rec[f"reference_{variant}_verdict"] = r["trip_flag"]
+    out["config2"] = rec
     return out
 
 
@@ -840,6 +945,26 @@ def cpu_reference(t, steps):
             "sample": f"{steps} coarse steps (+1 warm-up) of the full tunnel incl. patch, wall model and "
                       f"force, C++ oracle with OpenMP on {cpu_host()}",
             "seconds": round(dt, 2)}
+
+
+def cpu_config1():
+    """Config 1 in full on the host cores: the 64^3 periodic Taylor-Green
+    vortex (u0 0.05, tau 0.53, no LES), 1000 steps of the oracle port
+    (C++ restatement of the reference step, OpenMP, all host threads)."""
+    from oracle import oracle
+    from foil_cfd_gb300 import tunnels
+    oracle.build()
+    t = tunnels.taylor_green_periodic(64, 0.05)
+    n = int(np.prod(t.dims))
+    f0 = oracle.equilibrium(np.ones(n), t.extra["u"], t.extra["v"], np.zeros(n), np.float32)
+    o = oracle.OracleSolver(t.dims, t.flags, np.float32(0.53), np.float32(0.0), cs=-1.0)
+    o.set_state(f0)
+    t0 = time.perf_counter()
+    o.step_n(1000)
+    dt = time.perf_counter() - t0
+    return {"workload": "config 1: 64^3 periodic Taylor-Green, u0 0.05, tau 0.53, no LES, FP32, 1000 steps",
+            "value": round(n * 1000 / dt / 1e9, 5), "unit": UNIT, "seconds": round(dt, 2),
+            "cores": oracle.threads(), "kind": "port", "host": cpu_host()}
 
 
 def dist_setup():
@@ -902,6 +1027,9 @@ def main():
                     help="add the FP32/FP16/FP64 precision study (cylinder, airfoil, Taylor-Green)")
     ap.add_argument("--only-precision", action="store_true", help="run only the precision study")
     ap.add_argument("--only-polar", action="store_true", help="run only the batched-polar leg")
+    ap.add_argument("--only-stability", action="store_true",
+                    help="run only the watchdog-trip comparison with the reference's own step")
+    ap.add_argument("--no-stability", action="store_true", help="skip the watchdog-trip comparison")
     ap.add_argument("--polar-config", default="", help="block,rows,ctas_per_sm,group_mb: skip the autotuner")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
@@ -932,6 +1060,8 @@ def main():
                 "data": "synthetic", "config": cfg,
                 "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": ref["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if not args.no_cpu:
+            line["cpu_config1"] = cpu_config1()
         if not args.small:
             try:
                 line["reference_cuda_kernel"] = reference_cuda_leg()
@@ -947,6 +1077,10 @@ def main():
     if args.only_geometry:
         if rank == 0:
             print(json.dumps({"geometry_build": geometry_leg(t)}))
+        return
+    if args.only_stability:
+        if rank == 0:
+            print(json.dumps({"stability": stability_leg()}))
         return
     if args.only_polar:
         if rank == 0:
@@ -990,6 +1124,8 @@ def main():
         line["headline_plain_tunnel"] = headline_leg()
     if args.precision and ws == 1:
         line["precision"] = precision_leg()
+    if ws == 1 and not args.small and not args.no_stability:
+        line["stability"] = stability_leg()
     del r32
     if not args.no_fp16:
         r16 = measure(t, "fp16", args.steps, warmup, None)

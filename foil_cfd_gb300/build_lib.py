@@ -28,6 +28,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off"]
 # coupling must not contract multiply-adds (their rounding follows the
 # reference expression tree, so results are bit-identical to it).
 FILE_FLAGS = {"collide_f32.cu": ["--fmad=false"], "refine_kernels.cu": ["--fmad=false"], "batch_f32.cu": ["--fmad=false"],
+              "wall_kernels_x.cu": ["--fmad=false"],
               "geom_kernels.cu": ["--fmad=false"]}
 
 

@@ -10,19 +10,20 @@
 //
 // The array is part of the library's module image: every GPU that loads the
 // library holds its 96 KB until the process exits. Host code cannot use the
-// array's name as a device address, so the first call on each device looks
-// the address up once with cudaGetSymbolAddress (with that device current)
-// and caches it; make that first call before any stream capture on the
-// device. All calls share the array: each call writes the partials of its own
-// blocks before reading them, so nothing has to be cleared between calls, but
-// two calls that overlap on the GPU (different streams, no ordering) race on
-// the array and must be serialised by the caller.
+// array's name as a device address, so every call looks the address up with
+// cudaGetSymbolAddress on the current device. The first call on a device may
+// load the module there, so make it before any stream capture on that
+// device; later lookups are cheap, and because nothing is cached, a call
+// after cudaDeviceReset (a new context, possibly a new address) finds the
+// array where the new context put it. All calls share the array: each call
+// writes the partials of its own blocks before reading them, so nothing has
+// to be cleared between calls, but two calls that overlap on the GPU
+// (different streams, no ordering) race on the array and must be serialised
+// by the caller.
 #include "../../include/foilcfd_step.h"
 #include "d3q19.cuh"
 
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 // Block partials (Fx, Fy, Fz per block of a call): 3 doubles for every 256
 // links of the largest accepted list, 96 KB per device.
@@ -32,12 +33,8 @@ namespace fcfd {
 namespace {
 
 constexpr int kNoAllocBlock = 256;
-constexpr int kMaxDevices = 64;
 
 static_assert(FCFD_FORCE_NOALLOC_MAX_LINKS % kNoAllocBlock == 0, "link limit must fill whole blocks");
-
-std::mutex g_addr_mutex;
-double* g_addr[kMaxDevices] = {};
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -107,19 +104,12 @@ noalloc_final_kernel(const double* __restrict__ partials, int nb, double* __rest
     if (threadIdx.x == 0) { out[0] = fx; out[1] = fy; out[2] = fz; }
 }
 
-/// Device address of the partials array on the current device, looked up
-/// once per device with cudaGetSymbolAddress.
+/// Device address of the partials array in the current device's context
+/// (looked up on every call: no address outlives its context).
 cudaError_t partials_address(double** out) {
-    int dev = 0;
-    if (auto e = cudaGetDevice(&dev); e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        if (auto e = cudaGetSymbolAddress(&p, g_force_partials); e != cudaSuccess) return e;
-        g_addr[dev] = static_cast<double*>(p);
-    }
-    *out = g_addr[dev];
+    void* p = nullptr;
+    if (auto e = cudaGetSymbolAddress(&p, g_force_partials); e != cudaSuccess) return e;
+    *out = static_cast<double*>(p);
     return cudaSuccess;
 }
 

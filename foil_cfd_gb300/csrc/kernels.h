@@ -148,6 +148,13 @@ cudaError_t launch_wall_update(Storage s, const void* f, long long cells,
                                float nuLat, float utCutoff, float emaAlpha,
                                WallStatsDev* stats, cudaStream_t st,
                                int method = 0, const wallnet::NetDev* net = nullptr);
+/// The FP32 update, built without contraction (wall_kernels_x.cu): FP32
+/// storage rounds the wall model's expressions as written, like every other
+/// FP32 kernel; launch_wall_update routes FP32 storage here.
+cudaError_t launch_wall_update_f32_x(const void* f, long long cells, WallListDev list,
+                                     std::uint16_t* uwx, std::uint16_t* uwy, std::uint16_t* uwz,
+                                     float nuLat, float utCutoff, float emaAlpha, WallStatsDev* stats,
+                                     cudaStream_t st, int method, const wallnet::NetDev* net);
 /// Device view (BF16 weights + normalisation) of a learned seed network.
 wallnet::NetDev wallnet_view(const fcfd_wallnet* net);
 /// Sampled tangential speed (0 below the cut-off) and sample distance of

@@ -147,6 +147,16 @@ class LBMSolver:
             raise RuntimeError(f"fcfd_apply_edited_flags failed ({rc})")
         return int(edited.value)
 
+    def set_overlap_fills(self, enabled: bool) -> None:
+        """Interface fills on a side stream, overlapped with the collides."""
+        self._lib.fcfd_set_overlap_fills(self._h, int(enabled))
+
+    def mirror_buffers(self) -> None:
+        """Copy every level's current A/B buffer into the other one."""
+        rc = self._lib.fcfd_mirror_buffers(self._h)
+        if rc:
+            raise SolverError(f"buffer mirror failed ({rc})")
+
     def set_startup_ramp_enabled(self, enabled: bool):
         self._lib.fcfd_set_startup_ramp(self._h, int(enabled))
 

@@ -208,10 +208,14 @@ int fcfd_force_now(fcfd_solver* s, double out[3]);
  * allocate device memory -- a frame loop with a hard time budget, where
  * cudaMalloc may synchronise the device, or a host whose memory manager owns
  * every allocation: it calls no cudaMalloc/cudaFree; its scratch lives in a
- * static device array. The first call on each device looks that array's
- * address up (cudaGetSymbolAddress, with the device current); make it before
- * any stream capture. Calls share the array, so calls that overlap on the GPU
- * race. Returns cudaErrorInvalidValue (1) when count exceeds
+ * static device array. Each call looks that array's address up on the
+ * current device (cudaGetSymbolAddress); the first call on a device may load
+ * the module, so make it before any stream capture. Calls share the array,
+ * so calls that overlap on the GPU race. The buffer must hold FP32
+ * populations: fcfd_active_f of a solver created with FCFD_STORE_FP16 holds
+ * half-precision deviations (fcfd_f_bytes = 38 * ncells instead of
+ * 76 * ncells) and would be read past its end; check fcfd_f_bytes first.
+ * Returns cudaErrorInvalidValue (1) when count exceeds
  * FCFD_FORCE_NOALLOC_MAX_LINKS or an argument is missing. */
 int fcfd_force_links_noalloc(const float* f, long long ncells,
                              const uint32_t* link_cells,
@@ -237,6 +241,12 @@ void fcfd_notify_restored(fcfd_solver* s, int full_state);
  * tests/lbm_test_util.h:116-204). Import calls fcfd_notify_restored(s, 1). */
 int fcfd_import_f32(fcfd_solver* s, const float* host_f, size_t count);
 int fcfd_export_f32(fcfd_solver* s, float* host_f, size_t count);
+/* Copy every level's current population buffer into its other A/B buffer.
+ * Cells a step never writes (solid, slip planes, interface shell) keep the
+ * other buffer's contents, as in the reference's ping-pong pair; after
+ * importing a state that holds only the current buffer, this makes both
+ * buffers carry it. No reference counterpart. */
+int fcfd_mirror_buffers(fcfd_solver* s);
 /* Two-phase FP32 import, so that the host copy of the next state overlaps
  * the stepping of the current one (no reference counterpart: the reference
  * restores with blocking copies). fcfd_stage_f32 queues the host -> device
@@ -317,6 +327,12 @@ int fcfd_refinement_info(const fcfd_solver* s, fcfd_refine_info* out);
 /* FP32 SoA import/export of the fine level's current buffer. */
 int fcfd_import_fine_f32(fcfd_solver* s, const float* host_f, size_t count);
 int fcfd_export_fine_f32(fcfd_solver* s, float* host_f, size_t count);
+/* Interface fills of a factor-2 patch (no finer level) on a side stream of
+ * the solver, overlapped with the coarse collide and the first fine collide
+ * (default 1); 0 runs them in line on the solver stream. Same results either
+ * way. No reference counterpart (the reference launches everything on one
+ * stream, lbm_solver.cpp:1172-1291). */
+int fcfd_set_overlap_fills(fcfd_solver* s, int enabled);
 /* Factor-2 patches: form the restriction's child averages inside the last
  * fine sub-step's collide (1) instead of re-reading the fine level in a
  * separate pass (0; lbm_refine.cu:274-429 reads it in the restriction).

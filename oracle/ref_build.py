@@ -24,7 +24,9 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("FOILCFD_REFERENCE", "/root/reference"))
+# The reference checkout this recipe reads: FOILCFD_REFERENCE, else the
+# build container's read-only mount.
+REFERENCE = Path(os.environ.get("FOILCFD_REFERENCE") or "/root/reference")
 SIM = REFERENCE / "src" / "sim"
 UNITS = {
     "core": ("lbm_core.cu", "ref_driver_core.inc"),
@@ -35,6 +37,7 @@ FLAGS = ["-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fas
 
 
 def available() -> bool:
+    """True when the reference tree with the sources is present."""
     return (all((SIM / src).exists() for src, _ in UNITS.values()) and (SIM / "wall_model.cpp").exists()
             and (REFERENCE / "src" / "geom" / "voxelizer.cpp").exists() and (SIM / "snapshot.cpp").exists())
 
@@ -57,7 +60,7 @@ def _cuda_include() -> str:
 def build(force: bool = False) -> dict:
     """Build the three reference CPU libraries; returns {unit: path}."""
     if not available():
-        raise RuntimeError(f"reference sources not found under {SIM}")
+        raise RuntimeError(f"reference sources not found under {REFERENCE} (set FOILCFD_REFERENCE)")
     OUT.mkdir(parents=True, exist_ok=True)
     libs = {}
     for unit, (src, drv) in UNITS.items():
@@ -103,6 +106,9 @@ def build(force: bool = False) -> dict:
                                   ("cubin_nofma", "lbm_core.cu", "ref_core_sm103a_nofma.cubin", ["--fmad=false"]),
                                   ("cubin_refine", "lbm_refine.cu", "ref_refine_sm103a.cubin", []),
                                   ("cubin_refine_nofma", "lbm_refine.cu", "ref_refine_sm103a_nofma.cubin",
+                                   ["--fmad=false"]),
+                                  ("cubin_wall", "lbm_wallmodel.cu", "ref_wall_sm103a.cubin", []),
+                                  ("cubin_wall_nofma", "lbm_wallmodel.cu", "ref_wall_sm103a_nofma.cubin",
                                    ["--fmad=false"])):
         cubin = OUT / name
         libs[key] = cubin

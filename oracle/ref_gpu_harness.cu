@@ -1,11 +1,15 @@
-// ORACLE - measurement infrastructure only. Runs the reference's own CUDA
-// stream-collide kernel (src/sim/lbm_core.cu: streamCollideKernel<false,
-// false> and refreshGhostZKernel, compiled unmodified from the reference tree
-// into a cubin by ref_build.py) on this GPU through the driver API, in the
-// reference's padded layout (one ghost z plane on each side), so its speed can
-// be timed beside this library's kernel on the same hardware and inputs. The
-// kernels are found by name in the loaded module; their parameter lists are
-// the reference's (lbm_core.cu:214-226, 484-485), restated here.
+// ORACLE - measurement and test infrastructure only. Runs the reference's own
+// CUDA solver-step kernels on this GPU through the driver API, in the
+// reference's padded layout (one ghost z plane on each side): from
+// src/sim/lbm_core.cu streamCollideKernel<WM, false>, refreshGhostZKernel,
+// nanWatchdogKernel and forceReductionKernel<WM>; from lbm_refine.cu the
+// coarse-to-fine fill and the restriction; from lbm_wallmodel.cu the
+// wall-model update. Each is compiled unmodified from the reference tree into
+// a cubin by ref_build.py (as the reference builds it, and once more without
+// contraction). The kernels are found by name in the loaded modules; their
+// parameter lists are the reference's (lbm_core.cu:214-226, 484-485, 526-530,
+// 573-580; lbm_wallmodel.cu:76-84; lbm_wallmodel.cuh:47-82), restated here, and
+// the launch sequence is the reference's stepN (lbm_solver.cpp:1132-1390).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -31,9 +35,35 @@ struct QLinkViewArg {
     const std::uint32_t* ffMask = nullptr;
 };
 
-CUmodule gModule = nullptr, gRefineModule = nullptr;
+// WallCellListView, WallModelParams, WallModelDeviceStats
+// (lbm_wallmodel.cuh:47-82), field for field.
+struct WallListArg {
+    const long long* cellIdx = nullptr;
+    const long long* sampleIdx = nullptr;
+    const float* normalX = nullptr;
+    const float* normalY = nullptr;
+    const float* normalZ = nullptr;
+    const float* sampleDist = nullptr;
+    const std::uint32_t* linkMask = nullptr;
+    float* uTau = nullptr;
+    int count = 0;
+};
+struct WallParamsArg {
+    float nuLat, utCutoff, emaAlpha;
+};
+struct WallStatsArg {
+    float sumYplus;
+    int maxYplusBits, activeCells, clampedCells;
+};
+
+constexpr long long kWatchdogStride = 4093;   // lbm_core.cu:524
+constexpr int kWatchdogPeriod = 200;          // lbm_solver.cpp:25
+constexpr float kWallEma = 0.25f;             // kWallModelEmaAlpha
+
+CUmodule gModule = nullptr, gRefineModule = nullptr, gWallModule = nullptr;
 CUfunction gCollide = nullptr, gCollideWM = nullptr, gGhost = nullptr;
-CUfunction gFill = nullptr, gRestrict = nullptr;
+CUfunction gWatchdog = nullptr, gForce = nullptr, gForceWM = nullptr;
+CUfunction gFill = nullptr, gRestrict = nullptr, gWall = nullptr;
 std::string gErr;
 
 bool ok(CUresult r, const char* what) {
@@ -47,6 +77,19 @@ bool ok(CUresult r, const char* what) {
 } // namespace
 
 extern "C" const char* refgpu_error() { return gErr.c_str(); }
+
+// Unload every module (the next load may take another build variant).
+extern "C" int refgpu_unload() {
+    cudaDeviceSynchronize();
+    for (CUmodule* m : {&gModule, &gRefineModule, &gWallModule})
+        if (*m) {
+            cuModuleUnload(*m);
+            *m = nullptr;
+        }
+    gCollide = gCollideWM = gGhost = gWatchdog = gForce = gForceWM = nullptr;
+    gFill = gRestrict = gWall = nullptr;
+    return 0;
+}
 
 // Load the cubin and find the two kernels by their mangled names.
 extern "C" int refgpu_load(const char* cubin) {
@@ -68,6 +111,10 @@ extern "C" int refgpu_load(const char* cubin) {
         if (n.find("streamCollideKernel") != std::string::npos && n.find("ILb1ELb0E") != std::string::npos)
             gCollideWM = f;
         if (n.find("refreshGhostZKernel") != std::string::npos) gGhost = f;
+        if (n.find("nanWatchdogKernel") != std::string::npos) gWatchdog = f;
+        // forceReductionKernel<WM>: "ILb0EE" / "ILb1EE".
+        if (n.find("forceReductionKernel") != std::string::npos && n.find("ILb0E") != std::string::npos) gForce = f;
+        if (n.find("forceReductionKernel") != std::string::npos && n.find("ILb1E") != std::string::npos) gForceWM = f;
     }
     if (!gCollide || !gGhost) {
         gErr = "reference kernels not found in the module";
@@ -83,7 +130,7 @@ extern "C" int refgpu_load(const char* cubin) {
 // milliseconds. Every `batch`-th step writes the macroscopic fields, as the
 // reference's stepN does on a batch's last step.
 extern "C" int refgpu_run(int nx, int ny, int nz, const std::uint8_t* flags, float* f, float tau, float lambda,
-                          float cs, float uIn, int warmup, int steps, int batch, double* ms) {
+                          float cs, float uIn, int warmup, int steps, int batch, double* ms, int bothBuffers) {
     if (!gCollide || !gGhost || nx < 3 || ny < 3 || nz < 1 || !flags || !f || steps < 1 || batch < 1) {
         gErr = "bad arguments or module not loaded";
         return -1;
@@ -126,6 +173,10 @@ extern "C" int refgpu_run(int nx, int ny, int nz, const std::uint8_t* flags, flo
         std::memcpy(pad.data(), src + nxny * (nz - 1), static_cast<size_t>(nxny) * sizeof(float));
         std::memcpy(pad.data() + nxny * (nz + 1), src, static_cast<size_t>(nxny) * sizeof(float));
         cudaMemcpy(dA + q * npad, pad.data(), static_cast<size_t>(npad) * sizeof(float), cudaMemcpyHostToDevice);
+        // Cells a step never writes (slip planes) keep the other buffer's
+        // contents; with bothBuffers the other buffer starts equal to f.
+        if (bothBuffers)
+            cudaMemcpy(dB + q * npad, pad.data(), static_cast<size_t>(npad) * sizeof(float), cudaMemcpyHostToDevice);
     }
     // launchStreamCollide's prefactor: 18 sqrt(2) Cs^2 (0 disables the LES term).
     const float smagPre = cs > 0.0f ? 18.0f * 1.41421356f * cs * cs : 0.0f;
@@ -186,42 +237,102 @@ extern "C" int refgpu_run(int nx, int ny, int nz, const std::uint8_t* flags, flo
 
 // Load the refinement cubin (src/sim/lbm_refine.cu) and find the fill and
 // the restriction.
-extern "C" int refgpu_load_refine(const char* cubin) {
-    if (gRefineModule) return 0;
+namespace {
+
+bool load_module(CUmodule* mod, const char* cubin, const char* const* names, CUfunction* const* outs, int n) {
+    if (*mod) return true;
     cudaFree(nullptr);
-    if (!ok(cuModuleLoad(&gRefineModule, cubin), "cuModuleLoad")) return -1;
+    if (!ok(cuModuleLoad(mod, cubin), "cuModuleLoad")) return false;
     unsigned count = 0;
-    if (!ok(cuModuleGetFunctionCount(&count, gRefineModule), "cuModuleGetFunctionCount")) return -1;
+    if (!ok(cuModuleGetFunctionCount(&count, *mod), "cuModuleGetFunctionCount")) return false;
     std::vector<CUfunction> fns(count);
-    if (count && !ok(cuModuleEnumerateFunctions(fns.data(), count, gRefineModule), "cuModuleEnumerateFunctions"))
-        return -1;
+    if (count && !ok(cuModuleEnumerateFunctions(fns.data(), count, *mod), "cuModuleEnumerateFunctions"))
+        return false;
     for (CUfunction f : fns) {
         const char* name = nullptr;
         if (cuFuncGetName(&name, f) != CUDA_SUCCESS || !name) continue;
-        const std::string n(name);
-        if (n.find("coarseToFineFillKernel") != std::string::npos) gFill = f;
-        if (n.find("fineToCoarseRestrictKernel") != std::string::npos) gRestrict = f;
+        const std::string s(name);
+        for (int k = 0; k < n; ++k)
+            if (s.find(names[k]) != std::string::npos) *outs[k] = f;
     }
-    if (!gFill || !gRestrict) {
-        gErr = "reference refinement kernels not found in the module";
-        return -1;
-    }
-    return 0;
+    for (int k = 0; k < n; ++k)
+        if (!*outs[k]) {
+            gErr = std::string("reference kernel not found in the module: ") + names[k];
+            return false;
+        }
+    return true;
 }
+
+} // namespace
+
+extern "C" int refgpu_load_refine(const char* cubin) {
+    const char* names[] = {"coarseToFineFillKernel", "fineToCoarseRestrictKernel"};
+    CUfunction* outs[] = {&gFill, &gRestrict};
+    return load_module(&gRefineModule, cubin, names, outs, 2) ? 0 : -1;
+}
+
+// Load the wall-model cubin (src/sim/lbm_wallmodel.cu).
+extern "C" int refgpu_load_wall(const char* cubin) {
+    const char* names[] = {"wallModelUpdateKernel"};
+    CUfunction* outs[] = {&gWall};
+    return load_module(&gWallModule, cubin, names, outs, 1) ? 0 : -1;
+}
+
+// ---- full reference step -----------------------------------------------------
+
+/// One level of a run: flags, an optional initial state (both buffers), an
+/// optional wall-cell list (the reference's SoA, unpadded indices), and
+/// optional outputs.
+struct RefLevelIn {
+    int nx, ny, nz;
+    const std::uint8_t* flags;
+    const float* f0;             // unpadded FP32 SoA, both buffers; null: uniform feq(1, u_in)
+    int wallCount;               // 0: no wall-model update on this level
+    const long long* wallCell;
+    const long long* wallSample;
+    const float* wallNx;
+    const float* wallNy;
+    const float* wallNz;
+    const float* wallYs;
+    const std::uint32_t* wallMask;
+    float* outF;                 // final current buffer (unpadded), or null
+    float* outUTau;              // final u_tau (wallCount), or null
+};
+
+struct RefRunIn {
+    RefLevelIn coarse, fine;
+    int refined, bx0, by0, bx1, by1, factor;
+    float tau, lambda, cs, uIn;
+    int wm;         // WM collide/force instantiations (slip arrays on every level)
+    int warmup, steps, batch;
+    int forces;     // force reduction once per batch
+    int watchdog;   // watchdog every 200 steps
+};
+
+struct RefRunOut {
+    double ms;
+    long long tripStep;   // first step whose watchdog check read nonzero (0: none)
+    int tripFlag;         // its verdict (1/2 coarse, 3/4 fine)
+    int checks;           // watchdog checks run
+    float force[3];       // the last batch's force (FP32, atomics)
+    long long stepsRun;
+};
 
 namespace {
 
-/// One level in the reference's padded layout, initialised to the uniform
-/// equilibrium feq(1, u_in) (a constant per direction).
+/// One level in the reference's padded layout.
 struct PaddedLevel {
     int nx = 0, ny = 0, nz = 0;
     long long nxny = 0, n = 0, npad = 0;
     float* f[2] = {nullptr, nullptr};
     std::uint8_t* flags = nullptr;
-    std::uint16_t* slip = nullptr;   // three zero half arrays (wall model on, no slip yet)
+    std::uint16_t* slip = nullptr;   // three half arrays, zero until the wall model writes them
+    WallListArg wl;
+    void* wallMem = nullptr;
+    WallStatsArg* stats = nullptr;
 
-    bool alloc(int x, int y, int z, const std::uint8_t* hostFlags, float uIn, bool wm) {
-        nx = x; ny = y; nz = z;
+    bool alloc(const RefLevelIn& in, float uIn, bool wm) {
+        nx = in.nx; ny = in.ny; nz = in.nz;
         nxny = static_cast<long long>(nx) * ny;
         n = nxny * nz;
         npad = nxny * (nz + 2);
@@ -233,23 +344,61 @@ struct PaddedLevel {
         if (wm) cudaMemset(slip, 0, 3 * n * sizeof(std::uint16_t));
         cudaMemset(flags, 1, npad + slack);
         std::vector<std::uint8_t> pf(static_cast<size_t>(npad));
-        std::memcpy(pf.data() + nxny, hostFlags, static_cast<size_t>(n));
-        std::memcpy(pf.data(), hostFlags + nxny * (nz - 1), static_cast<size_t>(nxny));
-        std::memcpy(pf.data() + nxny * (nz + 1), hostFlags, static_cast<size_t>(nxny));
+        std::memcpy(pf.data() + nxny, in.flags, static_cast<size_t>(n));
+        std::memcpy(pf.data(), in.flags + nxny * (nz - 1), static_cast<size_t>(nxny));
+        std::memcpy(pf.data() + nxny * (nz + 1), in.flags, static_cast<size_t>(nxny));
         cudaMemcpy(flags, pf.data(), static_cast<size_t>(npad), cudaMemcpyHostToDevice);
-        // feq(1, u_in, 0, 0) per direction, the reference's equilibrium19.
-        static const int cxq[kQ] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0};
-        const float usq = 1.5f * (uIn * uIn);
-        for (int q = 0; q < kQ; ++q) {
-            const float w = q == 0 ? 1.0f / 3.0f : (q <= 6 ? 1.0f / 18.0f : 1.0f / 36.0f);
-            const float cu = 3.0f * (static_cast<float>(cxq[q]) * uIn);
-            const float v = (w * 1.0f) * (1.0f + cu + 0.5f * cu * cu - usq);
-            unsigned bits;
-            std::memcpy(&bits, &v, 4);
-            for (float* p : f)
-                if (cuMemsetD32(reinterpret_cast<CUdeviceptr>(p + q * npad), bits, static_cast<size_t>(npad))
-                    != CUDA_SUCCESS)
-                    return false;
+        for (float* p : f) cudaMemset(p, 0, (kQ * npad + slack) * sizeof(float));
+        if (in.f0) {
+            std::vector<float> pad(static_cast<size_t>(npad));
+            for (int q = 0; q < kQ; ++q) {
+                const float* src = in.f0 + q * n;
+                std::memcpy(pad.data() + nxny, src, static_cast<size_t>(n) * sizeof(float));
+                std::memcpy(pad.data(), src + nxny * (nz - 1), static_cast<size_t>(nxny) * sizeof(float));
+                std::memcpy(pad.data() + nxny * (nz + 1), src, static_cast<size_t>(nxny) * sizeof(float));
+                for (float* p : f)
+                    cudaMemcpy(p + q * npad, pad.data(), static_cast<size_t>(npad) * sizeof(float),
+                               cudaMemcpyHostToDevice);
+            }
+        } else {
+            // feq(1, u_in, 0, 0) per direction, the reference's equilibrium19.
+            static const int cxq[kQ] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0};
+            const float usq = 1.5f * (uIn * uIn);
+            for (int q = 0; q < kQ; ++q) {
+                const float w = q == 0 ? 1.0f / 3.0f : (q <= 6 ? 1.0f / 18.0f : 1.0f / 36.0f);
+                const float cu = 3.0f * (static_cast<float>(cxq[q]) * uIn);
+                const float v = (w * 1.0f) * (1.0f + cu + 0.5f * cu * cu - usq);
+                unsigned bits;
+                std::memcpy(&bits, &v, 4);
+                for (float* p : f)
+                    if (cuMemsetD32(reinterpret_cast<CUdeviceptr>(p + q * npad), bits, static_cast<size_t>(npad))
+                        != CUDA_SUCCESS)
+                        return false;
+            }
+        }
+        if (in.wallCount > 0) {
+            const size_t c = static_cast<size_t>(in.wallCount);
+            const size_t bytes = c * (2 * sizeof(long long) + 5 * sizeof(float) + sizeof(std::uint32_t)
+                                      + sizeof(float)) + sizeof(WallStatsArg) + 256;
+            if (cudaMalloc(&wallMem, bytes) != cudaSuccess) return false;
+            char* b = static_cast<char*>(wallMem);
+            auto put = [&](const void* h, size_t sz) {
+                void* d = b;
+                if (h) cudaMemcpy(d, h, sz, cudaMemcpyHostToDevice);
+                else cudaMemset(d, 0, sz);
+                b += (sz + 15) & ~static_cast<size_t>(15);
+                return d;
+            };
+            wl.cellIdx = static_cast<const long long*>(put(in.wallCell, c * 8));
+            wl.sampleIdx = static_cast<const long long*>(put(in.wallSample, c * 8));
+            wl.normalX = static_cast<const float*>(put(in.wallNx, c * 4));
+            wl.normalY = static_cast<const float*>(put(in.wallNy, c * 4));
+            wl.normalZ = static_cast<const float*>(put(in.wallNz, c * 4));
+            wl.sampleDist = static_cast<const float*>(put(in.wallYs, c * 4));
+            wl.linkMask = static_cast<const std::uint32_t*>(put(in.wallMask, c * 4));
+            wl.uTau = static_cast<float*>(put(nullptr, c * 4));   // fresh seeds (u_tau = 0)
+            stats = static_cast<WallStatsArg*>(put(nullptr, sizeof(WallStatsArg)));
+            wl.count = in.wallCount;
         }
         return true;
     }
@@ -257,7 +406,8 @@ struct PaddedLevel {
         for (float*& p : f) { if (p) cudaFree(p); p = nullptr; }
         if (flags) cudaFree(flags);
         if (slip) cudaFree(slip);
-        flags = nullptr; slip = nullptr;
+        if (wallMem) cudaFree(wallMem);
+        flags = nullptr; slip = nullptr; wallMem = nullptr;
     }
 };
 
@@ -286,97 +436,190 @@ bool launch_ghost(const PaddedLevel& L, float* f) {
     return ok(cuLaunchKernel(gGhost, grid, 1, 1, kBlock, 1, 1, 0, nullptr, args, nullptr), "ghost launch");
 }
 
+/// launchNaNWatchdog (lbm_core.cu:856-870): the strided sample of `f`.
+bool launch_watchdog(const PaddedLevel& L, const float* f, long long sampleOffset, int* flag, int flagBase) {
+    long long a_off = ((sampleOffset % kWatchdogStride) + kWatchdogStride) % kWatchdogStride;
+    long long a_n = L.n, a_npad = L.npad, a_nxny = L.nxny;
+    int a_base = flagBase;
+    const float* a_f = f;
+    void* args[] = {&a_f, &a_n, &a_npad, &a_nxny, &a_off, &flag, &a_base};
+    const long long samples = (L.n + kWatchdogStride - 1) / kWatchdogStride;
+    const unsigned grid = static_cast<unsigned>((samples + kBlock - 1) / kBlock);
+    return ok(cuLaunchKernel(gWatchdog, grid, 1, 1, kBlock, 1, 1, 0, nullptr, args, nullptr), "watchdog launch");
+}
+
+/// launchForceReduction (lbm_core.cu:880-901): zero the accumulator, reduce.
+bool launch_force(const PaddedLevel& L, const float* f, float* acc) {
+    if (cudaMemsetAsync(acc, 0, 3 * sizeof(float), nullptr) != cudaSuccess) return false;
+    long long a_n = L.n, a_npad = L.npad, a_nxny = L.nxny;
+    int a_nx = L.nx;
+    const float* a_f = f;
+    const std::uint8_t* a_fl = L.flags;
+    SlipViewArg slip;
+    if (L.slip) { slip.uwx = L.slip; slip.uwy = L.slip + L.n; slip.uwz = L.slip + 2 * L.n; }
+    void* args[] = {&a_f, &a_fl, &a_n, &a_npad, &a_nxny, &a_nx, &acc, &slip};
+    const unsigned grid = static_cast<unsigned>((L.n + kBlock - 1) / kBlock);
+    return ok(cuLaunchKernel(L.slip ? gForceWM : gForce, grid, 1, 1, kBlock, 1, 1, 0, nullptr, args, nullptr),
+              "force launch");
+}
+
+/// launchWallModelUpdate (lbm_wallmodel.cu:200-225).
+bool launch_wall(PaddedLevel& L, const float* f, float nuLat, float utCutoff) {
+    if (L.wl.count <= 0) return true;
+    if (cudaMemsetAsync(L.stats, 0, sizeof(WallStatsArg), nullptr) != cudaSuccess) return false;
+    WallListArg a_list = L.wl;
+    const float* a_f = f;
+    long long a_npad = L.npad, a_nxny = L.nxny;
+    std::uint16_t *a_x = L.slip, *a_y = L.slip + L.n, *a_z = L.slip + 2 * L.n;
+    WallParamsArg a_p{nuLat, utCutoff, kWallEma};
+    WallStatsArg* a_s = L.stats;
+    void* args[] = {&a_list, &a_f, &a_npad, &a_nxny, &a_x, &a_y, &a_z, &a_p, &a_s};
+    const unsigned grid = static_cast<unsigned>((L.wl.count + kBlock - 1) / kBlock);
+    return ok(cuLaunchKernel(gWall, grid, 1, 1, kBlock, 1, 1, 0, nullptr, args, nullptr), "wall launch");
+}
+
 } // namespace
 
-// The reference's refined step (lbm_solver.cpp:1140-1291) with one 2:1 (or
-// m:1) patch: coarse collide + ghost refresh; m times fill the fine shell
-// from the coarse pair at weight half/m, ghost refresh, fine collide, ghost
-// refresh; restriction into the new coarse buffer + ghost refresh. Uniform
-// equilibrium start; wall model on (zero slip arrays) or off. Times `steps`
-// coarse steps after `warmup`; macroscopic fields on every batch's last step.
-extern "C" int refgpu_run_refined(int cnx, int cny, int cnz, const std::uint8_t* cflags, int fnx, int fny, int fnz,
-                                  const std::uint8_t* fflags, int bx0, int by0, int bx1, int by1, int factor,
-                                  float tau, float lambda, float cs, float uIn, int wm, int warmup, int steps,
-                                  int batch, double* ms, float* outC, float* outF) {
+// The reference's stepN (lbm_solver.cpp:1132-1390) in batches of `batch`
+// steps: per step the coarse collide + ghost refresh; with the patch, m
+// times the fill of the fine shell at weight half/m, ghost refresh, fine
+// collide, ghost refresh, then the restriction + coarse ghost refresh; the
+// watchdog every 200 steps (coarse flagBase 0, fine 2, offset steps * 977).
+// Per batch, after its steps: the force reduction (fine level when present,
+// the reference's forcesFromFine) and the wall-model updates of the levels
+// with a list. Times `steps` after `warmup` (both rounded up to whole
+// batches is NOT done: a partial last batch is a shorter stepN call).
+extern "C" int refgpu_run_full(const RefRunIn* in, RefRunOut* out) {
+    if (!in || !out) return -1;
+    *out = RefRunOut{};
+    const bool refined = in->refined != 0;
+    const bool wm = in->wm != 0;
     CUfunction collide = wm ? gCollideWM : gCollide;
-    if (!collide || !gGhost || !gFill || !gRestrict || factor < 2 || steps < 1 || batch < 1 || !cflags || !fflags) {
+    const bool needWall = in->coarse.wallCount > 0 || (refined && in->fine.wallCount > 0);
+    if (!collide || !gGhost || (refined && (!gFill || !gRestrict)) || (needWall && (!gWall || !wm))
+        || (in->watchdog && !gWatchdog) || (in->forces && !(wm ? gForceWM : gForce)) || in->steps < 1
+        || in->batch < 1 || in->warmup < 0 || !in->coarse.flags || (refined && !in->fine.flags)) {
         gErr = "bad arguments or modules not loaded";
         return -1;
     }
-    if (fnx != factor * (bx1 - bx0) || fny != factor * (by1 - by0) || fnz != factor * cnz || bx0 < 3 || by0 < 3
-        || bx1 > cnx - 3 || by1 > cny - 3) {
+    const int m = in->factor;
+    if (refined && (m < 2 || in->fine.nx != m * (in->bx1 - in->bx0) || in->fine.ny != m * (in->by1 - in->by0)
+                    || in->fine.nz != m * in->coarse.nz || in->bx0 < 3 || in->by0 < 3
+                    || in->bx1 > in->coarse.nx - 3 || in->by1 > in->coarse.ny - 3)) {
         gErr = "patch dims do not match the box";
         return -1;
     }
     PaddedLevel C, F;
-    float *rho = nullptr, *u = nullptr, *v = nullptr, *w = nullptr;
-    bool good = C.alloc(cnx, cny, cnz, cflags, uIn, wm != 0) && F.alloc(fnx, fny, fnz, fflags, uIn, wm != 0);
+    float *rho = nullptr, *u = nullptr, *v = nullptr, *w = nullptr, *dForce = nullptr;
+    int* dTrips = nullptr;
+    const long long total = static_cast<long long>(in->warmup) + in->steps;
+    const int maxChecks = static_cast<int>(total / kWatchdogPeriod) + 1;
+    bool good = C.alloc(in->coarse, in->uIn, wm) && (!refined || F.alloc(in->fine, in->uIn, wm));
     for (float** p : {&rho, &u, &v, &w})
         if (good) good = cudaMalloc(p, C.n * sizeof(float)) == cudaSuccess;
+    if (good) good = cudaMalloc(&dForce, 3 * sizeof(float)) == cudaSuccess;
+    if (good) good = cudaMalloc(&dTrips, maxChecks * sizeof(int)) == cudaSuccess;
+    if (good) good = cudaMemset(dTrips, 0, maxChecks * sizeof(int)) == cudaSuccess;
+    auto cleanup = [&]() {
+        C.release();
+        F.release();
+        for (float* p : {rho, u, v, w, dForce}) if (p) cudaFree(p);
+        if (dTrips) cudaFree(dTrips);
+    };
     if (!good) {
         if (gErr.empty()) gErr = "allocation failed";
-        C.release(); F.release();
-        for (float* p : {rho, u, v, w}) if (p) cudaFree(p);
+        cleanup();
         return -1;
     }
-    const float smagPre = cs > 0.0f ? 18.0f * 1.41421356f * cs * cs : 0.0f;
-    const float tauF = static_cast<float>(factor) * (tau - 0.5f) + 0.5f;   // fineTauFor
-    const float neqScale = tauF / (static_cast<float>(factor) * tau);
-    const float neqScaleInv = (static_cast<float>(factor) * tau) / tauF;
-    const int rx0 = bx0 + 2, ry0 = by0 + 2, rx1 = bx1 - 2, ry1 = by1 - 2;   // kRestrictBandCoarse
+    const float smagPre = in->cs > 0.0f ? 18.0f * 1.41421356f * in->cs * in->cs : 0.0f;
+    const float tau = in->tau, lambda = in->lambda, uIn = in->uIn;
+    const float tauF = static_cast<float>(m) * (tau - 0.5f) + 0.5f;   // fineTauFor
+    const float neqScale = tauF / (static_cast<float>(m) * tau);
+    const float neqScaleInv = (static_cast<float>(m) * tau) / tauF;
+    const int rx0 = in->bx0 + 2, ry0 = in->by0 + 2, rx1 = in->bx1 - 2, ry1 = in->by1 - 2;   // kRestrictBandCoarse
     int cs_ = 0, fs = 0;
+    long long steps = 0;
+    int checks = 0, sinceWatchdog = 0;
     auto step = [&](int writeMacro) -> bool {
         if (!launch_collide(collide, C, C.f[cs_], C.f[1 - cs_], rho, u, v, w, tau, lambda, smagPre, uIn, writeMacro))
             return false;
         if (!launch_ghost(C, C.f[1 - cs_])) return false;
-        for (int half = 0; half < factor; ++half) {
-            const float* a_t0 = C.f[cs_];
-            const float* a_t1 = C.f[1 - cs_];
-            const std::uint8_t* a_cfl = C.flags;
+        if (refined) {
+            for (int half = 0; half < m; ++half) {
+                const float* a_t0 = C.f[cs_];
+                const float* a_t1 = C.f[1 - cs_];
+                const std::uint8_t* a_cfl = C.flags;
+                const std::uint8_t* a_ffl = F.flags;
+                float* a_ff = F.f[fs];
+                long long a_fn = F.n, a_fnxny = F.nxny, a_fnpad = F.npad, a_cnxny = C.nxny, a_cnpad = C.npad;
+                int a_fnx = F.nx, a_fny = F.ny, a_cnx = C.nx, a_cnz = C.nz, a_bx0 = in->bx0, a_by0 = in->by0,
+                    a_full = 0;
+                float a_inv = 1.0f / static_cast<float>(m);
+                float a_tw = static_cast<float>(half) / static_cast<float>(m), a_neq = neqScale;
+                void* fargs[] = {&a_t0, &a_t1, &a_cfl, &a_ffl, &a_ff, &a_fn, &a_fnxny, &a_fnpad, &a_fnx, &a_fny,
+                                 &a_cnxny, &a_cnpad, &a_cnx, &a_cnz, &a_bx0, &a_by0, &a_inv, &a_tw, &a_neq, &a_full};
+                const unsigned fgrid = static_cast<unsigned>((F.n + kBlock - 1) / kBlock);
+                if (!ok(cuLaunchKernel(gFill, fgrid, 1, 1, kBlock, 1, 1, 0, nullptr, fargs, nullptr), "fill launch"))
+                    return false;
+                if (!launch_ghost(F, F.f[fs])) return false;
+                if (!launch_collide(collide, F, F.f[fs], F.f[1 - fs], nullptr, nullptr, nullptr, nullptr, tauF, lambda,
+                                    smagPre, uIn, 0))
+                    return false;
+                if (!launch_ghost(F, F.f[1 - fs])) return false;
+                fs = 1 - fs;
+            }
+            const float* a_ff = F.f[fs];
             const std::uint8_t* a_ffl = F.flags;
-            float* a_ff = F.f[fs];
-            long long a_fn = F.n, a_fnxny = F.nxny, a_fnpad = F.npad, a_cnxny = C.nxny, a_cnpad = C.npad;
-            int a_fnx = F.nx, a_fny = F.ny, a_cnx = C.nx, a_cnz = C.nz, a_bx0 = bx0, a_by0 = by0, a_full = 0;
-            float a_inv = 1.0f / static_cast<float>(factor);
-            float a_tw = static_cast<float>(half) / static_cast<float>(factor), a_neq = neqScale;
-            void* fargs[] = {&a_t0, &a_t1, &a_cfl, &a_ffl, &a_ff, &a_fn, &a_fnxny, &a_fnpad, &a_fnx, &a_fny,
-                             &a_cnxny, &a_cnpad, &a_cnx, &a_cnz, &a_bx0, &a_by0, &a_inv, &a_tw, &a_neq, &a_full};
-            const unsigned fgrid = static_cast<unsigned>((F.n + kBlock - 1) / kBlock);
-            if (!ok(cuLaunchKernel(gFill, fgrid, 1, 1, kBlock, 1, 1, 0, nullptr, fargs, nullptr), "fill launch"))
+            float* a_fc = C.f[1 - cs_];
+            const std::uint8_t* a_cfl = C.flags;
+            long long a_fnxny = F.nxny, a_fnpad = F.npad, a_cnxny = C.nxny, a_cnpad = C.npad;
+            int a_fnx = F.nx, a_cnx = C.nx, a_cnz = C.nz, a_rx0 = rx0, a_ry0 = ry0, a_rx1 = rx1, a_ry1 = ry1;
+            int a_bx0 = in->bx0, a_by0 = in->by0, a_m = m, a_wm = writeMacro;
+            float a_inv = neqScaleInv;
+            void* rargs[] = {&a_ff, &a_ffl, &a_fc, &a_cfl, &a_fnxny, &a_fnpad, &a_fnx, &a_cnxny, &a_cnpad, &a_cnx,
+                             &a_cnz, &a_rx0, &a_ry0, &a_rx1, &a_ry1, &a_bx0, &a_by0, &a_m, &a_inv,
+                             &rho, &u, &v, &w, &a_wm};
+            const long long rtotal = static_cast<long long>(rx1 - rx0) * (ry1 - ry0) * C.nz;
+            const unsigned rgrid = static_cast<unsigned>((rtotal + kBlock - 1) / kBlock);
+            if (!ok(cuLaunchKernel(gRestrict, rgrid, 1, 1, kBlock, 1, 1, 0, nullptr, rargs, nullptr),
+                    "restrict launch"))
                 return false;
-            if (!launch_ghost(F, F.f[fs])) return false;
-            if (!launch_collide(collide, F, F.f[fs], F.f[1 - fs], nullptr, nullptr, nullptr, nullptr, tauF, lambda,
-                                smagPre, uIn, 0))
-                return false;
-            if (!launch_ghost(F, F.f[1 - fs])) return false;
-            fs = 1 - fs;
+            if (!launch_ghost(C, C.f[1 - cs_])) return false;
         }
-        const float* a_ff = F.f[fs];
-        const std::uint8_t* a_ffl = F.flags;
-        float* a_fc = C.f[1 - cs_];
-        const std::uint8_t* a_cfl = C.flags;
-        long long a_fnxny = F.nxny, a_fnpad = F.npad, a_cnxny = C.nxny, a_cnpad = C.npad;
-        int a_fnx = F.nx, a_cnx = C.nx, a_cnz = C.nz, a_rx0 = rx0, a_ry0 = ry0, a_rx1 = rx1, a_ry1 = ry1;
-        int a_bx0 = bx0, a_by0 = by0, a_m = factor, a_wm = writeMacro;
-        float a_inv = neqScaleInv;
-        void* rargs[] = {&a_ff, &a_ffl, &a_fc, &a_cfl, &a_fnxny, &a_fnpad, &a_fnx, &a_cnxny, &a_cnpad, &a_cnx,
-                         &a_cnz, &a_rx0, &a_ry0, &a_rx1, &a_ry1, &a_bx0, &a_by0, &a_m, &a_inv,
-                         &rho, &u, &v, &w, &a_wm};
-        const long long total = static_cast<long long>(rx1 - rx0) * (ry1 - ry0) * cnz;
-        const unsigned rgrid = static_cast<unsigned>((total + kBlock - 1) / kBlock);
-        if (!ok(cuLaunchKernel(gRestrict, rgrid, 1, 1, kBlock, 1, 1, 0, nullptr, rargs, nullptr), "restrict launch"))
-            return false;
-        if (!launch_ghost(C, C.f[1 - cs_])) return false;
         cs_ = 1 - cs_;
+        ++steps;
+        if (in->watchdog && ++sinceWatchdog >= kWatchdogPeriod && checks < maxChecks) {
+            sinceWatchdog = 0;
+            int* flag = dTrips + checks++;
+            if (!launch_watchdog(C, C.f[cs_], steps * 977, flag, 0)) return false;
+            if (refined && !launch_watchdog(F, F.f[fs], steps * 977, flag, 2)) return false;
+        }
         return true;
     };
-    for (int s = 0; s < warmup && good; ++s) good = step((s + 1) % batch == 0);
+    auto batchEnd = [&]() -> bool {
+        if (in->forces && !launch_force(refined ? F : C, refined ? F.f[fs] : C.f[cs_], dForce)) return false;
+        const float utCut = 1e-3f * uIn;
+        if (C.wl.count > 0 && !launch_wall(C, C.f[cs_], (tau - 0.5f) / 3.0f, utCut)) return false;
+        if (refined && F.wl.count > 0 && !launch_wall(F, F.f[fs], (tauF - 0.5f) / 3.0f, utCut)) return false;
+        return true;
+    };
+    // stepN(n) calls of `batch` steps; macroscopic fields on each call's last step.
+    auto run = [&](long long count) -> bool {
+        for (long long done = 0; done < count && good;) {
+            const long long nb = count - done < in->batch ? count - done : in->batch;
+            for (long long i = 0; i < nb && good; ++i) good = step(i == nb - 1);
+            if (good) good = batchEnd();
+            done += nb;
+        }
+        return good;
+    };
+    run(in->warmup);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaDeviceSynchronize();
     cudaEventRecord(e0, nullptr);
-    for (int s = 0; s < steps && good; ++s) good = step((s + 1) % batch == 0);
+    run(in->steps);
     cudaEventRecord(e1, nullptr);
     cudaError_t e = cudaEventSynchronize(e1);
     float t = 0.0f;
@@ -384,24 +627,38 @@ extern "C" int refgpu_run_refined(int cnx, int cny, int cnz, const std::uint8_t*
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e == cudaSuccess) e = cudaGetLastError();
-    // Final states (unpadded FP32 SoA) when asked for.
     if (good && e == cudaSuccess) {
-        for (int q = 0; q < kQ && outC; ++q)
-            cudaMemcpy(outC + q * C.n, C.f[cs_] + q * C.npad + C.nxny, static_cast<size_t>(C.n) * sizeof(float),
-                       cudaMemcpyDeviceToHost);
-        for (int q = 0; q < kQ && outF; ++q)
-            cudaMemcpy(outF + q * F.n, F.f[fs] + q * F.npad + F.nxny, static_cast<size_t>(F.n) * sizeof(float),
-                       cudaMemcpyDeviceToHost);
+        std::vector<int> trips(static_cast<size_t>(maxChecks));
+        cudaMemcpy(trips.data(), dTrips, maxChecks * sizeof(int), cudaMemcpyDeviceToHost);
+        for (int k = 0; k < checks; ++k)
+            if (trips[static_cast<size_t>(k)] != 0) {
+                out->tripStep = static_cast<long long>(k + 1) * kWatchdogPeriod;
+                out->tripFlag = trips[static_cast<size_t>(k)];
+                break;
+            }
+        cudaMemcpy(out->force, dForce, 3 * sizeof(float), cudaMemcpyDeviceToHost);
+        const RefLevelIn* lv[2] = {&in->coarse, &in->fine};
+        PaddedLevel* pl[2] = {&C, &F};
+        const int cur[2] = {cs_, fs};
+        for (int k = 0; k < (refined ? 2 : 1); ++k) {
+            if (lv[k]->outF)
+                for (int q = 0; q < kQ; ++q)
+                    cudaMemcpy(lv[k]->outF + q * pl[k]->n, pl[k]->f[cur[k]] + q * pl[k]->npad + pl[k]->nxny,
+                               static_cast<size_t>(pl[k]->n) * sizeof(float), cudaMemcpyDeviceToHost);
+            if (lv[k]->outUTau && pl[k]->wl.count > 0)
+                cudaMemcpy(lv[k]->outUTau, pl[k]->wl.uTau, static_cast<size_t>(pl[k]->wl.count) * sizeof(float),
+                           cudaMemcpyDeviceToHost);
+        }
         e = cudaGetLastError();
     }
-    C.release(); F.release();
-    for (float* p : {rho, u, v, w}) if (p) cudaFree(p);
+    out->checks = checks;
+    out->stepsRun = steps;
+    cleanup();
     if (!good) return -1;
     if (e != cudaSuccess) {
         gErr = cudaGetErrorString(e);
         return -1;
     }
-    *ms = t;
+    out->ms = t;
     return 0;
 }
-

@@ -470,6 +470,31 @@ def test_fused_child_average_equals_separate_pass(fc, storage):
         assert np.abs(out[True][1] - out[False][1]).max() <= 2e-4
 
 
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_overlapped_fills_equal_serial(fc, storage):
+    """Interface fills on the side stream (overlapped with the coarse and the
+    first fine collide) give the same coarse and fine populations, bit for
+    bit, as the fills in line on the solver stream: 60 steps of the airfoil
+    tunnel with its 2:1 patch and the wall model, in batches of 20."""
+    from foil_cfd_gb300.tunnels import airfoil_tunnel
+    t = airfoil_tunnel(160, 64, 16, chord=64, aoa=6.0)
+    out = {}
+    for overlap in (True, False):
+        s = fc.LBMSolver()
+        s.init(t.dims, fc.scaling_direct(0.52, t.u_lat, t.chord_cells), t.flags, storage=storage, les_cs=0.1)
+        s.set_wall_model_enabled(True)
+        s.set_startup_ramp_enabled(False)
+        s.reset()
+        s.init_refinement(t.box, t.factor, t.fine_flags)
+        s.set_overlap_fills(overlap)
+        for _ in range(3):
+            assert s.step_n(20) == 0
+        assert not s.nan_detected()
+        out[overlap] = (s.export_f32(), s.export_fine_f32())
+    assert np.array_equal(out[True][0], out[False][0])
+    assert np.array_equal(out[True][1], out[False][1])
+
+
 @pytest.mark.parametrize("kernel", ["cell", "staged"])
 @pytest.mark.parametrize("case,steps,slip", [("f1", 1, False), ("f20", 20, False), ("f20w", 20, True)])
 def test_qlibb_collide_vs_reference_golden(fc, golden, case, steps, slip, kernel):

@@ -57,6 +57,8 @@ def test_force_noalloc_matches_solver_reduction(built_lib, oracle_mod):
     s.reset()
     s.import_f32(f0)
 
+    # The entry point reads FP32 populations: this solver's buffer is one.
+    assert lib.fcfd_f_bytes(s._h) == 19 * 4 * n
     cells, masks = link_list(dims, flags)
     d_cells = torch.from_numpy(cells.view(np.int32)).cuda()
     d_masks = torch.from_numpy(masks.view(np.int32)).cuda()
@@ -91,6 +93,35 @@ def test_force_noalloc_matches_solver_reduction(built_lib, oracle_mod):
     for _ in range(2):
         got = call(slip)
         assert np.allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max()), (got, ref)
+
+    # A long list (the same links repeated, 300,000 entries = 1,172 blocks) so
+    # that the final pass sums several partials per thread, against an FP64
+    # host sum of the same per-link terms (t = 2 f_q - corr in FP32, widened).
+    reps = 300_000 // len(cells) + 1
+    big_cells = np.tile(cells, reps)[:300_000]
+    big_masks = np.tile(masks, reps)[:300_000]
+    d_big_cells = torch.from_numpy(big_cells.view(np.int32)).cuda()
+    d_big_masks = torch.from_numpy(big_masks.view(np.int32)).cuda()
+    f_host = s.export_f32().reshape(19, n)
+    _, slip_now = s.export_wall_state(0)
+    uw = [slip_now[k][big_cells].view(np.float16).astype(np.float32) for k in range(3)]
+    acc = np.zeros(3)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
+    for q in range(1, 19):
+        on = ((big_masks >> q) & 1) == 1
+        dot = (np.float32(CX[q]) * uw[0] + np.float32(CY[q]) * uw[1]) + np.float32(CZ[q]) * uw[2]
+        corr = (np.float32(6.0) * w[q]) * dot
+        t = (np.float32(2.0) * f_host[q, big_cells] - corr).astype(np.float64)
+        acc += np.array([CX[q], CY[q], CZ[q]]) * t[on].sum()
+    for _ in range(2):
+        torch.cuda.synchronize()
+        rc = lib.fcfd_force_links_noalloc(lib.fcfd_active_f(s._h), n, d_big_cells.data_ptr(), d_big_masks.data_ptr(),
+                                          len(big_cells), slip[0].data_ptr(), slip[1].data_ptr(), slip[2].data_ptr(),
+                                          out.data_ptr(), None)
+        assert rc == 0
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.allclose(got, acc, rtol=1e-10, atol=1e-10 * np.abs(acc).max()), (got, acc)
 
     # A list longer than the static scratch holds is refused before any work.
     too_many = capi.load().fcfd_force_links_noalloc(lib.fcfd_active_f(s._h), n, d_cells.data_ptr(),
