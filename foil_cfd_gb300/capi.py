@@ -114,7 +114,6 @@ _SIGS = {
     "fcfd_set_startup_ramp": (None, [P, C.c_int]),
     "fcfd_set_force_ema_window": (None, [P, C.c_float]),
     "fcfd_mirror_buffers": (C.c_int, [P]),
-    "fcfd_set_overlap_fills": (C.c_int, [P, C.c_int]),
     "fcfd_step_n": (C.c_int, [P, C.c_int]),
     "fcfd_synchronize": (C.c_int, [P]),
     "fcfd_step_count": (C.c_longlong, [P]),

@@ -39,7 +39,9 @@ __device__ __forceinline__ void limited_moments(const float (&fi)[kQ], float& rh
     ux = rn_mul(jx, inv); uy = rn_mul(jy, inv); uz = rn_mul(jz, inv);
     const float u2 = rn_add(rn_add(rn_mul(ux, ux), rn_mul(uy, uy)), rn_mul(uz, uz));
     if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
-        const float sc = rn_mul(kMaxSimSpeed, 1.0f / sqrtf(u2));
+        // The hardware rsqrtf of the reference's GPU build (lbm_refine.cu:238,
+        // 309); only cells beyond |u| = 0.3 take this branch.
+        const float sc = rn_mul(kMaxSimSpeed, rsqrtf(u2));
         ux = rn_mul(ux, sc); uy = rn_mul(uy, sc); uz = rn_mul(uz, sc);
     }
     rho = r;

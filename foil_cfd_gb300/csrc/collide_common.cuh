@@ -162,8 +162,10 @@ __device__ __forceinline__ void collide_exact(float (&f)[kQ], float tau0, float 
     float ux = jx * invRho, uy = jy * invRho, uz = jz * invRho;
     const float u2 = ux * ux + uy * uy + uz * uz;
     if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
-        // 1/sqrt as IEEE operations (the reference's rsqrtf is approximate).
-        const float s = kMaxSimSpeed * (1.0f / sqrtf(u2));
+        // The hardware reciprocal square root, as the reference's GPU build
+        // evaluates rsqrtf (lbm_core.cu:413); its CPU build and the oracle
+        // use IEEE 1/sqrtf. Only cells beyond |u| = 0.3 take this branch.
+        const float s = kMaxSimSpeed * rsqrtf(u2);
         ux *= s; uy *= s; uz *= s;
     }
     float feq[kQ];
@@ -200,69 +202,146 @@ __device__ __forceinline__ void collide_exact(float (&f)[kQ], float tau0, float 
     rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
 }
 
-__device__ __forceinline__ void collide_dev(float (&g)[kQ], float tau0, float lambda, float smagPre,
-                                            float& rhoO, float& uxO, float& uyO, float& uzO) {
+// ---- lane arithmetic of the deviation body ------------------------------------
+// Every operation is an explicit round-to-nearest intrinsic, so the compiler
+// contracts nothing on its own: the body on one cell (float lanes) and on an
+// x-pair of cells (float2 lanes on the packed FADD2 / FMUL2 / FFMA2 path,
+// which rounds each lane exactly like the scalar instruction) give the same
+// bits for a cell.
+template <class V> struct Lane;
+template <> struct Lane<float> {
+    __device__ __forceinline__ static float s(float v) { return v; }
+    __device__ __forceinline__ static float add(float a, float b) { return __fadd_rn(a, b); }
+    __device__ __forceinline__ static float sub(float a, float b) { return __fsub_rn(a, b); }
+    __device__ __forceinline__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+    __device__ __forceinline__ static float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    __device__ __forceinline__ static float neg(float a) { return -a; }
+    __device__ __forceinline__ static float rcp(float a) { return rcp_approx(a); }
+    __device__ __forceinline__ static float sqrt(float a) { return sqrt_approx(a); }
+};
+template <> struct Lane<float2> {
+    __device__ __forceinline__ static float2 s(float v) { return make_float2(v, v); }
+    __device__ __forceinline__ static float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+    __device__ __forceinline__ static float2 sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+    __device__ __forceinline__ static float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+    __device__ __forceinline__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+    __device__ __forceinline__ static float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+    __device__ __forceinline__ static float2 rcp(float2 a) { return make_float2(rcp_approx(a.x), rcp_approx(a.y)); }
+    __device__ __forceinline__ static float2 sqrt(float2 a) { return make_float2(sqrt_approx(a.x), sqrt_approx(a.y)); }
+};
+
+/// Density floor of one lane: rho = max-floored 1 + dr, rm1 = rho - 1.
+__device__ __forceinline__ void rho_floor(float dr, float& rho, float& rm1) {
+    const float r = __fadd_rn(1.0f, dr);
+    const bool floored = r < kRhoFloor;
+    rho = floored ? kRhoFloor : r;
+    rm1 = floored ? kRhoFloor - 1.0f : dr;
+}
+__device__ __forceinline__ void rho_floor(float2 dr, float2& rho, float2& rm1) {
+    rho_floor(dr.x, rho.x, rm1.x);
+    rho_floor(dr.y, rho.y, rm1.y);
+}
+
+/// The |u| <= 0.3 limiter of one lane (u2 recomputed when it acts).
+__device__ __forceinline__ void limit_u(float& ux, float& uy, float& uz, float& u2) {
+    if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
+        const float sc = __fmul_rn(kMaxSimSpeed, rsqrtf(u2));
+        ux = __fmul_rn(ux, sc); uy = __fmul_rn(uy, sc); uz = __fmul_rn(uz, sc);
+        u2 = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux)));
+    }
+}
+__device__ __forceinline__ void limit_u(float2& ux, float2& uy, float2& uz, float2& u2) {
+    if (u2.x > kMaxSimSpeed * kMaxSimSpeed || u2.y > kMaxSimSpeed * kMaxSimSpeed) {
+        limit_u(ux.x, uy.x, uz.x, u2.x);
+        limit_u(ux.y, uy.y, uz.y, u2.y);
+    }
+}
+
+/// c_a . u of pair direction a, components in the order x, y, z.
+template <class V>
+__device__ __forceinline__ V dot_lane(int a, V ux, V uy, V uz) {
+    using L = Lane<V>;
+    V d = L::s(0.0f);
+    bool any = false;
+    if (cx(a) != 0) { d = cx(a) > 0 ? ux : L::neg(ux); any = true; }
+    if (cy(a) != 0) { d = any ? (cy(a) > 0 ? L::add(d, uy) : L::sub(d, uy)) : (cy(a) > 0 ? uy : L::neg(uy)); any = true; }
+    if (cz(a) != 0) d = any ? (cz(a) > 0 ? L::add(d, uz) : L::sub(d, uz)) : (cz(a) > 0 ? uz : L::neg(uz));
+    return d;
+}
+
+/// TRT + Smagorinsky collision on the deviations g_q = f_q - w_q of one cell
+/// (V = float) or of an x-pair of cells (V = float2).
+template <class V>
+__device__ __forceinline__ void collide_dev_lanes(V (&g)[kQ], float tau0, float lambda, float smagPre, V& rhoO,
+                                                  V& uxO, V& uyO, V& uzO) {
+    using L = Lane<V>;
     // Pair sums of f are s[p] + 2 w_p, differences d[p] as for f. The
     // update needs only these (symmetric and antisymmetric parts), so the
     // pair's own values are not kept.
-    float s[10], d[10];
+    V s[10], d[10];
 #pragma unroll
     for (int p = 1; p <= 9; ++p) {
-        s[p] = g[2 * p - 1] + g[2 * p];
-        d[p] = g[2 * p - 1] - g[2 * p];
+        s[p] = L::add(g[2 * p - 1], g[2 * p]);
+        d[p] = L::sub(g[2 * p - 1], g[2 * p]);
     }
     // Pair p has velocity c_{2p-1}: p1 (1,0,0) p2 (0,1,0) p3 (0,0,1)
     // p4 (1,1,0) p5 (1,0,1) p6 (0,1,1) p7 (1,-1,0) p8 (1,0,-1) p9 (0,1,-1).
-    const float dr = g[0] + ((s[1] + s[2]) + (s[3] + s[4])) + ((s[5] + s[6]) + (s[7] + s[8])) + s[9];
-    const float jx = (d[1] + d[4]) + (d[5] + d[7]) + d[8];
-    const float jy = (d[2] + d[4]) + (d[6] - d[7]) + d[9];
-    const float jz = (d[3] + d[5]) + (d[6] - d[8]) - d[9];
-    const bool floored = 1.0f + dr < kRhoFloor;
-    const float rho = floored ? kRhoFloor : 1.0f + dr;
-    const float rm1 = floored ? kRhoFloor - 1.0f : dr;   // rho - 1
-    const float inv = rcp_approx(rho);
-    float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-    float u2 = ux * ux + uy * uy + uz * uz;
-    if (u2 > kMaxSimSpeed * kMaxSimSpeed) {
-        const float sc = kMaxSimSpeed * rsqrtf(u2);
-        ux *= sc; uy *= sc; uz *= sc;
-        u2 = ux * ux + uy * uy + uz * uz;
-    }
-    const float rux = rho * ux, ruy = rho * uy;
-    float tauEff = tau0;
+    const V dr = L::add(L::add(L::add(g[0], L::add(L::add(s[1], s[2]), L::add(s[3], s[4]))),
+                               L::add(L::add(s[5], s[6]), L::add(s[7], s[8]))),
+                        s[9]);
+    const V jx = L::add(L::add(L::add(d[1], d[4]), L::add(d[5], d[7])), d[8]);
+    const V jy = L::add(L::add(L::add(d[2], d[4]), L::sub(d[6], d[7])), d[9]);
+    const V jz = L::sub(L::add(L::add(d[3], d[5]), L::sub(d[6], d[8])), d[9]);
+    V rho, rm1;   // rm1 = rho - 1
+    rho_floor(dr, rho, rm1);
+    const V inv = L::rcp(rho);
+    V ux = L::mul(jx, inv), uy = L::mul(jy, inv), uz = L::mul(jz, inv);
+    V u2 = L::fma(uz, uz, L::fma(uy, uy, L::mul(ux, ux)));
+    limit_u(ux, uy, uz, u2);
+    const V rux = L::mul(rho, ux), ruy = L::mul(rho, uy);
+    V tauEff = L::s(tau0);
     if (smagPre > 0.0f) {
         // Non-equilibrium stress: the weights' share of the diagonal
         // (sum of w_q over c_a != 0 = 1/3) cancels against rho/3 up to rho - 1.
-        const float r3 = rm1 * (1.0f / 3.0f);
-        const float nxx = ((s[1] + s[4]) + (s[5] + s[7]) + s[8]) - r3 - rux * ux;
-        const float nyy = ((s[2] + s[4]) + (s[6] + s[7]) + s[9]) - r3 - ruy * uy;
-        const float nzz = ((s[3] + s[5]) + (s[6] + s[8]) + s[9]) - r3 - rho * uz * uz;
-        const float nxy = (s[4] - s[7]) - rux * uy;
-        const float nxz = (s[5] - s[8]) - rux * uz;
-        const float nyz = (s[6] - s[9]) - ruy * uz;
-        const float qbar = sqrt_approx(nxx * nxx + nyy * nyy + nzz * nzz + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz));
-        tauEff = 0.5f * (tau0 + sqrt_approx(tau0 * tau0 + smagPre * qbar * inv));
+        const V r3 = L::mul(rm1, L::s(1.0f / 3.0f));
+        const V nxx = L::fma(L::neg(rux), ux, L::sub(L::add(L::add(L::add(s[1], s[4]), L::add(s[5], s[7])), s[8]), r3));
+        const V nyy = L::fma(L::neg(ruy), uy, L::sub(L::add(L::add(L::add(s[2], s[4]), L::add(s[6], s[7])), s[9]), r3));
+        const V nzz = L::fma(L::neg(L::mul(rho, uz)), uz,
+                             L::sub(L::add(L::add(L::add(s[3], s[5]), L::add(s[6], s[8])), s[9]), r3));
+        const V nxy = L::fma(L::neg(rux), uy, L::sub(s[4], s[7]));
+        const V nxz = L::fma(L::neg(rux), uz, L::sub(s[5], s[8]));
+        const V nyz = L::fma(L::neg(ruy), uz, L::sub(s[6], s[9]));
+        const V dia = L::fma(nzz, nzz, L::fma(nyy, nyy, L::mul(nxx, nxx)));
+        const V off = L::fma(nyz, nyz, L::fma(nxz, nxz, L::mul(nxy, nxy)));
+        const V qbar = L::sqrt(L::fma(L::s(2.0f), off, dia));
+        const V inner = L::fma(L::mul(L::s(smagPre), qbar), inv, L::s(__fmul_rn(tau0, tau0)));
+        tauEff = L::mul(L::s(0.5f), L::add(L::s(tau0), L::sqrt(inner)));
     }
-    const float omP = rcp_approx(tauEff);
-    const float omM = rcp_approx(0.5f + lambda * rcp_approx(tauEff - 0.5f));
+    const V omP = L::rcp(tauEff);
+    const V omM = L::rcp(L::fma(L::s(lambda), L::rcp(L::sub(tauEff, L::s(0.5f))), L::s(0.5f)));
     // feq_q - w_q = w_q (A + 4.5 rho (c_q.u)^2) + 3 w_q rho (c_q.u), A = rho - 1 - 1.5 rho u^2.
-    const float A = rm1 - 1.5f * rho * u2;
-    const float r45 = 4.5f * rho;
-    g[0] = g[0] - omP * (g[0] - (1.0f / 3.0f) * A);
+    const V A = L::fma(L::mul(L::s(-1.5f), rho), u2, rm1);
+    const V r45 = L::mul(L::s(4.5f), rho);
+    g[0] = L::fma(L::neg(omP), L::fma(L::s(-1.0f / 3.0f), A, g[0]), g[0]);
 #pragma unroll
     for (int p = 1; p <= 9; ++p) {
         const int a = 2 * p - 1;
         const float w = wgt(a);
-        const float cu = cx(a) * ux + cy(a) * uy + cz(a) * uz;
-        const float es = w * (A + r45 * cu * cu);
-        const float ea = (3.0f * w * rho) * cu;
-        const float hs = 0.5f * s[p], hd = 0.5f * d[p];
-        const float sym = hs - omP * (hs - es);
-        const float asym = hd - omM * (hd - ea);
-        g[a] = sym + asym;
-        g[a + 1] = sym - asym;
+        const V cu = dot_lane<V>(a, ux, uy, uz);
+        const V es = L::mul(L::s(w), L::fma(L::mul(r45, cu), cu, A));
+        const V ea = L::mul(L::mul(L::s(3.0f * w), rho), cu);
+        const V hs = L::mul(L::s(0.5f), s[p]), hd = L::mul(L::s(0.5f), d[p]);
+        const V sym = L::fma(L::neg(omP), L::sub(hs, es), hs);
+        const V asym = L::fma(L::neg(omM), L::sub(hd, ea), hd);
+        g[a] = L::add(sym, asym);
+        g[a + 1] = L::sub(sym, asym);
     }
     rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
+}
+
+__device__ __forceinline__ void collide_dev(float (&g)[kQ], float tau0, float lambda, float smagPre,
+                                            float& rhoO, float& uxO, float& uyO, float& uzO) {
+    collide_dev_lanes<float>(g, tau0, lambda, smagPre, rhoO, uxO, uyO, uzO);
 }
 
 /// The collision of a cell's 19 populations: f with the exact body, the
@@ -511,6 +590,69 @@ collide_flat_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
     const unsigned z = fdiv(row, divY);
     collide_one<S, WM, EXACT, QL>(src, dst, kind, a, static_cast<int>(cell - row * divX.d),
                                   static_cast<int>(row - z * divY.d), static_cast<int>(z), &off);
+}
+
+// ---- FP16 storage: an x-pair of cells per thread ---------------------------------
+// Thread t updates cells 2t and 2t + 1 of the flattened lattice (nx even, so
+// a pair never straddles a row). When both are bulk fluid cells away from
+// every periodic face, the pair is one unit: the 9 pulls with c_x = 0 are
+// one aligned 4-byte half2 load each (both cells' sources sit side by side),
+// the 10 others two 2-byte loads, the collision runs on float2 lanes (packed
+// FADD2 / FMUL2 / FFMA2: half the arithmetic instructions per cell), and
+// each direction is stored as one half2. Any other pair takes the one-cell
+// path for both cells. The float2 body rounds each lane like the one-cell
+// body, so every cell gets the same bits either way.
+constexpr int kPairX = 128;
+/// Resident 128-thread blocks per SM the pair kernel is compiled for.
+constexpr int kPairMinBlocks = 4;
+
+__device__ __forceinline__ float2 ld_pf2(const __half* p) {
+    unsigned v;
+    asm("ld.global.nc.L2::256B.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    __half2 h;
+    *reinterpret_cast<unsigned*>(&h) = v;
+    return __half22float2(h);
+}
+
+template <bool WM, bool QL>
+__global__ void __launch_bounds__(kPairX, kPairMinBlocks)
+collide_pair_f16_kernel(const __half* __restrict__ src, __half* __restrict__ dst,
+                        const std::uint8_t* __restrict__ kind, CollideArgs a,
+                        const __grid_constant__ PullOffsets off, FastDiv divX, FastDiv divY) {
+    const unsigned cell = 2u * (blockIdx.x * kPairX + threadIdx.x);
+    if (cell >= static_cast<unsigned long long>(a.n)) return;
+    const unsigned row = fdiv(cell, divX);
+    const unsigned z = fdiv(row, divY);
+    const int x = static_cast<int>(cell - row * divX.d), y = static_cast<int>(row - z * divY.d);
+    // Both kind bytes: flag 0 (fluid) and no near-wall bit in either.
+    const unsigned kk = *reinterpret_cast<const unsigned short*>(kind + cell);
+    const bool bulk = (kk & 0x8F8Fu) == 0 && x >= 2 && x <= a.nx - 4 && y >= 1 && y <= a.ny - 2
+                      && static_cast<int>(z) >= 1 && static_cast<int>(z) <= a.nz - 2;
+    if (!bulk) {
+        collide_one<StoreF16, WM, false, QL>(src, dst, kind, a, x, y, static_cast<int>(z), &off);
+        collide_one<StoreF16, WM, false, QL>(src, dst, kind, a, x + 1, y, static_cast<int>(z), &off);
+        return;
+    }
+    float2 g[kQ];
+    const __half* base = src + cell;
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+        const __half* p = byte_add(base, off.pull[q]);
+        if (cx(q) == 0) g[q] = ld_pf2(p);
+        else g[q] = make_float2(ld_pf(p), ld_pf(p + 1));
+    }
+    float2 r, ux, uy, uz;
+    collide_dev_lanes<float2>(g, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
+    __half* ob = dst + cell;
+#pragma unroll
+    for (int q = 0; q < kQ; ++q)
+        *reinterpret_cast<__half2*>(byte_add(ob, off.slice[q])) = __floats2half2_rn(g[q].x, g[q].y);
+    if (a.writeMacro) {
+        *reinterpret_cast<float2*>(a.rho + cell) = r;
+        *reinterpret_cast<float2*>(a.u + cell) = ux;
+        *reinterpret_cast<float2*>(a.v + cell) = uy;
+        *reinterpret_cast<float2*>(a.w + cell) = uz;
+    }
 }
 
 // ---- warm-restart flag edits (applyFlagEditsKernel, lbm_core.cu:644-717) -----
@@ -1016,6 +1158,20 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
         if (grid > rows) grid = rows;
         kern<<<static_cast<unsigned>(grid), kStagedThreads, plan.smem, st>>>(src, dst, kind, a, plan.stages);
         return cudaGetLastError();
+    }
+    if constexpr (!EXACT && std::is_same_v<S, StoreF16>) {
+        // FP16 storage: the pair kernel unless the one-cell kernel is asked
+        // for (nx even, so pairs never straddle rows).
+        if ((p.kernel == 0 || p.kernel == 3) && d.nx % 2 == 0 && d.nx >= 4 && d.ny >= 2) {
+            const FastDiv fx = fast_div(static_cast<unsigned>(d.nx)), fy = fast_div(static_cast<unsigned>(d.ny));
+            const PullOffsets po = pull_offsets<T>(d.nx, d.ny, a.n);
+            const unsigned blocks = static_cast<unsigned>((a.n / 2 + kPairX - 1) / kPairX);
+            const bool ql = a.qFrac != nullptr;
+            auto kern = wm ? (ql ? collide_pair_f16_kernel<true, true> : collide_pair_f16_kernel<true, false>)
+                           : (ql ? collide_pair_f16_kernel<false, true> : collide_pair_f16_kernel<false, false>);
+            kern<<<blocks, kPairX, 0, st>>>(src, dst, kind, a, po, fx, fy);
+            return cudaGetLastError();
+        }
     }
     const int bx = d.nx >= kCellBlockX ? kCellBlockX : ((d.nx + 31) / 32) * 32;
     const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),

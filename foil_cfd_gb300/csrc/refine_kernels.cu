@@ -22,8 +22,9 @@
 // filters from scratch.
 //
 // Built with --fmad=false: every expression keeps the reference's rounding,
-// so fill and restriction are bit-identical to the reference kernels (the
-// limiter's 1/sqrt is evaluated as IEEE operations).
+// so fill and restriction are bit-identical to the reference kernels
+// compiled without contraction (the limiter's rsqrtf is the same hardware
+// instruction the reference's GPU build uses).
 #include "child_record.cuh"
 #include "d3q19.cuh"
 #include "kernels.h"

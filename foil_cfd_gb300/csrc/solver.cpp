@@ -198,12 +198,6 @@ struct fcfd_solver {
     } staged[3];
     cudaStream_t copyStream = nullptr;
     cudaEvent_t evStaged = nullptr, evCommitted = nullptr;
-    // Interface fills of a factor-2 patch on a side stream, concurrent with
-    // the coarse collide (first sub-step's fill) and with the first fine
-    // collide (second sub-step's fill); events fork and join the streams.
-    bool overlapFills = true;
-    cudaStream_t fillStream = nullptr;
-    cudaEvent_t evFork0 = nullptr, evFork1 = nullptr, evFill0 = nullptr, evFill1 = nullptr;
     int factor = 2;
     fcfd_patch_box box{};
     fcfd_scaling fineScaling{};
@@ -614,27 +608,8 @@ struct fcfd_solver {
         return cudaSuccess;
     }
 
-    cudaError_t ensureFillStream() {
-        if (fillStream) return cudaSuccess;
-        if (auto e = cudaStreamCreateWithFlags(&fillStream, cudaStreamNonBlocking); e != cudaSuccess) return e;
-        for (cudaEvent_t* ev : {&evFork0, &evFork1, &evFill0, &evFill1})
-            if (auto e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming); e != cudaSuccess) return e;
-        return cudaSuccess;
-    }
-
-    void freeFillStream() {
-        if (fillStream) {
-            cudaStreamSynchronize(fillStream);
-            cudaStreamDestroy(fillStream);
-            fillStream = nullptr;
-        }
-        for (cudaEvent_t* ev : {&evFork0, &evFork1, &evFill0, &evFill1})
-            if (*ev) { cudaEventDestroy(*ev); *ev = nullptr; }
-    }
-
     void freeAll() {
         if (stream) cudaStreamSynchronize(stream);
-        freeFillStream();
         freeStaged();
         freeFine();
         coarse.free_all();
@@ -724,47 +699,7 @@ struct fcfd_solver {
             p.writeMacro = (i == n - 1) ? 1 : 0;
             p.status = dStatus;
             p.kernel = collideKernel;
-            // Factor-2 patch without a finer level: both interface fills run
-            // on the side stream. The first sub-step's fill (time weight 0)
-            // reads only the coarse source level, which the coarse collide
-            // reads too, and writes only the fine source buffer's shell
-            // cells, which nothing reads before the first fine collide: it
-            // runs during the coarse collide. The second sub-step's fill
-            // needs the collided coarse level and writes only the shell cells
-            // of the buffer the first fine collide writes everywhere else: it
-            // runs during that collide. The fine collides wait for them.
-            const bool overlap = fineActive && overlapFills && factor == 2 && !finerActive;
-            if (overlap) {
-                if (auto e = ensureFillStream(); e != cudaSuccess) return e;
-                const float tc = p.tau, tf = fineTau(tc, 2);
-                cudaEventRecord(evFork0, stream);
-                cudaStreamWaitEvent(fillStream, evFork0, 0);
-                ++launches;
-                // The time-weight-0 fill is given the source level as its
-                // second level too: it must not read the level the coarse
-                // collide is writing. s0 + 0 (s1 - s0) is s0 for any finite
-                // s1, so only an exactly zero or non-finite interpolated
-                // population could round differently.
-                if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[coarse.src], coarse.kind,
-                                             fine.f[fine.src], dShell, shellCount, geom(), 0.0f,
-                                             tf / (2.0f * tc), fillStream);
-                    e != cudaSuccess)
-                    return e;
-                cudaEventRecord(evFill0, fillStream);
-            }
             if (auto e = collide(coarse, p, rho, u, v, w); e != cudaSuccess) return e;
-            if (overlap) {
-                const float tc = p.tau, tf = fineTau(tc, 2);
-                cudaEventRecord(evFork1, stream);
-                cudaStreamWaitEvent(fillStream, evFork1, 0);
-                ++launches;
-                if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src], coarse.kind,
-                                             fine.f[1 - fine.src], dShell, shellCount, geom(), 0.5f,
-                                             tf / (2.0f * tc), fillStream);
-                    e != cudaSuccess)
-                    return e;
-                cudaEventRecord(evFill1, fillStream);
-            }
             if (fineActive) {
                 const int m = factor;
                 const float tc = p.tau, tf = fineTau(tc, m);
@@ -776,17 +711,13 @@ struct fcfd_solver {
                 // -- unless a finer level rewrites the fine state after it.
                 const bool fuse = fuseOn() && m == 2 && !finerActive;
                 for (int k = 0; k < m; ++k) {
-                    if (overlap) {
-                        cudaStreamWaitEvent(stream, k == 0 ? evFill0 : evFill1, 0);
-                    } else {
-                        ++launches;
-                        if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src],
-                                                     coarse.kind, fine.f[fine.src], dShell, shellCount, geom(),
-                                                     static_cast<float>(k) / static_cast<float>(m),
-                                                     tf / (static_cast<float>(m) * tc), stream);
-                            e != cudaSuccess)
-                            return e;
-                    }
+                    ++launches;
+                    if (auto e = launch_fill_c2f(storage, coarse.f[coarse.src], coarse.f[1 - coarse.src],
+                                                 coarse.kind, fine.f[fine.src], dShell, shellCount, geom(),
+                                                 static_cast<float>(k) / static_cast<float>(m),
+                                                 tf / (static_cast<float>(m) * tc), stream);
+                        e != cudaSuccess)
+                        return e;
                     const cudaError_t ce = (fuse && k == m - 1) ? collideChild(fine, fp, geom(), dScratch)
                                                                 : collide(fine, fp, nullptr, nullptr, nullptr, nullptr);
                     if (ce != cudaSuccess) return ce;
@@ -1053,7 +984,7 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
         s->storage = opts->storage == FCFD_STORE_FP16 ? Storage::F16 : Storage::F32;
         if (opts->les_cs != 0.0f) s->lesCs = opts->les_cs;
         if (opts->magic_lambda > 0.0f) s->lambda = opts->magic_lambda;
-        s->collideKernel = (opts->collide_kernel >= 0 && opts->collide_kernel <= 2) ? opts->collide_kernel : 0;
+        s->collideKernel = (opts->collide_kernel >= 0 && opts->collide_kernel <= 3) ? opts->collide_kernel : 0;
     }
     auto fail = [&](const char* what, cudaError_t e) {
         set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));
@@ -1777,13 +1708,6 @@ int fcfd_wall_update_timed(fcfd_solver* s, int level, int reps, float* ms, fcfd_
         stats->fallbacks = st.fallbackCells;
         stats->newton_iterations = static_cast<long long>(st.newtonIters);
     }
-    return 0;
-}
-
-int fcfd_set_overlap_fills(fcfd_solver* s, int enabled) {
-    if (!s) return cudaErrorInvalidValue;
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    s->overlapFills = enabled != 0;
     return 0;
 }
 

@@ -79,9 +79,12 @@ typedef struct fcfd_options {
     float les_cs;       /* Smagorinsky constant                          */
     float magic_lambda; /* TRT magic parameter                           */
     int use_graphs;     /* 1: replay steady-state batches as CUDA graphs */
-    int collide_kernel; /* 0 automatic (= 1), 1 one cell per thread,
-                           2 staged rows (bulk async copies into shared
-                           memory; slower on GB300, kept selectable) */
+    int collide_kernel; /* 0 automatic: 3 with FP16 storage and an even
+                           nx, else 1; 1 one cell per thread; 2 staged rows
+                           (bulk async copies into shared memory; slower
+                           on GB300, kept selectable); 3 an x-pair of cells
+                           per thread on packed FP32 lanes (FP16 storage,
+                           even nx; otherwise 1) */
 } fcfd_options;
 
 /* Refinement patch in coarse cells, [x0,x1) x [y0,y1) x [0,nz)
@@ -327,12 +330,6 @@ int fcfd_refinement_info(const fcfd_solver* s, fcfd_refine_info* out);
 /* FP32 SoA import/export of the fine level's current buffer. */
 int fcfd_import_fine_f32(fcfd_solver* s, const float* host_f, size_t count);
 int fcfd_export_fine_f32(fcfd_solver* s, float* host_f, size_t count);
-/* Interface fills of a factor-2 patch (no finer level) on a side stream of
- * the solver, overlapped with the coarse collide and the first fine collide
- * (default 1); 0 runs them in line on the solver stream. Same results either
- * way. No reference counterpart (the reference launches everything on one
- * stream, lbm_solver.cpp:1172-1291). */
-int fcfd_set_overlap_fills(fcfd_solver* s, int enabled);
 /* Factor-2 patches: form the restriction's child averages inside the last
  * fine sub-step's collide (1) instead of re-reading the fine level in a
  * separate pass (0; lbm_refine.cu:274-429 reads it in the restriction).
