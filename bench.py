@@ -1031,7 +1031,7 @@ def main():
                     help="run only the watchdog-trip comparison with the reference's own step")
     ap.add_argument("--no-stability", action="store_true", help="skip the watchdog-trip comparison")
     ap.add_argument("--polar-config", default="", help="block,rows,ctas_per_sm,group_mb: skip the autotuner")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged", "pair"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
     args = ap.parse_args()
     global COLLIDE_KERNEL

@@ -202,12 +202,11 @@ __device__ __forceinline__ void collide_exact(float (&f)[kQ], float tau0, float 
     rhoO = rho; uxO = ux; uyO = uy; uzO = uz;
 }
 
-// ---- lane arithmetic of the deviation body ------------------------------------
-// Every operation is an explicit round-to-nearest intrinsic, so the compiler
-// contracts nothing on its own: the body on one cell (float lanes) and on an
-// x-pair of cells (float2 lanes on the packed FADD2 / FMUL2 / FFMA2 path,
-// which rounds each lane exactly like the scalar instruction) give the same
-// bits for a cell.
+// ---- arithmetic of the deviation body -----------------------------------------
+// Every operation is an explicit round-to-nearest intrinsic (the fused
+// multiply-adds written out where the body wants them), so the compiler
+// contracts nothing on its own and the body rounds the same in every
+// translation unit and kernel that includes it.
 template <class V> struct Lane;
 template <> struct Lane<float> {
     __device__ __forceinline__ static float s(float v) { return v; }
@@ -219,16 +218,6 @@ template <> struct Lane<float> {
     __device__ __forceinline__ static float rcp(float a) { return rcp_approx(a); }
     __device__ __forceinline__ static float sqrt(float a) { return sqrt_approx(a); }
 };
-template <> struct Lane<float2> {
-    __device__ __forceinline__ static float2 s(float v) { return make_float2(v, v); }
-    __device__ __forceinline__ static float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-    __device__ __forceinline__ static float2 sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-    __device__ __forceinline__ static float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-    __device__ __forceinline__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-    __device__ __forceinline__ static float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
-    __device__ __forceinline__ static float2 rcp(float2 a) { return make_float2(rcp_approx(a.x), rcp_approx(a.y)); }
-    __device__ __forceinline__ static float2 sqrt(float2 a) { return make_float2(sqrt_approx(a.x), sqrt_approx(a.y)); }
-};
 
 /// Density floor of one lane: rho = max-floored 1 + dr, rm1 = rho - 1.
 __device__ __forceinline__ void rho_floor(float dr, float& rho, float& rm1) {
@@ -237,10 +226,6 @@ __device__ __forceinline__ void rho_floor(float dr, float& rho, float& rm1) {
     rho = floored ? kRhoFloor : r;
     rm1 = floored ? kRhoFloor - 1.0f : dr;
 }
-__device__ __forceinline__ void rho_floor(float2 dr, float2& rho, float2& rm1) {
-    rho_floor(dr.x, rho.x, rm1.x);
-    rho_floor(dr.y, rho.y, rm1.y);
-}
 
 /// The |u| <= 0.3 limiter of one lane (u2 recomputed when it acts).
 __device__ __forceinline__ void limit_u(float& ux, float& uy, float& uz, float& u2) {
@@ -248,12 +233,6 @@ __device__ __forceinline__ void limit_u(float& ux, float& uy, float& uz, float& 
         const float sc = __fmul_rn(kMaxSimSpeed, rsqrtf(u2));
         ux = __fmul_rn(ux, sc); uy = __fmul_rn(uy, sc); uz = __fmul_rn(uz, sc);
         u2 = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux)));
-    }
-}
-__device__ __forceinline__ void limit_u(float2& ux, float2& uy, float2& uz, float2& u2) {
-    if (u2.x > kMaxSimSpeed * kMaxSimSpeed || u2.y > kMaxSimSpeed * kMaxSimSpeed) {
-        limit_u(ux.x, uy.x, uz.x, u2.x);
-        limit_u(ux.y, uy.y, uz.y, u2.y);
     }
 }
 
@@ -269,8 +248,7 @@ __device__ __forceinline__ V dot_lane(int a, V ux, V uy, V uz) {
     return d;
 }
 
-/// TRT + Smagorinsky collision on the deviations g_q = f_q - w_q of one cell
-/// (V = float) or of an x-pair of cells (V = float2).
+/// TRT + Smagorinsky collision on the deviations g_q = f_q - w_q of one cell.
 template <class V>
 __device__ __forceinline__ void collide_dev_lanes(V (&g)[kQ], float tau0, float lambda, float smagPre, V& rhoO,
                                                   V& uxO, V& uyO, V& uzO) {
@@ -590,69 +568,6 @@ collide_flat_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
     const unsigned z = fdiv(row, divY);
     collide_one<S, WM, EXACT, QL>(src, dst, kind, a, static_cast<int>(cell - row * divX.d),
                                   static_cast<int>(row - z * divY.d), static_cast<int>(z), &off);
-}
-
-// ---- FP16 storage: an x-pair of cells per thread ---------------------------------
-// Thread t updates cells 2t and 2t + 1 of the flattened lattice (nx even, so
-// a pair never straddles a row). When both are bulk fluid cells away from
-// every periodic face, the pair is one unit: the 9 pulls with c_x = 0 are
-// one aligned 4-byte half2 load each (both cells' sources sit side by side),
-// the 10 others two 2-byte loads, the collision runs on float2 lanes (packed
-// FADD2 / FMUL2 / FFMA2: half the arithmetic instructions per cell), and
-// each direction is stored as one half2. Any other pair takes the one-cell
-// path for both cells. The float2 body rounds each lane like the one-cell
-// body, so every cell gets the same bits either way.
-constexpr int kPairX = 128;
-/// Resident 128-thread blocks per SM the pair kernel is compiled for.
-constexpr int kPairMinBlocks = 4;
-
-__device__ __forceinline__ float2 ld_pf2(const __half* p) {
-    unsigned v;
-    asm("ld.global.nc.L2::256B.b32 %0, [%1];" : "=r"(v) : "l"(p));
-    __half2 h;
-    *reinterpret_cast<unsigned*>(&h) = v;
-    return __half22float2(h);
-}
-
-template <bool WM, bool QL>
-__global__ void __launch_bounds__(kPairX, kPairMinBlocks)
-collide_pair_f16_kernel(const __half* __restrict__ src, __half* __restrict__ dst,
-                        const std::uint8_t* __restrict__ kind, CollideArgs a,
-                        const __grid_constant__ PullOffsets off, FastDiv divX, FastDiv divY) {
-    const unsigned cell = 2u * (blockIdx.x * kPairX + threadIdx.x);
-    if (cell >= static_cast<unsigned long long>(a.n)) return;
-    const unsigned row = fdiv(cell, divX);
-    const unsigned z = fdiv(row, divY);
-    const int x = static_cast<int>(cell - row * divX.d), y = static_cast<int>(row - z * divY.d);
-    // Both kind bytes: flag 0 (fluid) and no near-wall bit in either.
-    const unsigned kk = *reinterpret_cast<const unsigned short*>(kind + cell);
-    const bool bulk = (kk & 0x8F8Fu) == 0 && x >= 2 && x <= a.nx - 4 && y >= 1 && y <= a.ny - 2
-                      && static_cast<int>(z) >= 1 && static_cast<int>(z) <= a.nz - 2;
-    if (!bulk) {
-        collide_one<StoreF16, WM, false, QL>(src, dst, kind, a, x, y, static_cast<int>(z), &off);
-        collide_one<StoreF16, WM, false, QL>(src, dst, kind, a, x + 1, y, static_cast<int>(z), &off);
-        return;
-    }
-    float2 g[kQ];
-    const __half* base = src + cell;
-#pragma unroll
-    for (int q = 0; q < kQ; ++q) {
-        const __half* p = byte_add(base, off.pull[q]);
-        if (cx(q) == 0) g[q] = ld_pf2(p);
-        else g[q] = make_float2(ld_pf(p), ld_pf(p + 1));
-    }
-    float2 r, ux, uy, uz;
-    collide_dev_lanes<float2>(g, a.tau0, a.lambda, a.smagPre, r, ux, uy, uz);
-    __half* ob = dst + cell;
-#pragma unroll
-    for (int q = 0; q < kQ; ++q)
-        *reinterpret_cast<__half2*>(byte_add(ob, off.slice[q])) = __floats2half2_rn(g[q].x, g[q].y);
-    if (a.writeMacro) {
-        *reinterpret_cast<float2*>(a.rho + cell) = r;
-        *reinterpret_cast<float2*>(a.u + cell) = ux;
-        *reinterpret_cast<float2*>(a.v + cell) = uy;
-        *reinterpret_cast<float2*>(a.w + cell) = uz;
-    }
 }
 
 // ---- warm-restart flag edits (applyFlagEditsKernel, lbm_core.cu:644-717) -----
@@ -1158,20 +1073,6 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
         if (grid > rows) grid = rows;
         kern<<<static_cast<unsigned>(grid), kStagedThreads, plan.smem, st>>>(src, dst, kind, a, plan.stages);
         return cudaGetLastError();
-    }
-    if constexpr (!EXACT && std::is_same_v<S, StoreF16>) {
-        // FP16 storage: the pair kernel unless the one-cell kernel is asked
-        // for (nx even, so pairs never straddle rows).
-        if ((p.kernel == 0 || p.kernel == 3) && d.nx % 2 == 0 && d.nx >= 4 && d.ny >= 2) {
-            const FastDiv fx = fast_div(static_cast<unsigned>(d.nx)), fy = fast_div(static_cast<unsigned>(d.ny));
-            const PullOffsets po = pull_offsets<T>(d.nx, d.ny, a.n);
-            const unsigned blocks = static_cast<unsigned>((a.n / 2 + kPairX - 1) / kPairX);
-            const bool ql = a.qFrac != nullptr;
-            auto kern = wm ? (ql ? collide_pair_f16_kernel<true, true> : collide_pair_f16_kernel<true, false>)
-                           : (ql ? collide_pair_f16_kernel<false, true> : collide_pair_f16_kernel<false, false>);
-            kern<<<blocks, kPairX, 0, st>>>(src, dst, kind, a, po, fx, fy);
-            return cudaGetLastError();
-        }
     }
     const int bx = d.nx >= kCellBlockX ? kCellBlockX : ((d.nx + 31) / 32) * 32;
     const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),

@@ -984,7 +984,7 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
         s->storage = opts->storage == FCFD_STORE_FP16 ? Storage::F16 : Storage::F32;
         if (opts->les_cs != 0.0f) s->lesCs = opts->les_cs;
         if (opts->magic_lambda > 0.0f) s->lambda = opts->magic_lambda;
-        s->collideKernel = (opts->collide_kernel >= 0 && opts->collide_kernel <= 3) ? opts->collide_kernel : 0;
+        s->collideKernel = (opts->collide_kernel >= 0 && opts->collide_kernel <= 2) ? opts->collide_kernel : 0;
     }
     auto fail = [&](const char* what, cudaError_t e) {
         set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));

@@ -79,12 +79,9 @@ typedef struct fcfd_options {
     float les_cs;       /* Smagorinsky constant                          */
     float magic_lambda; /* TRT magic parameter                           */
     int use_graphs;     /* 1: replay steady-state batches as CUDA graphs */
-    int collide_kernel; /* 0 automatic: 3 with FP16 storage and an even
-                           nx, else 1; 1 one cell per thread; 2 staged rows
-                           (bulk async copies into shared memory; slower
-                           on GB300, kept selectable); 3 an x-pair of cells
-                           per thread on packed FP32 lanes (FP16 storage,
-                           even nx; otherwise 1) */
+    int collide_kernel; /* 0 automatic (= 1), 1 one cell per thread,
+                           2 staged rows (bulk async copies into shared
+                           memory; slower on GB300, kept selectable) */
 } fcfd_options;
 
 /* Refinement patch in coarse cells, [x0,x1) x [y0,y1) x [0,nz)

@@ -470,35 +470,6 @@ def test_fused_child_average_equals_separate_pass(fc, storage):
         assert np.abs(out[True][1] - out[False][1]).max() <= 2e-4
 
 
-@pytest.mark.parametrize("patch", [False, True])
-def test_fp16_pair_kernel_equals_one_cell_kernel(fc, patch):
-    """FP16 storage: the x-pair kernel (packed float2 lanes, half2 loads and
-    stores for bulk pairs, the one-cell path for every other pair) gives the
-    same populations and macroscopic fields, bit for bit, as the one-cell
-    kernel: airfoil tunnel with the wall model (and the 2:1 patch), 40 steps
-    in batches of 20 (macroscopic fields written on each batch's last step)."""
-    from foil_cfd_gb300.tunnels import airfoil_tunnel
-    t = airfoil_tunnel(160, 64, 16, chord=64, aoa=6.0, patch=patch)
-    out = {}
-    for kernel in ("pair", "cell"):
-        s = fc.LBMSolver()
-        s.init(t.dims, fc.scaling_direct(0.52, t.u_lat, t.chord_cells), t.flags, storage="fp16", les_cs=0.1,
-               kernel=kernel)
-        s.set_wall_model_enabled(True)
-        s.set_startup_ramp_enabled(False)
-        s.reset()
-        if patch:
-            s.init_refinement(t.box, t.factor, t.fine_flags)
-        assert s.step_n(20) == 0 and s.step_n(20) == 0
-        assert not s.nan_detected()
-        out[kernel] = (s.export_f32(), s.export_fine_f32() if patch else None, s.download_macro())
-    assert np.array_equal(out["pair"][0], out["cell"][0])
-    if patch:
-        assert np.array_equal(out["pair"][1], out["cell"][1])
-    for a, b in zip(out["pair"][2], out["cell"][2]):
-        assert np.array_equal(a, b)
-
-
 @pytest.mark.parametrize("kernel", ["cell", "staged"])
 @pytest.mark.parametrize("case,steps,slip", [("f1", 1, False), ("f20", 20, False), ("f20w", 20, True)])
 def test_qlibb_collide_vs_reference_golden(fc, golden, case, steps, slip, kernel):
