@@ -32,6 +32,12 @@ class Options(C.Structure):
                 ("use_graphs", C.c_int), ("collide_kernel", C.c_int)]
 
 
+class Lattice(C.Structure):
+    """fcfd_lattice (foilcfd_step.h): a level's current source buffer."""
+    _fields_ = [("f", C.c_void_p), ("flags", C.c_void_p), ("dims", Dims), ("cells", C.c_longlong),
+                ("storage", C.c_int), ("uwx", C.c_void_p), ("uwy", C.c_void_p), ("uwz", C.c_void_p)]
+
+
 class PatchBox(C.Structure):
     _fields_ = [("x0", C.c_int), ("y0", C.c_int), ("x1", C.c_int), ("y1", C.c_int)]
 
@@ -114,6 +120,8 @@ _SIGS = {
     "fcfd_set_startup_ramp": (None, [P, C.c_int]),
     "fcfd_set_force_ema_window": (None, [P, C.c_float]),
     "fcfd_mirror_buffers": (C.c_int, [P]),
+    "fcfd_device_flags": (C.c_int, [P, C.c_int, C.POINTER(C.c_void_p)]),
+    "fcfd_lattice_view": (C.c_int, [P, C.c_int, C.POINTER(Lattice)]),
     "fcfd_step_n": (C.c_int, [P, C.c_int]),
     "fcfd_synchronize": (C.c_int, [P]),
     "fcfd_step_count": (C.c_longlong, [P]),

@@ -1113,7 +1113,9 @@ int fcfd_forces(fcfd_solver* s, fcfd_force_readout* r) {
     if (!s || !r) return cudaErrorInvalidValue;
     *r = fcfd_force_readout{};
     if (!s->initialized) return cudaErrorNotReady;
-    cudaStreamSynchronize(s->stream);
+    // As the reference's forces() (lbm_solver.cpp:1414-1509): read what the
+    // asynchronous read-backs have delivered so far. Folding completed
+    // samples only queries events, so the call never waits on the stream.
     s->pollAsync();
     r->flow_throughs = fcfd_flow_throughs(s);
     const bool fineForces = s->fineActive && s->forcesFromFine;
@@ -1151,6 +1153,41 @@ int fcfd_forces(fcfd_solver* s, fcfd_force_readout* r) {
             stats(ld, r->ld_avg, r->ld_min, r->ld_max, r->ld_median);
         }
     }
+    return 0;
+}
+
+/// Level 0 coarse, 1 fine, 2 finer; null when that level is not active.
+static const Level* active_level(const fcfd_solver* s, int level) {
+    if (level == 0) return &s->coarse;
+    if (level == 1 && s->fineActive) return &s->fine;
+    if (level == 2 && s->finerActive) return &s->finer;
+    return nullptr;
+}
+
+int fcfd_device_flags(fcfd_solver* s, int level, const uint8_t** flags) {
+    if (!s || !flags) return cudaErrorInvalidValue;
+    *flags = nullptr;
+    if (!s->initialized) return cudaErrorNotReady;
+    const Level* L = active_level(s, level);
+    if (!L) return cudaErrorInvalidValue;
+    *flags = L->flags;
+    return 0;
+}
+
+int fcfd_lattice_view(fcfd_solver* s, int level, fcfd_lattice* out) {
+    if (!s || !out) return cudaErrorInvalidValue;
+    *out = fcfd_lattice{};
+    if (!s->initialized) return cudaErrorNotReady;
+    const Level* L = active_level(s, level);
+    if (!L) return cudaErrorInvalidValue;
+    out->f = L->f[L->src];
+    out->flags = L->flags;
+    out->dims = fcfd_dims{L->d.nx, L->d.ny, L->d.nz};
+    out->cells = L->n;
+    out->storage = s->storage == Storage::F32 ? FCFD_STORE_FP32 : FCFD_STORE_FP16;
+    out->uwx = L->wm.active ? L->wm.dUwx : nullptr;
+    out->uwy = L->wm.active ? L->wm.dUwy : nullptr;
+    out->uwz = L->wm.active ? L->wm.dUwz : nullptr;
     return 0;
 }
 

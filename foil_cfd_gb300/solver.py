@@ -181,6 +181,22 @@ class LBMSolver:
         self._lib.fcfd_forces(self._h, C.byref(r))
         return r
 
+    def lattice_view(self, level: int = 0) -> capi.Lattice:
+        """latticeView(): the level's current source buffer and its layout."""
+        v = capi.Lattice()
+        rc = self._lib.fcfd_lattice_view(self._h, level, C.byref(v))
+        if rc:
+            raise SolverError(f"lattice view failed ({rc})")
+        return v
+
+    def device_flags(self, level: int = 0) -> int:
+        """deviceFlags(): device address of the level's CellFlag bytes."""
+        p = C.c_void_p()
+        rc = self._lib.fcfd_device_flags(self._h, level, C.byref(p))
+        if rc:
+            raise SolverError(f"device flags failed ({rc})")
+        return p.value
+
     def force_raw(self) -> np.ndarray:
         out = np.zeros(3, np.float64)
         rc = self._lib.fcfd_force_raw(self._h, ptr(out))

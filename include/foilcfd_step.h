@@ -90,7 +90,10 @@ typedef struct fcfd_patch_box {
     int x0, y0, x1, y1;
 } fcfd_patch_box;
 
-/* ForceReadout (lbm_solver.h:28-50), coefficients from the EMA force. */
+/* ForceReadout (lbm_solver.h:28-50), coefficients from the EMA force.
+ * fcfd_forces reads the force samples whose asynchronous read-back has
+ * completed (as the reference's const forces() reads the state its last
+ * poll folded): it never waits on the stream. */
 typedef struct fcfd_force_readout {
     float cl, cd, lift_to_drag;
     int valid;
@@ -229,6 +232,26 @@ int fcfd_macro(fcfd_solver* s, const float** rho, const float** u,
 /* Synchronous copy of the four macroscopic arrays to host memory. */
 int fcfd_download_macro(fcfd_solver* s, float* rho, float* u, float* v,
                         float* w);
+/* deviceFlags() (lbm_solver.h:431-437): device CellFlag bytes of a level
+ * (0 coarse, 1 fine, 2 finer), cellCount bytes, unpadded x + nx*(y + ny*z)
+ * -- here the same layout the kernels index, since nothing is padded. */
+int fcfd_device_flags(fcfd_solver* s, int level, const uint8_t** flags);
+/* latticeView() (lbm_solver.h:439-444): the current source buffer of a
+ * level with everything an external kernel needs to read it -- the
+ * population base (unpadded SoA f[q*cells + cell] in the storage precision:
+ * float for FCFD_STORE_FP32, half(f - w_q) for FCFD_STORE_FP16), the flag
+ * bytes, the grid and, with the wall model on, the level's half-bit slip
+ * field (else NULL). Valid until the next step, flag change or refinement
+ * change. fcfd_force_links_noalloc takes an FP32 view's f and slip arrays. */
+typedef struct fcfd_lattice {
+    void* f;
+    const uint8_t* flags;
+    fcfd_dims dims;
+    long long cells;
+    int storage;
+    const uint16_t *uwx, *uwy, *uwz;
+} fcfd_lattice;
+int fcfd_lattice_view(fcfd_solver* s, int level, fcfd_lattice* out);
 /* Device pointer of the current population buffer and its size
  * (activeDeviceF / fBufferBytes, lbm_solver.h:446-458). The layout is
  * unpadded SoA f[q*ncells + cell] in the solver's storage precision. */
