@@ -132,6 +132,10 @@ def build(force: bool = False) -> dict:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference snapshot build failed:\n{r.stderr[-4000:]}")
+    # The reference's own solver tests, staged for relinking against this
+    # library through the LBMSolver shim (oracle/relink.py).
+    from oracle import relink
+    libs["relink"] = relink.stage(REFERENCE)
     return libs
 
 
