@@ -375,11 +375,41 @@ def wall_seed_leg(sol, t, epochs=150, n_harvest=2_000_000, n_synth=1_000_000, ba
     return out
 
 
-def polar_leg(steps=10000, seq_steps=2000, trial_steps=10, fixed=None):
-    """Batched polar: 24 NACA 4-digit tunnels of uneven size in one launch per
-    step (FP16 storage, graph-replayed chunks, autotuned shape) from a uniform
-    start; against 24 sequential single-tunnel FP32 runs (the drop-in)."""
+def _sequential_runs(tunnels, storage, steps):
+    """Each tunnel on its own single-tunnel solver, one after the other, for
+    `steps` steps in stepN batches (the drop-in run of a polar). A run whose
+    watchdog latches stops there (stepN does nothing while latched); the
+    work counted is the steps each run took."""
     import foil_cfd_gb300 as fc
+    wall, upd, latched = 0.0, 0.0, 0
+    for t in tunnels:
+        s = fc.LBMSolver()
+        s.init(t.dims, fc.scaling_direct(t.tau, t.u_lat, t.chord), t.flags, storage=storage, les_cs=0.1)
+        s.set_startup_ramp_enabled(False)
+        s.reset()
+        s.synchronize()
+        t0 = time.perf_counter()
+        left = steps
+        while left > 0:
+            k = min(BATCH, left)
+            assert s.step_n(k) == 0
+            left -= k
+        s.synchronize()
+        wall += time.perf_counter() - t0
+        upd += float(t.cells) * s.step_count()
+        latched += int(s.nan_detected())
+        del s
+    return {"glups": round(upd / wall / 1e9, 3), "wall_s": round(wall, 3), "steps": steps,
+            "watchdog_latched_runs": latched}
+
+
+def polar_leg(steps=10000, fp32_steps=2000, trial_steps=10, fixed=None):
+    """Batched polar: 24 NACA 4-digit tunnels of uneven size in one launch per
+    step (graph-replayed chunks, autotuned shape, a full-field watchdog per
+    tunnel after every force sample) from a uniform start, against the same
+    24 tunnels run one after the other on single-tunnel solvers of the same
+    storage for the same steps. FP16 storage is the polar's configuration
+    (full steps); FP32 is timed on fewer steps beside it."""
     import torch
     from foil_cfd_gb300 import batch
     t0 = time.perf_counter()
@@ -393,14 +423,15 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10, fixed=None):
     dev_build_s = time.perf_counter() - t0
     same = all(np.array_equal(d.flags.cpu().numpy(), h.flags) for d, h in zip(dev_tunnels, tunnels))
     del dev_tunnels
-    upd = float(sum(t.cells for t in tunnels))
-    out = {"tunnels": len(tunnels), "cells": int(upd), "steps": steps,
+    cells = np.array([float(t.cells) for t in tunnels])
+    out = {"tunnels": len(tunnels), "cells": int(cells.sum()), "steps": steps,
            "sections": "NACA 0012/2412/4412, -4..16 deg by 2.5 (first 24), chord 96-192 cells, 2.5 x 1.5 chords, "
                        "span 16 periodic, Re 1000 on the chord, uniform-flow start",
            "geometry_build_ms": {"host": round(host_build_s * 1e3, 1), "device": round(dev_build_s * 1e3, 1),
-                                 "identical": same}}
+                                 "identical": same},
+           "counting": "lattice updates each tunnel actually took (a latched tunnel stops at its latch)"}
     res = {}
-    for storage in ("fp16", "fp32"):
+    for storage, n in (("fp16", steps), ("fp32", fp32_steps)):
         b = batch.BatchSolver()
         b.init(tunnels, storage=storage, les_cs=0.1, force_every=100)
         if fixed is None:
@@ -409,52 +440,34 @@ def polar_leg(steps=10000, seq_steps=2000, trial_steps=10, fixed=None):
             b.set_config(*fixed)
             chosen, table = tuple(fixed), []
         b.reset()
-        n = steps if storage == "fp16" else min(steps, seq_steps)
         b.synchronize()
         l0 = b.kernel_launches()
         t0 = time.perf_counter()
         assert b.step_n(n, use_graphs=True) == 0
         b.synchronize()
         wall = time.perf_counter() - t0
-        res[storage] = {"glups": round(upd * n / wall / 1e9, 3), "wall_s": round(wall, 3), "steps": n,
+        verdicts, ran = b.latched(with_steps=True)
+        upd = float((cells * ran).sum())
+        res[storage] = {"glups": round(upd / wall / 1e9, 3), "wall_s": round(wall, 3), "steps": n,
                         "device_ms_per_step": round(b.last_ms() / n, 4), "autotuned_shape": list(chosen),
                         "shapes_timed": len(table), "launches_per_step": round((b.kernel_launches() - l0) / n, 3),
-                        "tuning_ms_per_step": {"/".join(map(str, c)): round(m, 4) for c, m in table}}
-        speed, bad = b.health()
-        res[storage]["diverged_tunnels"] = int(((speed >= 0.285) | (bad > 0)).sum())
+                        "tuning_ms_per_step": {"/".join(map(str, c)): round(m, 4) for c, m in table},
+                        "latched_tunnels": int((verdicts != 0).sum())}
         if storage == "fp16":
             cl, cd = b.coefficients(0.5)
-            out["polar"] = [{"section": t.digits, "aoa": t.aoa, "chord": t.chord, "cl": round(float(a), 4),
-                             "cd": round(float(c), 5), "max_speed": round(float(v), 4), "diverged": bool(v >= 0.285 or k)}
-                            for t, a, c, v, k in zip(tunnels, cl, cd, speed, bad)]
+            speed, bad = b.health()
+            out["polar"] = [{"section": t.digits, "aoa": t.aoa, "chord": t.chord,
+                             "cl": None if v else round(float(a), 4), "cd": None if v else round(float(c), 5),
+                             "max_speed": round(float(sp), 4),
+                             "latched": {0: None, 1: "non-finite", 2: "speed at the limiter"}[int(v)],
+                             "latched_at_step": int(r) if v else None}
+                            for t, a, c, sp, v, r in zip(tunnels, cl, cd, speed, verdicts, ran)]
         b.close()
-    out["batched_fp16"] = res["fp16"]
-    out["batched_fp32"] = res["fp32"]
-    # 24 sequential plain FP32 runs (one solver per tunnel, its own launches).
-    seq = 0.0
-    latched = 0
-    for t in tunnels:
-        s = fc.LBMSolver()
-        s.init(t.dims, fc.scaling_direct(t.tau, t.u_lat, t.chord), t.flags, storage="fp32", les_cs=0.1)
-        s.set_startup_ramp_enabled(False)
-        s.reset()
-        s.synchronize()
-        t0 = time.perf_counter()
-        left = seq_steps
-        while left > 0:
-            k = min(BATCH, left)
-            assert s.step_n(k) == 0
-            left -= k
-        s.synchronize()
-        seq += time.perf_counter() - t0
-        latched += int(s.nan_detected())
-        del s
-    out["sequential_fp32"] = {"glups": round(upd * seq_steps / seq / 1e9, 3), "wall_s": round(seq, 3),
-                              "steps": seq_steps, "watchdog_latched_runs": latched,
-                              "wall_s_projected_full_polar": round(seq * steps / seq_steps, 2)}
-    out["polar_wall_s_batched_fp16"] = res["fp16"]["wall_s"] * steps / res["fp16"]["steps"]
-    out["speedup_batched_fp16_vs_sequential_fp32"] = round(out["sequential_fp32"]["wall_s_projected_full_polar"]
-                                                          / out["polar_wall_s_batched_fp16"], 2)
+        res[f"sequential_{storage}"] = _sequential_runs(tunnels, storage, n)
+    out["batched_fp16"], out["sequential_fp16"] = res["fp16"], res["sequential_fp16"]
+    out["batched_fp32"], out["sequential_fp32"] = res["fp32"], res["sequential_fp32"]
+    out["speedup_batched_vs_sequential_fp16"] = round(res["sequential_fp16"]["wall_s"] / res["fp16"]["wall_s"], 2)
+    out["speedup_batched_vs_sequential_fp32"] = round(res["sequential_fp32"]["wall_s"] / res["fp32"]["wall_s"], 2)
     return out
 
 

@@ -172,6 +172,15 @@ class BatchSolver:
         self._check(self._lib.fcfd_batch_health(self._h, capi.ptr(sp), capi.ptr(bad)), "health")
         return sp, bad
 
+    def latched(self, with_steps: bool = False):
+        """Watchdog verdict per tunnel: 0 running, 1 non-finite cell, 2 speed
+        at the limiter (the tunnel stopped stepping when it was latched);
+        with_steps also the steps each tunnel has taken since the reset."""
+        v = np.zeros(len(self.tunnels), np.int32)
+        st = np.zeros(len(self.tunnels), np.int64)
+        self._check(self._lib.fcfd_batch_latched(self._h, capi.ptr(v), capi.ptr(st)), "latch read-back")
+        return (v, st) if with_steps else v
+
     def export_f32(self, i: int) -> np.ndarray:
         f = np.empty(Q * int(np.prod(self.tunnels[i].dims)), np.float32)
         self._check(self._lib.fcfd_batch_export_f32(self._h, i, capi.ptr(f), f.size), "export")

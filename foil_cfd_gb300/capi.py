@@ -258,6 +258,7 @@ _SIGS = {
     "fcfd_batch_force_history": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_int)]),
     "fcfd_batch_forces_now": (C.c_int, [P, P]),
     "fcfd_batch_health": (C.c_int, [P, P, P]),
+    "fcfd_batch_latched": (C.c_int, [P, P, P]),
     "fcfd_batch_export_f32": (C.c_int, [P, C.c_int, P, C.c_size_t]),
     "fcfd_batch_import_f32": (C.c_int, [P, C.c_int, P, C.c_size_t]),
     "fcfd_batch_last_ms": (C.c_int, [P, C.POINTER(C.c_double)]),

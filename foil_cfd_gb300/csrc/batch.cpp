@@ -67,6 +67,8 @@ struct fcfd_batch {
     int sms = 0;
 
     double* dPartials = nullptr;
+    int* dLatch = nullptr;    // per-tunnel watchdog verdict (0 running), then the sample count at the latch
+    int* dHealth = nullptr;   // per-tunnel max speed bits, then non-finite counts
     double* dForceCur = nullptr;
     double* dHist = nullptr;
     int* dHistCount = nullptr;
@@ -92,7 +94,8 @@ struct fcfd_batch {
         }
         t.clear();
         cudaFree(dPartials); cudaFree(dForceCur); cudaFree(dHist); cudaFree(dHistCount);
-        dPartials = dForceCur = dHist = nullptr; dHistCount = nullptr;
+        cudaFree(dLatch); cudaFree(dHealth);
+        dPartials = dForceCur = dHist = nullptr; dHistCount = dLatch = dHealth = nullptr;
         if (ev0) { cudaEventDestroy(ev0); ev0 = nullptr; }
         if (ev1) { cudaEventDestroy(ev1); ev1 = nullptr; }
         if (ownStream && stream) cudaStreamDestroy(stream);
@@ -124,6 +127,7 @@ struct fcfd_batch {
         table.ntun = ntun();
         table.lambda = lambda;
         table.smagPre = smagPre();
+        table.latch = dLatch;
         groups.clear();
         const size_t limit = static_cast<size_t>(std::max(cfg.group_mb, 0)) << 20;
         size_t groupBytes = 0;
@@ -181,10 +185,35 @@ struct fcfd_batch {
         return cudaSuccess;
     }
 
+    /// Watchdog of every tunnel: a full-field scan (max |u|, non-finite
+    /// cells), then the latch of each tunnel at the limiter speed of the
+    /// single-tunnel watchdog (0.95 x 0.3, lbm_core.cu:526-559) or with a
+    /// non-finite cell. Unlike the single-tunnel watchdog's 1-in-4093 sample,
+    /// every cell is looked at.
+    cudaError_t watchdog() {
+        const int nt = ntun();
+        if (auto e = cudaMemsetAsync(dHealth, 0, 2 * nt * sizeof(int), stream); e != cudaSuccess) return e;
+        for (int i = 0; i < nt; ++i) {
+            const Tunnel& x = t[i];
+            ++launches;
+            if (auto e = launch_batch_health(storage == Storage::F32, x.f[parity], x.kind, x.n, dHealth + i,
+                                             dHealth + nt + i, stream);
+                e != cudaSuccess)
+                return e;
+        }
+        ++launches;
+        return launch_batch_latch(dHealth, dHealth + nt, nt, 0.95f * 0.3f, dHistCount, dLatch, stream);   // 0.95 x the limiter speed
+    }
+
+    /// Per chunk: every tunnel's force appended to the history, then the
+    /// watchdog.
     cudaError_t forceSample() {
         if (auto e = forcesNow(); e != cudaSuccess) return e;
         ++launches;
-        return launch_force_append(dForceCur, 3 * ntun(), dHist, kHistCapacity, dHistCount, stream);
+        if (auto e = launch_force_append(dForceCur, 3 * ntun(), dHist, kHistCapacity, dHistCount, stream);
+            e != cudaSuccess)
+            return e;
+        return watchdog();
     }
 
     /// One step launched directly (+ the force sample on the cadence).
@@ -266,6 +295,7 @@ struct fcfd_batch {
                     return e;
             }
         if (auto e = cudaMemsetAsync(dHistCount, 0, sizeof(int), stream); e != cudaSuccess) return e;
+        if (auto e = cudaMemsetAsync(dLatch, 0, 2 * ntun() * sizeof(int), stream); e != cudaSuccess) return e;
         return cudaStreamSynchronize(stream);
     }
 };
@@ -350,6 +380,8 @@ int fcfd_batch_init(fcfd_batch* b, const fcfd_batch_tunnel* tunnels, int count, 
     if (e == cudaSuccess) e = cudaMalloc(&b->dForceCur, 3 * count * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&b->dHist, static_cast<size_t>(kHistCapacity) * 3 * count * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&b->dHistCount, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dLatch, 2 * count * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dHealth, 2 * count * sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     if (e == cudaSuccess) e = b->uploadTable();
@@ -518,6 +550,20 @@ int fcfd_batch_health(fcfd_batch* b, float* maxSpeed, int* nonFinite) {
     for (int i = 0; i < nt; ++i) {
         std::memcpy(&maxSpeed[i], &h[i], sizeof(float));
         nonFinite[i] = h[nt + i];
+    }
+    return 0;
+}
+
+int fcfd_batch_latched(fcfd_batch* b, int* verdicts, long long* steps_run) {
+    if (!b || !b->initialized || !verdicts) return cudaErrorInvalidValue;
+    if (auto e = cudaStreamSynchronize(b->stream); e != cudaSuccess) return e;
+    const int nt = b->ntun();
+    std::vector<int> h(2 * static_cast<size_t>(nt));
+    if (auto e = cudaMemcpy(h.data(), b->dLatch, h.size() * sizeof(int), cudaMemcpyDeviceToHost); e != cudaSuccess)
+        return e;
+    for (int i = 0; i < nt; ++i) {
+        verdicts[i] = h[i];
+        if (steps_run) steps_run[i] = h[i] ? static_cast<long long>(h[nt + i]) * b->forceEvery : b->steps;
     }
     return 0;
 }

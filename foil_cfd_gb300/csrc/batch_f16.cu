@@ -66,6 +66,26 @@ cudaError_t launch_batch_health(bool fp32, const void* f, const std::uint8_t* ki
     return cudaGetLastError();
 }
 
+/// Latch every running tunnel whose health scan found a non-finite cell
+/// (verdict 1) or a speed at the limiter (verdict 2, |u| >= cap); latch[ntun
+/// + t] records the force-sample count at that moment.
+__global__ void batch_latch_kernel(const int* __restrict__ maxSpeedBits, const int* __restrict__ nonFinite, int ntun,
+                                   float cap, const int* __restrict__ samples, int* __restrict__ latch) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntun || latch[t] != 0) return;
+    const int v = nonFinite[t] > 0 ? 1 : (__int_as_float(maxSpeedBits[t]) >= cap ? 2 : 0);
+    if (v) {
+        latch[t] = v;
+        latch[ntun + t] = *samples;
+    }
+}
+
+cudaError_t launch_batch_latch(const int* maxSpeedBits, const int* nonFinite, int ntun, float cap,
+                               const int* samples, int* latch, cudaStream_t st) {
+    batch_latch_kernel<<<(ntun + 63) / 64, 64, 0, st>>>(maxSpeedBits, nonFinite, ntun, cap, samples, latch);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_force_append(const double* cur, int n3, double* hist, int cap, int* count, cudaStream_t st) {
     force_append_kernel<<<1, 256, 0, st>>>(cur, n3, hist, cap, count);
     return cudaGetLastError();

@@ -12,7 +12,8 @@
 // a uniform index. Item decoding is 32-bit. Every cell runs the same per-cell
 // update as the single-tunnel kernels (collide_one), so a batch produces the
 // same populations, bit for bit, as stepping each tunnel on its own with the
-// same collision body.
+// same collision body. Items of a tunnel whose watchdog latch is set are
+// skipped: a diverged tunnel stops where it tripped.
 #pragma once
 
 #include "batch_types.h"
@@ -36,6 +37,7 @@ batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, un
             if (P.begins[mid] <= item) lo = mid;
             else hi = mid - 1;
         }
+        if (P.latch && P.latch[lo] != 0) continue;   // a latched tunnel no longer steps
         const BatchTunnelParam& tp = P.t[lo];
         CollideArgs a;
         a.nx = tp.nx; a.ny = tp.ny; a.nz = tp.nz; a.n = tp.n;

@@ -25,6 +25,9 @@ struct BatchTunnelParam {
 struct BatchTable {
     int ntun;
     float lambda, smagPre;
+    /// Per-tunnel watchdog latch in device memory (0 running; nonzero: the
+    /// tunnel diverged and its work items are skipped).
+    const int* latch;
     unsigned begins[kMaxBatchTunnels];
     BatchTunnelParam t[kMaxBatchTunnels];
 };

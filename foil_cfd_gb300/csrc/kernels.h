@@ -179,6 +179,11 @@ cudaError_t launch_force_append(const double* cur, int n3, double* hist, int cap
 /// *maxSpeedBits, which must start at 0) and non-finite cell count.
 cudaError_t launch_batch_health(bool fp32, const void* f, const std::uint8_t* kind, long long n, int* maxSpeedBits,
                                 int* nonFinite, cudaStream_t st);
+/// Set latch[t] (1 non-finite, 2 speed >= cap) of every running tunnel from
+/// its health scan (maxSpeedBits[t], nonFinite[t]), and latch[ntun + t] to the
+/// force-sample count *samples when it does.
+cudaError_t launch_batch_latch(const int* maxSpeedBits, const int* nonFinite, int ntun, float cap,
+                               const int* samples, int* latch, cudaStream_t st);
 
 // ---- refinement (refine_kernels.cu) ----------------------------------------
 struct RefineGeom {

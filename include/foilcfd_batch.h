@@ -109,10 +109,18 @@ int fcfd_batch_forces_now(fcfd_batch* b, double* out);
 
 /* Health of every tunnel at the current state: largest speed |u| over the
  * non-solid cells (max_speed, count floats) and the number of cells with a
- * non-finite density or momentum (non_finite, count ints). The batch has no
- * watchdog latch: a caller checks this after a run (a speed at the 0.3
- * limiter or any non-finite cell marks a diverged tunnel). */
+ * non-finite density or momentum (non_finite, count ints). */
 int fcfd_batch_health(fcfd_batch* b, float* max_speed, int* non_finite);
+/* Per-tunnel watchdog (the batch counterpart of the solver's NaN watchdog,
+ * lbm_core.cu:508-559): after every force sample (each force_every steps)
+ * the same full-field scan latches each tunnel that reached 0.95 x the 0.3
+ * limiter speed (verdict 2) or holds a non-finite cell (verdict 1); a
+ * latched tunnel stops stepping (its work items are skipped, its state
+ * freezes; its force samples repeat the frozen state) until
+ * fcfd_batch_reset. verdicts: count ints, 0 for a tunnel still running;
+ * steps_run (count long longs, may be NULL): the steps a tunnel has taken
+ * since the reset (up to its latch). Synchronises the batch stream. */
+int fcfd_batch_latched(fcfd_batch* b, int* verdicts, long long* steps_run);
 
 /* FP32 SoA populations of one tunnel (19 * cells floats). */
 int fcfd_batch_export_f32(fcfd_batch* b, int tunnel, float* f, size_t n);

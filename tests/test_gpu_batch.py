@@ -147,3 +147,40 @@ def test_device_built_polar_matches_host_built(fc):
         assert np.array_equal(bh.export_f32(i), bd.export_f32(i))
     assert np.array_equal(np.asarray(bh.forces_now()), np.asarray(bd.forces_now()))
 
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_watchdog_latches_and_stops_a_diverged_tunnel(fc, oracle_mod, storage):
+    """The batch's per-tunnel watchdog: a tunnel given a block of fluid at
+    |u| = 0.6 (twice the 0.3 limiter) is latched with verdict 2 at the next
+    force sample (every 2 steps here) and stops stepping (its populations
+    freeze, graph replays included), while the other tunnels keep stepping
+    exactly as their single-tunnel twins; a reset clears the latch."""
+    ts = small_polar()
+    b = make_batch(ts, storage, force_every=2)
+    f = b.export_f32(0).reshape(19, -1).copy()
+    nx, ny, nz = ts[0].dims
+    fl = ts[0].flags.reshape(nz, ny, nx)
+    hot = np.zeros((nz, ny, nx), bool)
+    hot[:, ny // 2 - 8:ny // 2 + 8, nx // 2 + 10:nx // 2 + 26] = True
+    hot &= fl == 0
+    m = hot.ravel()
+    k = int(m.sum())
+    assert k > 500
+    f[:, m] = oracle_mod.equilibrium(np.ones(k), np.full(k, 0.6), np.zeros(k), np.zeros(k), np.float32).reshape(19, k)
+    b.import_f32(0, f.ravel())
+    assert b.step_n(2, use_graphs=False) == 0
+    v, steps = b.latched(with_steps=True)
+    assert v[0] == 2 and not v[1:].any(), v
+    assert steps[0] == 2 and (steps[1:] == 2).all()
+    frozen = b.export_f32(0)
+    assert b.step_n(40, use_graphs=True) == 0
+    assert np.array_equal(b.export_f32(0), frozen)
+    v, steps = b.latched(with_steps=True)
+    assert not v[1:].any() and steps[0] == 2 and (steps[1:] == 42).all()
+    for i in range(1, len(ts)):
+        s = single(fc, ts[i], storage)
+        assert s.step_n(42) == 0
+        assert np.array_equal(b.export_f32(i), s.export_f32()), (storage, i)
+    b.reset()
+    assert not b.latched().any()
