@@ -826,6 +826,58 @@ def reference_cuda_leg(warmup=100, steps=100):
     return out
 
 
+def layout_leg(dims=(640, 192, 192), steps=100, warmup=20, tg_steps=1000):
+    """The two streaming layouts on the same work: an all-fluid periodic box
+    (Smagorinsky on, tau 0.52, uniform flow u 0.08 with the spanwise speck),
+    A/B ping-pong against the AA in-place pattern, each storage. Whole-step
+    GLUPS from CUDA events around `steps` steps, and the collide launches
+    timed one by one for the roofline (algorithmic bytes 2 x 19 populations
+    per cell, plus the kind byte the A/B kernel reads). Also the Taylor-Green
+    64^3 case (1000 steps, nu 0.01, no LES) in both layouts on the GPU."""
+    import foil_cfd_gb300 as fc
+    peak, kind = peaks()
+    n = int(np.prod(dims))
+    out = {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} all-fluid periodic box, TRT + Smagorinsky Cs 0.1, "
+                       "tau 0.52, u 0.08 + speck", "steps": steps, "warmup": warmup, "peak_kind": kind}
+    for storage in ("fp32", "fp16"):
+        for layout in ("ab", "aa"):
+            sol = fc.LBMSolver()
+            sol.init(dims, fc.scaling_direct(0.52, 0.08), np.zeros(n, np.uint8), storage=storage, les_cs=0.1,
+                     layout=layout)
+            sol.set_startup_ramp_enabled(False)
+            sol.reset()
+            assert sol.step_n(warmup) == 0
+            ms = timed_steps(sol, steps)
+            sol.enable_collide_timing(True)
+            timed_steps(sol, 40)
+            col_ms, col_n, _cells, col_bytes = sol.collide_time_ms()
+            sol.enable_collide_timing(False)
+            avg = col_ms / max(col_n, 1)
+            achieved = col_bytes / max(col_n, 1) / (avg * 1e-3) / 1e9
+            out[f"{storage}_{layout}"] = {
+                "glups": round(n * steps / (ms * 1e-3) / 1e9, 3), "ms_per_step": round(ms / steps, 4),
+                "collide_ms": round(avg, 4), "collide_gbs": round(achieved, 1),
+                "collide_frac": round(achieved / peak, 4), "latched": bool(sol.nan_detected())}
+            del sol
+        out[f"{storage}_aa_over_ab"] = round(out[f"{storage}_aa"]["glups"] / out[f"{storage}_ab"]["glups"], 4)
+    from foil_cfd_gb300 import tunnels
+    tg = tunnels.taylor_green_periodic(64, 0.05)
+    macro = (np.ones(64 ** 3, np.float32), tg.extra["u"], tg.extra["v"], np.zeros(64 ** 3, np.float32))
+    for layout in ("ab", "aa"):
+        sol = fc.LBMSolver()
+        sol.init(tg.dims, fc.scaling_direct(0.53, 0.0), tg.flags, les_cs=-1.0, layout=layout)
+        sol.set_startup_ramp_enabled(False)
+        sol.reset()
+        sol.restore_from_macroscopic(*macro)
+        assert sol.step_n(20) == 0
+        sol.restore_from_macroscopic(*macro)
+        ms = timed_steps(sol, tg_steps)
+        out[f"taylor_green_64_{layout}"] = {"ms_1000_steps": round(ms * 1000.0 / tg_steps, 3),
+                                            "glups": round(64 ** 3 * tg_steps / (ms * 1e-3) / 1e9, 3)}
+        del sol
+    return out
+
+
 def _uniform_feq(u):
     """feq(1, u, 0, 0) per direction in FP32, in the reference's equilibrium19
     expression order without contraction (the harness's uniform start)."""
@@ -1043,6 +1095,9 @@ def main():
     ap.add_argument("--only-stability", action="store_true",
                     help="run only the watchdog-trip comparison with the reference's own step")
     ap.add_argument("--no-stability", action="store_true", help="skip the watchdog-trip comparison")
+    ap.add_argument("--only-layout", action="store_true", help="run only the A/B vs AA layout comparison")
+    ap.add_argument("--no-layout", action="store_true", help="skip the A/B vs AA layout comparison")
+    ap.add_argument("--layout-dims", default="640,192,192", help="box of the layout comparison")
     ap.add_argument("--polar-config", default="", help="block,rows,ctas_per_sm,group_mb: skip the autotuner")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
@@ -1095,6 +1150,11 @@ def main():
         if rank == 0:
             print(json.dumps({"stability": stability_leg()}))
         return
+    if args.only_layout:
+        if rank == 0:
+            print(json.dumps({"layout": layout_leg(tuple(int(v) for v in args.layout_dims.split(",")),
+                                                   steps=args.steps, warmup=warmup)}))
+        return
     if args.only_polar:
         if rank == 0:
             fixed = tuple(int(v) for v in args.polar_config.split(",")) if args.polar_config else None
@@ -1139,6 +1199,8 @@ def main():
         line["precision"] = precision_leg()
     if ws == 1 and not args.small and not args.no_stability:
         line["stability"] = stability_leg()
+    if ws == 1 and not args.small and not args.no_layout:
+        line["layout"] = layout_leg()
     del r32
     if not args.no_fp16:
         r16 = measure(t, "fp16", args.steps, warmup, None)

@@ -29,7 +29,7 @@ class Scaling(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("storage", C.c_int), ("les_cs", C.c_float), ("magic_lambda", C.c_float),
-                ("use_graphs", C.c_int), ("collide_kernel", C.c_int)]
+                ("use_graphs", C.c_int), ("collide_kernel", C.c_int), ("layout", C.c_int)]
 
 
 class Lattice(C.Structure):

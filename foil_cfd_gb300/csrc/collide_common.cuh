@@ -570,6 +570,101 @@ collide_flat_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
                                   static_cast<int>(row - z * divY.d), static_cast<int>(z), &off);
 }
 
+// ---- AA-pattern in-place streaming (all-fluid periodic lattices) --------------
+// One population array A instead of the A/B pair (Bailey, Myre, Walsh, Lilja,
+// Wilson 2009, "Accelerating lattice Boltzmann fluid flow simulations using
+// graphics processors"). Between steps the array holds one of two layouts:
+//  * swapped:  A[opp(q)][x] = f*_q(x), each cell's post-collision populations
+//    with the slots of every opposite pair exchanged;
+//  * streamed: A[q][x] = f*_q(x - c_q), the post-streaming populations.
+// An odd step reads the swapped layout from the upstream cells, f_q(x) =
+// A[opp(q)][x - c_q], collides and writes f*_q(x) to A[q][x + c_q] -- the
+// slot it read for direction opp(q) -- leaving the streamed layout. An even
+// step reads A[q][x] of its own cell and writes f*_q(x) to A[opp(q)][x],
+// leaving the swapped layout. Every cell writes exactly the slots it read and
+// no other cell touches them, so the update is in place without races, and
+// the non-coherent loads never see a slot another thread has written. The
+// populations entering each collision are the A/B kernel's, so the results
+// are identical bit for bit. Opposite directions share a weight, so the FP16
+// deviation bytes move between slots unchanged.
+
+/// Byte offsets from &A[0][x] of the odd-step read A[opp(q)][x - c_q] of an
+/// interior cell; its write A[q][x + c_q] is the read offset of opp(q).
+struct AAOffsets {
+    long long rd[kQ];
+};
+
+template <class T>
+__host__ AAOffsets aa_offsets(int nx, int ny, long long n) {
+    AAOffsets o;
+    const long long sx = nx, sxy = static_cast<long long>(nx) * ny;
+    for (int q = 0; q < kQ; ++q)
+        o.rd[q] = (opp(q) * n - (cx(q) + sx * cy(q) + sxy * cz(q))) * static_cast<long long>(sizeof(T));
+    return o;
+}
+
+template <class S, bool EXACT, bool ODD>
+__global__ void __launch_bounds__(kCellBlockX, S::kCellMinBlocks)
+collide_aa_kernel(typename S::T* __restrict__ A, CollideArgs a, const __grid_constant__ AAOffsets off) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= a.nx) return;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const unsigned unx = a.nx, uny = a.ny;
+    const unsigned cell = static_cast<unsigned>(x) + unx * (static_cast<unsigned>(y) + uny * static_cast<unsigned>(z));
+    const long long n = a.n;
+    using P = Pop<S, !EXACT>;
+    float f[kQ], r, ux, uy, uz;
+    // One collision body for every path; the wrapped neighbour indices of a
+    // face cell are formed again for the stores rather than held across it.
+    const bool inner = ODD && interior(x, y, z, a);
+    typename S::T* base = A + cell;
+    if constexpr (!ODD) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) f[q] = P::ld(A + q * n, cell, wgt(q));
+    } else if (inner) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) f[q] = P::ld(byte_add(base, off.rd[q]), 0, wgt(q));
+    } else {
+        const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
+#pragma unroll
+        for (int q = 0; q < kQ; ++q)
+            f[q] = P::ld(A + opp(q) * n, b.sx[1 + cx(q)] + unx * (b.sy[1 + cy(q)] + uny * b.sz[1 + cz(q)]), wgt(q));
+    }
+    collide_body<EXACT>(f, a, r, ux, uy, uz);
+    if constexpr (!ODD) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) P::st(A + opp(q) * n, cell, f[q], wgt(q));
+    } else if (inner) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) P::st(byte_add(base, off.rd[opp(q)]), 0, f[q], wgt(q));
+    } else {
+        const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
+#pragma unroll
+        for (int q = 0; q < kQ; ++q)
+            P::st(A + q * n, b.sx[1 - cx(q)] + unx * (b.sy[1 - cy(q)] + uny * b.sz[1 - cz(q)]), f[q], wgt(q));
+    }
+    if (a.writeMacro) { a.rho[cell] = r; a.u[cell] = ux; a.v[cell] = uy; a.w[cell] = uz; }
+}
+
+template <class S, bool EXACT>
+cudaError_t launch_collide_aa_impl(void* fv, LevelDims d, const CollideParams& p, int odd, float* rho, float* u,
+                                   float* v, float* w, cudaStream_t st) {
+    using T = typename S::T;
+    CollideArgs a{};
+    a.nx = d.nx; a.ny = d.ny; a.nz = d.nz; a.n = d.cells();
+    a.tau0 = p.tau; a.lambda = p.magicLambda; a.smagPre = p.smagPrefactor; a.uIn = p.uInlet;
+    a.writeMacro = (p.writeMacro && rho && u && v && w) ? 1 : 0;
+    a.rho = rho; a.u = u; a.v = v; a.w = w;
+    T* f = static_cast<T*>(fv);
+    const int bx = d.nx >= kCellBlockX ? kCellBlockX : ((d.nx + 31) / 32) * 32;
+    const dim3 grid(static_cast<unsigned>((d.nx + bx - 1) / bx), static_cast<unsigned>(d.ny),
+                    static_cast<unsigned>(d.nz));
+    const AAOffsets off = aa_offsets<T>(d.nx, d.ny, a.n);
+    if (odd) collide_aa_kernel<S, EXACT, true><<<grid, bx, 0, st>>>(f, a, off);
+    else collide_aa_kernel<S, EXACT, false><<<grid, bx, 0, st>>>(f, a, off);
+    return cudaGetLastError();
+}
+
 // ---- warm-restart flag edits (applyFlagEditsKernel, lbm_core.cu:644-717) -----
 // mask 1: newly solid -> every population of both buffers zeroed; mask 2:
 // newly fluid -> equilibrium of the mean rho, u of the neighbours (x + c_q,

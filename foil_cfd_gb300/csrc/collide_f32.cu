@@ -53,6 +53,11 @@ cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint
     return launch_collide_impl<StoreF32, true>(src, dst, kind, d, p, rho, u, v, w, slip, st);
 }
 
+cudaError_t launch_collide_aa_f32(float* f, LevelDims d, const CollideParams& p, int odd, float* rho, float* u,
+                                  float* v, float* w, cudaStream_t st) {
+    return launch_collide_aa_impl<StoreF32, true>(f, d, p, odd, rho, u, v, w, st);
+}
+
 cudaError_t launch_collide_child_f32(const float* src, float* dst, const std::uint8_t* kind, LevelDims d,
                                      const CollideParams& p, SlipField slip, const ChildFuse& cf, cudaStream_t st) {
     return launch_collide_child_impl<StoreF32, true>(src, dst, kind, d, p, slip, cf, st);

@@ -73,6 +73,17 @@ cudaError_t launch_store_to_f32(Storage s, const void* in, float* out,
                                 long long cells, cudaStream_t st);
 cudaError_t launch_fill(float* dst, long long n, float v, cudaStream_t st);
 
+/// AA-pattern in-place step of an all-fluid periodic level (one population
+/// array): odd steps read the swapped layout and leave the streamed one, even
+/// steps the reverse (collide_common.cuh).
+cudaError_t launch_collide_aa(Storage s, void* f, LevelDims d, const CollideParams& p, int odd, float* rho,
+                              float* u, float* v, float* w, cudaStream_t st);
+/// A/B state <-> swapped layout, in place.
+cudaError_t launch_aa_pair_swap(Storage s, void* f, long long cells, cudaStream_t st);
+/// Streamed layout -> A/B state (toAB 1) or back (0), in place through a
+/// one-slice scratch buffer (cells elements of the storage type).
+cudaError_t launch_aa_shift(Storage s, void* f, void* slice, LevelDims d, int toAB, cudaStream_t st);
+
 /// The restriction's child-average pass fused into the last fine sub-step
 /// (factor 2): scratch records of the coarse cells of the restricted sub-box.
 struct ChildFuse {
@@ -94,6 +105,8 @@ cudaError_t launch_collide_f32_ref(const float* src, float* dst, const std::uint
                                    LevelDims d, const CollideParams& p, float* rho,
                                    float* u, float* v, float* w, SlipField slip,
                                    cudaStream_t st);
+cudaError_t launch_collide_aa_f32(float* f, LevelDims d, const CollideParams& p, int odd, float* rho, float* u,
+                                  float* v, float* w, cudaStream_t st);
 /// Whether the staged kernel serves a level (16-byte rows, >= 2 stages fit).
 bool staged_applies(LevelDims d, Storage s);
 cudaError_t launch_init_eq_f32(float* f, const std::uint8_t* kind, long long n, float uIn,

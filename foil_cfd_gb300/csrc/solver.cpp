@@ -53,6 +53,19 @@ void assign_flags(std::vector<std::uint8_t>& v, const std::uint8_t* p, size_t n)
     else std::memcpy(v.data(), p, n);
 }
 
+/// The AA layout's lattices: every cell fluid (periodic on all three axes).
+bool aa_lattice(const std::uint8_t* host, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (host[i] != FCFD_FLAG_FLUID) return false;
+    return true;
+}
+bool aa_flags_ok(const std::uint8_t* p, size_t n) {
+    if (!on_device(p)) return aa_lattice(p, n);
+    std::vector<std::uint8_t> h;
+    assign_flags(h, p, n);
+    return aa_lattice(h.data(), n);
+}
+
 template <class T>
 cudaError_t dalloc(T** p, size_t bytes) {
     return cudaMalloc(reinterpret_cast<void**>(p), bytes == 0 ? 1 : bytes);
@@ -185,6 +198,16 @@ struct fcfd_solver {
     float lambda = kDefaultLambda;
     int collideKernel = 0;
     bool initialized = false;
+    // AA-pattern layout (fcfd_options.layout): one population array. Between
+    // steps it holds the swapped layout (next step odd) or the streamed one
+    // (next step even) -- or, after the state was read or written through the
+    // API, the A/B state (aaAB), turned back into the swapped layout before
+    // the next step. aaSlice is the one-slice scratch of the streamed
+    // layout's conversion.
+    bool aa = false;
+    bool aaAB = false;
+    int aaNextOdd = 1;
+    void* aaSlice = nullptr;
 
     // ---- levels ----
     Level coarse;
@@ -324,8 +347,8 @@ struct fcfd_solver {
         L.d = d;
         L.n = d.cells();
         const size_t fb = static_cast<size_t>(L.n) * 19 * (storage == Storage::F32 ? 4 : 2);
-        for (void*& p : L.f)
-            if (auto e = cudaMalloc(&p, fb); e != cudaSuccess) return e;
+        for (int i = 0; i < (aa ? 1 : 2); ++i)
+            if (auto e = cudaMalloc(&L.f[i], fb); e != cudaSuccess) return e;
         if (auto e = dalloc(&L.flags, static_cast<size_t>(L.n)); e != cudaSuccess) return e;
         // Kind bytes are fetched in 16-byte-aligned row copies that may run
         // up to 31 bytes past the last row: pad the allocation.
@@ -593,6 +616,7 @@ struct fcfd_solver {
             st.pending = false;
             Level* L = levelAt(level);
             if (!L || st.bytes != static_cast<size_t>(L->n) * 19 * sizeof(float)) return cudaErrorInvalidValue;
+            if (level == 0) aaAB = aa;
             cudaError_t e;
             if (storage == Storage::F32) {
                 e = cudaMemcpyAsync(L->f[L->src], st.buf, st.bytes, cudaMemcpyDeviceToDevice, stream);
@@ -613,6 +637,7 @@ struct fcfd_solver {
         freeStaged();
         freeFine();
         coarse.free_all();
+        dfree(aaSlice);
         dfree(rho); dfree(u); dfree(v); dfree(w); dfree(dForce); dfree(dNan); dfree(dStatus);
         dfree(dNetW);
         wallMethod = 0;
@@ -632,14 +657,22 @@ struct fcfd_solver {
 
     // ---- stepping ----
     cudaError_t collide(Level& L, const CollideParams& p, float* r, float* uu, float* vv, float* ww) {
-        cudaEvent_t e2 = collideTiming ? colT.begin(static_cast<double>(L.n), L.collideBytes(storage), stream)
-                                       : nullptr;
+        // The AA kernels read no kind byte: 2 x 19 populations per cell.
+        const double bytes = aa ? 38.0 * (storage == Storage::F32 ? 4.0 : 2.0) * static_cast<double>(L.n)
+                                : L.collideBytes(storage);
+        cudaEvent_t e2 = collideTiming ? colT.begin(static_cast<double>(L.n), bytes, stream) : nullptr;
         ++launches;
         CollideParams lp = p;
         lp.qFrac = L.dQFrac;
         lp.ffMask = L.dFFMask;
-        const cudaError_t e = launch_collide(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, lp, r, uu,
-                                             vv, ww, L.wm.slip(), stream);
+        cudaError_t e;
+        if (aa) {
+            e = launch_collide_aa(storage, L.f[0], L.d, lp, aaNextOdd, r, uu, vv, ww, stream);
+            aaNextOdd ^= 1;
+        } else {
+            e = launch_collide(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, lp, r, uu, vv, ww, L.wm.slip(),
+                               stream);
+        }
         if (e2) cudaEventRecord(e2, stream);
         return e;
     }
@@ -683,11 +716,28 @@ struct fcfd_solver {
                                   wallMethod, &netView);
     }
 
+    /// AA layout: leave the A/B state (post-collision f*_q(x) in slot q of
+    /// cell x) in the population array for a reader; a no-op otherwise.
+    cudaError_t aaToAB() {
+        if (!aa || aaAB) return cudaSuccess;
+        launches += aaNextOdd ? 1 : 18;
+        const cudaError_t e = aaNextOdd ? launch_aa_pair_swap(storage, coarse.f[0], coarse.n, stream)
+                                        : launch_aa_shift(storage, coarse.f[0], aaSlice, coarse.d, 1, stream);
+        if (e == cudaSuccess) aaAB = true;
+        return e;
+    }
+
     int stepN(int n) {
         if (!initialized) return cudaErrorNotReady;
         if (n <= 0) return cudaSuccess;
         pollAsync();
         if (nanLatched) return cudaSuccess;
+        if (aa && aaAB) {
+            ++launches;
+            if (auto e = launch_aa_pair_swap(storage, coarse.f[0], coarse.n, stream); e != cudaSuccess) return e;
+            aaAB = false;
+            aaNextOdd = 1;
+        }
         const bool timeIt = !timingPending;
         if (timeIt) cudaEventRecord(evT0, stream);
         for (int i = 0; i < n; ++i) {
@@ -763,7 +813,7 @@ struct fcfd_solver {
                     e != cudaSuccess)
                     return e;
             }
-            coarse.src = 1 - coarse.src;
+            if (!aa) coarse.src = 1 - coarse.src;
             ++steps;
             if (++sinceWatchdog >= kWatchdogPeriod && !nanPending) {
                 sinceWatchdog = 0;
@@ -825,12 +875,13 @@ struct fcfd_solver {
         cudaMemsetAsync(dNan, 0, sizeof(int), stream);
         cudaMemsetAsync(dStatus, 0, sizeof(int), stream);
         const float initU = rampEnabled ? 0.0f : scaling.u_lat;
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < (aa ? 1 : 2); ++i) {
             launches += 2;
             launch_init_equilibrium(storage, coarse.f[i], coarse.kind, coarse.d, initU, stream);
             launch_speck(storage, coarse.f[i], coarse.kind, coarse.d, kSpeckAmplitudeFrac * scaling.u_lat,
                          kSpeckSeed, stream);
         }
+        aaAB = aa;
         seedFine();
         seedFiner();
         resetWMState();
@@ -851,6 +902,7 @@ struct fcfd_solver {
     cudaError_t importF32(Level& L, const float* host, size_t count) {
         if (count != static_cast<size_t>(L.n) * 19) return cudaErrorInvalidValue;
         const size_t bytes = count * sizeof(float);
+        if (&L == &coarse) aaAB = aa;  // a whole A/B state replaces the layout
         if (storage == Storage::F32)
             return cudaMemcpy(L.f[L.src], host, bytes, cudaMemcpyHostToDevice);
         float* stage = nullptr;
@@ -865,6 +917,8 @@ struct fcfd_solver {
     cudaError_t exportF32(Level& L, float* host, size_t count) {
         if (count != static_cast<size_t>(L.n) * 19) return cudaErrorInvalidValue;
         const size_t bytes = count * sizeof(float);
+        if (&L == &coarse)
+            if (auto e = aaToAB(); e != cudaSuccess) return e;
         if (auto e = cudaStreamSynchronize(stream); e != cudaSuccess) return e;
         if (storage == Storage::F32)
             return cudaMemcpy(host, L.f[L.src], bytes, cudaMemcpyDeviceToHost);
@@ -980,11 +1034,20 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
     s->lesCs = kDefaultCs;
     s->lambda = kDefaultLambda;
     s->collideKernel = 0;
+    s->aa = false;
+    s->aaAB = false;
+    s->aaNextOdd = 1;
     if (opts) {
         s->storage = opts->storage == FCFD_STORE_FP16 ? Storage::F16 : Storage::F32;
         if (opts->les_cs != 0.0f) s->lesCs = opts->les_cs;
         if (opts->magic_lambda > 0.0f) s->lambda = opts->magic_lambda;
         s->collideKernel = (opts->collide_kernel >= 0 && opts->collide_kernel <= 2) ? opts->collide_kernel : 0;
+        s->aa = opts->layout == FCFD_LAYOUT_AA;
+    }
+    if (s->aa && !aa_lattice(hf, n)) {
+        set_err(err, errlen, "the AA layout serves all-fluid periodic lattices only");
+        s->aa = false;
+        return cudaErrorNotSupported;
     }
     auto fail = [&](const char* what, cudaError_t e) {
         set_err(err, errlen, std::string(what) + ": " + cudaGetErrorString(e));
@@ -994,6 +1057,9 @@ int fcfd_init(fcfd_solver* s, const fcfd_dims* dims, const fcfd_scaling* scaling
     };
     if (auto e = s->allocLevel(s->coarse, d); e != cudaSuccess) return fail("population buffer allocation failed", e);
     const size_t cells = static_cast<size_t>(d.cells());
+    if (s->aa)
+        if (auto e = cudaMalloc(&s->aaSlice, cells * (s->storage == Storage::F32 ? 4 : 2)); e != cudaSuccess)
+            return fail("AA scratch allocation failed", e);
     for (float** p : {&s->rho, &s->u, &s->v, &s->w})
         if (auto e = dalloc(p, cells * 4); e != cudaSuccess) return fail("macroscopic allocation failed", e);
     if (auto e = dalloc(&s->dForce, 3 * sizeof(double)); e != cudaSuccess) return fail("force slot allocation failed", e);
@@ -1034,6 +1100,7 @@ void fcfd_reset(fcfd_solver* s) {
 
 int fcfd_set_flags(fcfd_solver* s, const uint8_t* flags, size_t n) {
     if (!s || !s->initialized || !flags || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
+    if (s->aa && !aa_flags_ok(flags, n)) return cudaErrorNotSupported;
     if (auto e = s->uploadLevelFlags(s->coarse, flags); e != cudaSuccess) return e;
     s->updateForcesFromFine();
     if (auto e = s->buildWM(s->coarse, kWallSampleCoarse); e != cudaSuccess) return e;
@@ -1044,6 +1111,7 @@ int fcfd_set_flags(fcfd_solver* s, const uint8_t* flags, size_t n) {
 int fcfd_apply_edited_flags(fcfd_solver* s, const uint8_t* flags, size_t n, long long* edited) {
     if (edited) *edited = 0;
     if (!s || !s->initialized || !flags || n != static_cast<size_t>(s->coarse.n)) return cudaErrorInvalidValue;
+    if (s->aa && !aa_flags_ok(flags, n)) return cudaErrorNotSupported;
     Level& L = s->coarse;
     std::vector<std::uint8_t> hostNew;
     const std::uint8_t* nf = flags;
@@ -1180,6 +1248,7 @@ int fcfd_lattice_view(fcfd_solver* s, int level, fcfd_lattice* out) {
     if (!s->initialized) return cudaErrorNotReady;
     const Level* L = active_level(s, level);
     if (!L) return cudaErrorInvalidValue;
+    if (auto e = s->aaToAB(); e != cudaSuccess) return e;
     out->f = L->f[L->src];
     out->flags = L->flags;
     out->dims = fcfd_dims{L->d.nx, L->d.ny, L->d.nz};
@@ -1235,7 +1304,10 @@ int fcfd_download_macro(fcfd_solver* s, float* r, float* u, float* v, float* w) 
     return cudaStreamSynchronize(s->stream);
 }
 
-void* fcfd_active_f(fcfd_solver* s) { return (s && s->initialized) ? s->coarse.f[s->coarse.src] : nullptr; }
+void* fcfd_active_f(fcfd_solver* s) {
+    if (!s || !s->initialized || s->aaToAB() != cudaSuccess) return nullptr;
+    return s->coarse.f[s->coarse.src];
+}
 
 size_t fcfd_f_bytes(const fcfd_solver* s) {
     if (!s || !s->initialized) return 0;
@@ -1256,6 +1328,7 @@ int fcfd_import_f32(fcfd_solver* s, const float* f, size_t count) {
 int fcfd_mirror_buffers(fcfd_solver* s) {
     if (!s || !s->initialized) return cudaErrorInvalidValue;
     const size_t pop = s->storage == Storage::F32 ? 4 : 2;
+    if (s->aa) return 0;  // one population array: nothing to mirror
     Level* levels[3] = {&s->coarse, s->fineActive ? &s->fine : nullptr, s->finerActive ? &s->finer : nullptr};
     for (Level* L : levels) {
         if (!L) continue;
@@ -1288,13 +1361,14 @@ int fcfd_restore_from_macro(fcfd_solver* s, const float* r, const float* u, cons
     struct { const float* h; float* d; } c[] = {{r, s->rho}, {u, s->u}, {v, s->v}, {w, s->w}};
     for (auto& x : c)
         if (auto e = cudaMemcpyAsync(x.d, x.h, b, cudaMemcpyHostToDevice, s->stream); e != cudaSuccess) return e;
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < (s->aa ? 1 : 2); ++i) {
         ++s->launches;
         if (auto e = launch_init_from_macro(s->storage, s->coarse.f[i], s->coarse.kind, s->coarse.d, s->rho,
                                             s->u, s->v, s->w, s->stream);
             e != cudaSuccess)
             return e;
     }
+    s->aaAB = s->aa;
     s->notifyRestored(false);
     if (auto e = s->seedFine(); e != cudaSuccess) return e;
     if (auto e = s->seedFiner(); e != cudaSuccess) return e;
@@ -1448,6 +1522,10 @@ int fcfd_init_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor, 
     if (!s || !s->initialized) {
         set_err(err, errlen, "solver not initialized");
         return cudaErrorNotReady;
+    }
+    if (s->aa) {
+        set_err(err, errlen, "the AA layout serves all-fluid periodic lattices only (no refinement)");
+        return cudaErrorNotSupported;
     }
     fcfd_shutdown_refinement(s);
     if (!box || !ff) {
@@ -1761,6 +1839,7 @@ int fcfd_set_q_links(fcfd_solver* s, int level, const uint8_t* qFrac, size_t nq,
                      size_t nm, int links, int fallback) {
     Level* L = level_of(s, level);
     if (!L) return cudaErrorInvalidValue;
+    if (s->aa && nq != 0) return cudaErrorNotSupported;
     cudaStreamSynchronize(s->stream);
     dfree(L->dQFrac);
     dfree(L->dFFMask);
@@ -1909,6 +1988,7 @@ int fcfd_export_finer_f32(fcfd_solver* s, float* f, size_t count) {
 int fcfd::solver_field_view(fcfd_solver* s, SolverFieldView* v) {
     if (!s || !s->initialized || !v) return cudaErrorNotReady;
     *v = SolverFieldView{};
+    if (auto e = s->aaToAB(); e != cudaSuccess) return e;
     const size_t pop = s->storage == Storage::F32 ? 4 : 2;
     const Level* levels[3] = {&s->coarse, s->fineActive ? &s->fine : nullptr,
                                            s->finerActive ? &s->finer : nullptr};

@@ -131,6 +131,37 @@ __global__ void store_to_f32_kernel(const typename S::T* __restrict__ in, float*
     out[i] = S::ld(in, i, wgt(q));
 }
 
+/// AA pattern: exchange the slots of every opposite pair of each cell, in
+/// place (A/B state <-> swapped layout). E is the raw element type; opposite
+/// directions share a weight, so FP16 deviation bytes move unchanged.
+template <class E>
+__global__ void aa_pair_swap_kernel(E* __restrict__ f, long long n) {
+    const long long c = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+#pragma unroll
+    for (int q = 1; q < kQ; q += 2) {
+        const E a = f[q * n + c], b = f[(q + 1) * n + c];
+        f[q * n + c] = b;
+        f[(q + 1) * n + c] = a;
+    }
+}
+
+/// AA pattern: out[x] = in[x + s] of one direction slice, periodic on all
+/// three axes (s = +c_q: streamed layout -> A/B state; s = -c_q: back).
+template <class E>
+__global__ void aa_shift_kernel(const E* __restrict__ in, E* __restrict__ out, int nx, int ny, int nz, int sx,
+                                int sy, int sz) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nx) return;
+    const int y = blockIdx.y, z = blockIdx.z;
+    int xs = x + sx, ys = y + sy, zs = z + sz;
+    xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
+    ys = ys < 0 ? ys + ny : (ys >= ny ? ys - ny : ys);
+    zs = zs < 0 ? zs + nz : (zs >= nz ? zs - nz : zs);
+    out[x + static_cast<long long>(nx) * (y + static_cast<long long>(ny) * z)] =
+        in[xs + static_cast<long long>(nx) * (ys + static_cast<long long>(ny) * zs)];
+}
+
 __global__ void fill_kernel(float* __restrict__ d, long long n, float v) {
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n) d[i] = v;
@@ -165,6 +196,46 @@ cudaError_t launch_collide(Storage s, const void* src, void* dst, const std::uin
         return launch_collide_f32_ref(static_cast<const float*>(src), static_cast<float*>(dst), kind, d, p,
                                       rho, u, v, w, slip, st);
     return launch_collide_impl<StoreF16, false>(src, dst, kind, d, p, rho, u, v, w, slip, st);
+}
+
+cudaError_t launch_collide_aa(Storage s, void* f, LevelDims d, const CollideParams& p, int odd, float* rho,
+                              float* u, float* v, float* w, cudaStream_t st) {
+    if (!f || d.cells() <= 0) return cudaErrorInvalidValue;
+    if (s == Storage::F32) return launch_collide_aa_f32(static_cast<float*>(f), d, p, odd, rho, u, v, w, st);
+    return launch_collide_aa_impl<StoreF16, false>(f, d, p, odd, rho, u, v, w, st);
+}
+
+cudaError_t launch_aa_pair_swap(Storage s, void* f, long long cells, cudaStream_t st) {
+    if (!f || cells <= 0) return cudaErrorInvalidValue;
+    if (s == Storage::F32)
+        aa_pair_swap_kernel<unsigned><<<blocks_for(cells), kBlock1D, 0, st>>>(static_cast<unsigned*>(f), cells);
+    else
+        aa_pair_swap_kernel<unsigned short><<<blocks_for(cells), kBlock1D, 0, st>>>(
+            static_cast<unsigned short*>(f), cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aa_shift(Storage s, void* f, void* slice, LevelDims d, int toAB, cudaStream_t st) {
+    const long long n = d.cells();
+    if (!f || !slice || n <= 0) return cudaErrorInvalidValue;
+    const size_t eb = s == Storage::F32 ? 4 : 2;
+    for (int q = 1; q < kQ; ++q) {
+        const int sg = toAB ? 1 : -1;
+        char* sl = static_cast<char*>(f) + static_cast<size_t>(q) * static_cast<size_t>(n) * eb;
+        if (s == Storage::F32)
+            aa_shift_kernel<unsigned><<<plane_grid(d, 128), 128, 0, st>>>(
+                reinterpret_cast<const unsigned*>(sl), static_cast<unsigned*>(slice), d.nx, d.ny, d.nz,
+                sg * cx(q), sg * cy(q), sg * cz(q));
+        else
+            aa_shift_kernel<unsigned short><<<plane_grid(d, 128), 128, 0, st>>>(
+                reinterpret_cast<const unsigned short*>(sl), static_cast<unsigned short*>(slice), d.nx, d.ny, d.nz,
+                sg * cx(q), sg * cy(q), sg * cz(q));
+        if (auto e = cudaGetLastError(); e != cudaSuccess) return e;
+        if (auto e = cudaMemcpyAsync(sl, slice, static_cast<size_t>(n) * eb, cudaMemcpyDeviceToDevice, st);
+            e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_collide_child(Storage s, const void* src, void* dst, const std::uint8_t* kind, LevelDims d,

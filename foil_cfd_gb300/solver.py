@@ -108,14 +108,17 @@ class LBMSolver:
 
     # ---- lifecycle -------------------------------------------------------
     def init(self, dims, scaling: capi.Scaling, flags: np.ndarray, stream=None, storage: str = "fp32",
-             les_cs: float | None = None, magic_lambda: float | None = None, kernel: str = "auto") -> None:
+             les_cs: float | None = None, magic_lambda: float | None = None, kernel: str = "auto",
+             layout: str = "ab") -> None:
         """kernel: "auto", "cell" (one cell per thread) or "staged" (rows
-        streamed through shared memory by bulk async copies)."""
+        streamed through shared memory by bulk async copies). layout: "ab"
+        (two population arrays, pull from one into the other) or "aa" (one
+        array updated in place; all-fluid periodic lattices only)."""
         fp, fn, _keep = _flags_arg(flags)
         d = capi.Dims(*dims)
         opt = capi.Options(STORE[storage], 0.0 if les_cs is None else (les_cs if les_cs > 0 else -1.0),
                            0.0 if magic_lambda is None else magic_lambda, 0,
-                           {"auto": 0, "cell": 1, "staged": 2}[kernel])
+                           {"auto": 0, "cell": 1, "staged": 2}[kernel], {"ab": 0, "aa": 1}[layout])
         err = C.create_string_buffer(512)
         rc = self._lib.fcfd_init(self._h, C.byref(d), C.byref(scaling), fp, fn, stream,
                                  C.byref(opt), err, 512)

@@ -82,7 +82,21 @@ typedef struct fcfd_options {
     int collide_kernel; /* 0 automatic (= 1), 1 one cell per thread,
                            2 staged rows (bulk async copies into shared
                            memory; slower on GB300, kept selectable) */
+    int layout;         /* FCFD_LAYOUT_AB (default) or FCFD_LAYOUT_AA     */
 } fcfd_options;
+
+/* Streaming layouts. AB: two population arrays, each step pulls from one
+ * into the other (the reference's ping-pong, lbm_solver.cpp:1156-1160). AA:
+ * one array updated in place, odd and even steps alternating between a
+ * swapped and a streamed slot layout (half the population memory; same
+ * results bit for bit). The AA layout serves all-fluid periodic lattices
+ * (every flag FCFD_FLAG_FLUID, no refinement, no link fields): fcfd_init
+ * refuses other flag fields with cudaErrorNotSupported, as do
+ * fcfd_set_flags, fcfd_apply_edited_flags, fcfd_init_refinement and
+ * fcfd_set_q_links. Every read of the populations through this interface
+ * (export, lattice view, fcfd_active_f, snapshots) sees the A/B state; the
+ * solver converts in place and back around such reads. */
+enum { FCFD_LAYOUT_AB = 0, FCFD_LAYOUT_AA = 1 };
 
 /* Refinement patch in coarse cells, [x0,x1) x [y0,y1) x [0,nz)
  * (PatchBox, src/sim/lbm_refine.cuh:54-61). */
