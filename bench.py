@@ -826,7 +826,7 @@ def reference_cuda_leg(warmup=100, steps=100):
     return out
 
 
-def layout_leg(dims=(640, 192, 192), steps=100, warmup=20, tg_steps=1000):
+def layout_leg(dims=(640, 192, 192), steps=100, warmup=20, tg_steps=1000, storages=("fp32", "fp16")):
     """The two streaming layouts on the same work: an all-fluid periodic box
     (Smagorinsky on, tau 0.52, uniform flow u 0.08 with the spanwise speck),
     A/B ping-pong against the AA in-place pattern, each storage. Whole-step
@@ -839,7 +839,7 @@ def layout_leg(dims=(640, 192, 192), steps=100, warmup=20, tg_steps=1000):
     n = int(np.prod(dims))
     out = {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} all-fluid periodic box, TRT + Smagorinsky Cs 0.1, "
                        "tau 0.52, u 0.08 + speck", "steps": steps, "warmup": warmup, "peak_kind": kind}
-    for storage in ("fp32", "fp16"):
+    for storage in storages:
         for layout in ("ab", "aa"):
             sol = fc.LBMSolver()
             sol.init(dims, fc.scaling_direct(0.52, 0.08), np.zeros(n, np.uint8), storage=storage, les_cs=0.1,
@@ -863,7 +863,7 @@ def layout_leg(dims=(640, 192, 192), steps=100, warmup=20, tg_steps=1000):
     from foil_cfd_gb300 import tunnels
     tg = tunnels.taylor_green_periodic(64, 0.05)
     macro = (np.ones(64 ** 3, np.float32), tg.extra["u"], tg.extra["v"], np.zeros(64 ** 3, np.float32))
-    for layout in ("ab", "aa"):
+    for layout in (("ab", "aa") if tg_steps > 0 else ()):
         sol = fc.LBMSolver()
         sol.init(tg.dims, fc.scaling_direct(0.53, 0.0), tg.flags, les_cs=-1.0, layout=layout)
         sol.set_startup_ramp_enabled(False)
@@ -1098,6 +1098,8 @@ def main():
     ap.add_argument("--only-layout", action="store_true", help="run only the A/B vs AA layout comparison")
     ap.add_argument("--no-layout", action="store_true", help="skip the A/B vs AA layout comparison")
     ap.add_argument("--layout-dims", default="640,192,192", help="box of the layout comparison")
+    ap.add_argument("--layout-storage", default="fp32,fp16", help="storages of the layout comparison")
+    ap.add_argument("--layout-tg-steps", type=int, default=1000, help="Taylor-Green steps per layout (0: none)")
     ap.add_argument("--polar-config", default="", help="block,rows,ctas_per_sm,group_mb: skip the autotuner")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "staged"],
                     help="collide kernel variant")
@@ -1153,7 +1155,8 @@ def main():
     if args.only_layout:
         if rank == 0:
             print(json.dumps({"layout": layout_leg(tuple(int(v) for v in args.layout_dims.split(",")),
-                                                   steps=args.steps, warmup=warmup)}))
+                                                   steps=args.steps, warmup=warmup, tg_steps=args.layout_tg_steps,
+                                                   storages=tuple(args.layout_storage.split(",")))}))
         return
     if args.only_polar:
         if rank == 0:

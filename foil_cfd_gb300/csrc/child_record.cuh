@@ -2,7 +2,12 @@
 // the density floor and the |u| <= 0.3 limiter, their non-equilibrium part,
 // and the scratch record the restriction filter reads (fneq[19], valid
 // flag, rho, ux, uy, uz; 96 B with FP32 storage, 64 B with FP16). Shared by the stand-alone
-// child-average kernel and the fine collide that fuses it. Every multiply
+// child-average kernel and the fine collide that fuses it.
+//
+// The scratch is planar: float4 k of record t sits at base[k * stride + t]
+// (stride = records in the scratch), so the 32 lanes of a warp reading the
+// same part of the records of 32 consecutive coarse cells read 512
+// contiguous bytes, not 32 pieces 96 bytes apart. Every multiply
 // and add is an explicit round-to-nearest intrinsic in the reference's
 // operation order, so the record rounds the same in a translation unit built
 // with or without FMA contraction, and is bit-identical to the reference's
@@ -66,51 +71,53 @@ template <class S> struct ChildRecord;
 
 template <> struct ChildRecord<StoreF32> {
     static constexpr int kVec = kScratchVals / 4;
-    __device__ __forceinline__ static void write(float4* rec, const float (&fneq)[kQ], float rho, float ux,
-                                                 float uy, float uz) {
+    __device__ __forceinline__ static void write(float4* rec, long long st, const float (&fneq)[kQ], float rho,
+                                                 float ux, float uy, float uz) {
         float r[kScratchVals];
 #pragma unroll
         for (int q = 0; q < kQ; ++q) r[q] = fneq[q];
         r[kScratchValid] = 1.0f;
         r[kScratchRho] = rho; r[kScratchRho + 1] = ux; r[kScratchRho + 2] = uy; r[kScratchRho + 3] = uz;
 #pragma unroll
-        for (int k = 0; k < kVec; ++k) rec[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+        for (int k = 0; k < kVec; ++k) rec[k * st] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
     }
-    __device__ __forceinline__ static void write_invalid(float4* rec) {
-        rec[kScratchValid / 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    __device__ __forceinline__ static void write_invalid(float4* rec, long long st) {
+        rec[(kScratchValid / 4) * st] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     /// fneq of the record into out; false (out untouched) when not valid.
-    __device__ __forceinline__ static bool load(const float4* rec, float (&out)[kQ]) {
-        const float4 v4 = __ldg(rec + kScratchValid / 4);   // fneq[16..18], valid
+    __device__ __forceinline__ static bool load(const float4* rec, long long st, float (&out)[kQ]) {
+        const float4 v4 = __ldg(rec + (kScratchValid / 4) * st);   // fneq[16..18], valid
         if (v4.w == 0.0f) return false;
         out[16] = v4.x; out[17] = v4.y; out[18] = v4.z;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float4 a = __ldg(rec + k);
+            const float4 a = __ldg(rec + k * st);
             out[4 * k] = a.x; out[4 * k + 1] = a.y; out[4 * k + 2] = a.z; out[4 * k + 3] = a.w;
         }
         return true;
     }
     /// acc[q] += fneq[q] for every q when the record is valid.
-    __device__ __forceinline__ static bool add(const float4* rec, float (&acc)[kQ]) {
-        const float4 last = __ldg(rec + kScratchValid / 4);
+    __device__ __forceinline__ static bool add(const float4* rec, long long st, float (&acc)[kQ]) {
+        const float4 last = __ldg(rec + (kScratchValid / 4) * st);
         if (last.w == 0.0f) return false;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float4 a = __ldg(rec + k);
+            const float4 a = __ldg(rec + k * st);
             acc[4 * k] += a.x; acc[4 * k + 1] += a.y; acc[4 * k + 2] += a.z; acc[4 * k + 3] += a.w;
         }
         acc[16] += last.x; acc[17] += last.y; acc[18] += last.z;
         return true;
     }
-    __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + kScratchRho / 4); }
+    __device__ __forceinline__ static float4 moments(const float4* rec, long long st) {
+        return __ldg(rec + (kScratchRho / 4) * st);
+    }
     /// As add, but every part of the record is read before the valid flag
     /// decides (a select keeps acc when the record is invalid), so the loads
     /// of successive neighbours do not wait on each other's flags.
-    __device__ __forceinline__ static bool add_sel(const float4* rec, float (&acc)[kQ]) {
+    __device__ __forceinline__ static bool add_sel(const float4* rec, long long st, float (&acc)[kQ]) {
         float4 a[5];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) a[k] = __ldg(rec + k);
+        for (int k = 0; k < 5; ++k) a[k] = __ldg(rec + k * st);
         const bool ok = a[4].w != 0.0f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -136,27 +143,27 @@ template <> struct ChildRecord<StoreF16> {
         const __half2 h = *reinterpret_cast<const __half2*>(&u);
         return __half22float2(h);
     }
-    __device__ __forceinline__ static void write(float4* rec, const float (&fneq)[kQ], float rho, float ux,
-                                                 float uy, float uz) {
+    __device__ __forceinline__ static void write(float4* rec, long long st, const float (&fneq)[kQ], float rho,
+                                                 float ux, float uy, float uz) {
         uint4* r = reinterpret_cast<uint4*>(rec);
         r[0] = make_uint4(pack(fneq[0], fneq[1]), pack(fneq[2], fneq[3]), pack(fneq[4], fneq[5]),
                           pack(fneq[6], fneq[7]));
-        r[1] = make_uint4(pack(fneq[8], fneq[9]), pack(fneq[10], fneq[11]), pack(fneq[12], fneq[13]),
-                          pack(fneq[14], fneq[15]));
-        r[2] = make_uint4(pack(fneq[16], fneq[17]), pack(fneq[18], 0.0f), __float_as_uint(1.0f), 0u);
-        rec[3] = make_float4(rho, ux, uy, uz);
+        r[st] = make_uint4(pack(fneq[8], fneq[9]), pack(fneq[10], fneq[11]), pack(fneq[12], fneq[13]),
+                           pack(fneq[14], fneq[15]));
+        r[2 * st] = make_uint4(pack(fneq[16], fneq[17]), pack(fneq[18], 0.0f), __float_as_uint(1.0f), 0u);
+        rec[3 * st] = make_float4(rho, ux, uy, uz);
     }
-    __device__ __forceinline__ static void write_invalid(float4* rec) {
-        reinterpret_cast<uint4*>(rec)[2] = make_uint4(0u, 0u, 0u, 0u);
+    __device__ __forceinline__ static void write_invalid(float4* rec, long long st) {
+        reinterpret_cast<uint4*>(rec)[2 * st] = make_uint4(0u, 0u, 0u, 0u);
     }
-    __device__ __forceinline__ static bool load(const float4* rec, float (&out)[kQ]) {
-        const uint4 c2 = __ldg(reinterpret_cast<const uint4*>(rec) + 2);
+    __device__ __forceinline__ static bool load(const float4* rec, long long st, float (&out)[kQ]) {
+        const uint4 c2 = __ldg(reinterpret_cast<const uint4*>(rec) + 2 * st);
         if (__uint_as_float(c2.z) == 0.0f) return false;
         const float2 p16 = unpack(c2.x), p18 = unpack(c2.y);
         out[16] = p16.x; out[17] = p16.y; out[18] = p18.x;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const uint4 c = __ldg(reinterpret_cast<const uint4*>(rec) + k);
+            const uint4 c = __ldg(reinterpret_cast<const uint4*>(rec) + k * st);
             const unsigned w[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -166,12 +173,12 @@ template <> struct ChildRecord<StoreF16> {
         }
         return true;
     }
-    __device__ __forceinline__ static bool add(const float4* rec, float (&acc)[kQ]) {
-        const uint4 c2 = __ldg(reinterpret_cast<const uint4*>(rec) + 2);
+    __device__ __forceinline__ static bool add(const float4* rec, long long st, float (&acc)[kQ]) {
+        const uint4 c2 = __ldg(reinterpret_cast<const uint4*>(rec) + 2 * st);
         if (__uint_as_float(c2.z) == 0.0f) return false;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const uint4 c = __ldg(reinterpret_cast<const uint4*>(rec) + k);
+            const uint4 c = __ldg(reinterpret_cast<const uint4*>(rec) + k * st);
             const unsigned w[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -183,11 +190,11 @@ template <> struct ChildRecord<StoreF16> {
         acc[16] += p16.x; acc[17] += p16.y; acc[18] += p18.x;
         return true;
     }
-    __device__ __forceinline__ static float4 moments(const float4* rec) { return __ldg(rec + 3); }
-    __device__ __forceinline__ static bool add_sel(const float4* rec, float (&acc)[kQ]) {
+    __device__ __forceinline__ static float4 moments(const float4* rec, long long st) { return __ldg(rec + 3 * st); }
+    __device__ __forceinline__ static bool add_sel(const float4* rec, long long st, float (&acc)[kQ]) {
         uint4 c[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) c[k] = __ldg(reinterpret_cast<const uint4*>(rec) + k);
+        for (int k = 0; k < 3; ++k) c[k] = __ldg(reinterpret_cast<const uint4*>(rec) + k * st);
         const bool ok = __uint_as_float(c[2].z) != 0.0f;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
@@ -208,11 +215,12 @@ template <> struct ChildRecord<StoreF16> {
 };
 
 /// Record of a coarse cell from the sum fi of its nFluid fluid children
-/// (sums of the deviations f - w_q when DEV).
+/// (sums of the deviations f - w_q when DEV), at rec = base + t of a planar
+/// scratch of stride st.
 template <class S, bool DEV = false>
-__device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, float4* rec) {
+__device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, float4* rec, long long st) {
     if (nFluid == 0) {
-        ChildRecord<S>::write_invalid(rec);
+        ChildRecord<S>::write_invalid(rec, st);
         return;
     }
     const float invN = 1.0f / static_cast<float>(nFluid);
@@ -224,7 +232,7 @@ __device__ __forceinline__ void write_child_record(float (&fi)[kQ], int nFluid, 
     float fneq[kQ];
 #pragma unroll
     for (int q = 0; q < kQ; ++q) fneq[q] = rn_sub(fi[q], feq_q_rn(q, rho, ux, uy, uz, usq));
-    ChildRecord<S>::write(rec, fneq, rho, ux, uy, uz);
+    ChildRecord<S>::write(rec, st, fneq, rho, ux, uy, uz);
 }
 
 } // namespace fcfd

@@ -844,7 +844,8 @@ collide_child_kernel(const typename S::T* __restrict__ src, typename S::T* __res
     for (int k = 0; k + kSplit < kQ; ++k) fi[k + kSplit] = __shfl_xor_sync(0xffffffffu, acc[k], 1);
     if (!record || !even) return;
     const long long t = lx + static_cast<long long>(cf.rw) * (ly + static_cast<long long>(cf.rh) * blockIdx.z);
-    write_child_record<S, !EXACT>(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t * ChildRecord<S>::kVec);
+    write_child_record<S, !EXACT>(fi, nFluid + nOdd, reinterpret_cast<float4*>(cf.scratch) + t,
+                                  static_cast<long long>(cf.rw) * cf.rh * (a.nz / 2));
 }
 
 template <class S, bool EXACT>

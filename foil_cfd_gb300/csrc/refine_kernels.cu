@@ -18,8 +18,8 @@
 // m tau_c / tau_f and blend into the coarse post-collision state over a
 // 3-cell edge ramp. The reference recomputes each neighbour's child average
 // inside the filter (19 averages per cell); here pass 1 stores every child
-// average once in scratch (one 96-byte record per coarse cell) and pass 2
-// filters from scratch.
+// average once in scratch (one 96-byte record per coarse cell, stored
+// planar: see child_record.cuh) and pass 2 filters from scratch.
 //
 // Built with --fmad=false: every expression keeps the reference's rounding,
 // so fill and restriction are bit-identical to the reference kernels
@@ -194,7 +194,8 @@ child_avg_kernel(const typename S::T* __restrict__ ff, const std::uint8_t* __res
 #pragma unroll
                 for (int q = 0; q < kQ; ++q) fi[q] += S::ld(ff + q * fn, c, wgt(q));
             }
-    write_child_record<S>(fi, nFluid, reinterpret_cast<float4*>(scratch) + t * ChildRecord<S>::kVec);
+    const long long nrec = static_cast<long long>(rw) * rh * g.coarse.nz;
+    write_child_record<S>(fi, nFluid, reinterpret_cast<float4*>(scratch) + t, nrec);
 }
 
 constexpr int kRestrictTX = 32, kRestrictTY = 2, kRestrictTZ = 2;
@@ -217,9 +218,9 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
                         * (static_cast<unsigned>(yc) + static_cast<unsigned>(g.coarse.ny) * zc);
     if ((ckind[cell] & kFlagMask) != kFluid) return;
     const float4* rec = reinterpret_cast<const float4*>(scratch);
-    constexpr int kRec = ChildRecord<S>::kVec;
+    const long long nrec = static_cast<long long>(rw) * rh * nz;
     float fneq[kQ];
-    if (!ChildRecord<S>::load(rec + t * kRec, fneq)) return;
+    if (!ChildRecord<S>::load(rec + t, nrec, fneq)) return;
 
     const int dEdge = min(min(lx, rw - 1 - lx), min(ly, rh - 1 - ly));
     const float blend = fminf(1.0f, static_cast<float>(dEdge + 1) / static_cast<float>(kRestrictBlend + 1));
@@ -232,13 +233,13 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
         const int nzw = wrapi(zc + cz(nb), nz);
         const long long tn = nlx + static_cast<long long>(rw) * (nly + static_cast<long long>(rh) * nzw);
         // Same per-q accumulation order as summing slot by slot.
-        nStencil += ChildRecord<S>::add_sel(rec + tn * kRec, fneq) ? 1 : 0;
+        nStencil += ChildRecord<S>::add_sel(rec + tn, nrec, fneq) ? 1 : 0;
     }
     const float invS = 1.0f / static_cast<float>(nStencil);
 #pragma unroll
     for (int q = 0; q < kQ; ++q) fneq[q] *= invS;
     regularize(fneq);
-    const float4 m4 = ChildRecord<S>::moments(rec + t * kRec);
+    const float4 m4 = ChildRecord<S>::moments(rec + t, nrec);
     const float rho = m4.x, ux = m4.y, uy = m4.z, uz = m4.w;
     const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
     float br = 0.f, bjx = 0.f, bjy = 0.f, bjz = 0.f;
