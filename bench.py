@@ -1117,6 +1117,10 @@ def main():
            "updates_per_step": t.updates_per_step(), "batch": BATCH,
            "counting": "coarse + 2 x fine lattice updates per coarse step",
            "l2": "populations (>10 GB) exceed the 129 MB L2; no flush needed",
+           "window": f"every timed run is at most {CHUNK} steps from the state {SETTLE} steps after the "
+                     "uniform-flow start (exact device restore between runs, outside the timed region): the "
+                     "as-specified tunnel trips the speed watchdog between 110 and 200 steps from the start, in "
+                     "the reference's own step as in this one (stability leg)",
            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 
     if args.impl == "reference":
