@@ -1088,6 +1088,7 @@ def main():
     ap.add_argument("--no-geometry", action="store_true", help="skip the host-vs-device geometry build leg")
     ap.add_argument("--only-geometry", action="store_true", help="run only the geometry build leg")
     ap.add_argument("--polar-steps", type=int, default=10000)
+    ap.add_argument("--polar-fp32-steps", type=int, default=2000)
     ap.add_argument("--precision", action="store_true",
                     help="add the FP32/FP16/FP64 precision study (cylinder, airfoil, Taylor-Green)")
     ap.add_argument("--only-precision", action="store_true", help="run only the precision study")
@@ -1165,7 +1166,7 @@ def main():
     if args.only_polar:
         if rank == 0:
             fixed = tuple(int(v) for v in args.polar_config.split(",")) if args.polar_config else None
-            print(json.dumps({"batched_polar": polar_leg(args.polar_steps, fixed=fixed)}))
+            print(json.dumps({"batched_polar": polar_leg(args.polar_steps, args.polar_fp32_steps, fixed=fixed)}))
         return
 
     clocks = Clocks() if rank == 0 else None

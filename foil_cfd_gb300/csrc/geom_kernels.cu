@@ -265,6 +265,30 @@ struct FlagEqPred {     // flag == value (interface-shell list)
     }
 };
 
+// Interface cells a step reads: the shell cells with a fluid or outlet cell
+// among their 18 neighbours (wrapped). The stream-collide reaches no
+// further than one cell, so the rest of a 2-cell shell is read by nothing.
+struct ShellPulledPred {
+    Grid3 g;
+    const std::uint8_t* f;
+    std::uint32_t* cells;
+    __device__ std::uint32_t eval(long long c, int x, int y, int z, int*) const {
+        if (f[c] != kInterfaceB) return 0;
+#pragma unroll
+        for (int q = 1; q < kQ; ++q) {
+            const int X = wrapi(x + cx(q), g.nx), Y = wrapi(y + cy(q), g.ny), Z = wrapi(z + cz(q), g.nz);
+            const std::uint8_t nf = f[static_cast<unsigned>(X)
+                                      + static_cast<unsigned>(g.nx) * (static_cast<unsigned>(Y)
+                                                                       + static_cast<unsigned>(g.ny) * Z)];
+            if (nf == kFluidB || nf == kOutletB || nf == kOutletEqB) return 1u;
+        }
+        return 0u;
+    }
+    __device__ void emit(long long slot, long long c, int, int, int, std::uint32_t) const {
+        cells[slot] = static_cast<std::uint32_t>(c);
+    }
+};
+
 struct FlagNePred {     // flag != value (non-solid seed list)
     const std::uint8_t* f;
     std::uint8_t value;
@@ -711,6 +735,12 @@ cudaError_t device_cells_where(LevelDims d, const std::uint8_t* flags, std::uint
                                std::uint32_t* cells, long long cap, long long* count, cudaStream_t st) {
     if (equal) return compact_into(FlagEqPred{flags, value, cells}, {d.nx, d.ny, d.nz}, cap, count, nullptr, st);
     return compact_into(FlagNePred{flags, value, cells}, {d.nx, d.ny, d.nz}, cap, count, nullptr, st);
+}
+
+cudaError_t device_shell_pulled(LevelDims d, const std::uint8_t* flags, std::uint32_t* cells, long long cap,
+                                long long* count, cudaStream_t st) {
+    return compact_into(ShellPulledPred{{d.nx, d.ny, d.nz}, flags, cells}, {d.nx, d.ny, d.nz}, cap, count, nullptr,
+                        st);
 }
 
 cudaError_t device_wall_list(LevelDims d, const std::uint8_t* active, const std::uint8_t* clean, int sampleCells,

@@ -253,6 +253,10 @@ cudaError_t device_force_links(LevelDims d, const std::uint8_t* flags, std::uint
                                long long cap, long long* count, cudaStream_t st);
 cudaError_t device_cells_where(LevelDims d, const std::uint8_t* flags, std::uint8_t value, bool equal,
                                std::uint32_t* cells, long long cap, long long* count, cudaStream_t st);
+/// Interface cells with a fluid or outlet cell among their 18 neighbours
+/// (the shell cells a stream-collide reads), ascending; as device_cells_where.
+cudaError_t device_shell_pulled(LevelDims d, const std::uint8_t* flags, std::uint32_t* cells, long long cap,
+                                long long* count, cudaStream_t st);
 cudaError_t device_wall_list(LevelDims d, const std::uint8_t* active, const std::uint8_t* clean, int sampleCells,
                              const WallListOut& out, long long cap, long long* count, int stats[3],
                              cudaStream_t st);

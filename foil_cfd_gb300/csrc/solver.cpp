@@ -236,6 +236,9 @@ struct fcfd_solver {
     float* dScratchFiner = nullptr;
     std::uint32_t* dShell = nullptr;
     int shellCount = 0;
+    // The fine level's fill covers every interface cell while a finer box
+    // reaches its outer shell layer (the finer fill gathers from there).
+    bool fineShellFull = false;
     std::uint32_t* dSeed = nullptr;
     int seedCount = 0;
     float* dScratch = nullptr;
@@ -401,6 +404,30 @@ struct fcfd_solver {
         return cudaStreamSynchronize(stream);
     }
 
+    /// Fill targets of a refined level: the interface cells its stream-collide
+    /// reads (a fluid or outlet cell among their 18 neighbours). The
+    /// reference fills every interface cell, but the collide reaches one
+    /// cell, so the outer layer of the 2-cell shell is read by no step and
+    /// every population a step computes is the same. With `full` (the fine
+    /// level while a finer level nests in it, whose fill may gather from
+    /// the fine shell) every interface cell.
+    cudaError_t shellList(const Level& L, bool full, std::uint32_t** out, int* count) {
+        if (full) return cellList(L, FCFD_FLAG_INTERFACE, true, out, count);
+        dfree(*out);
+        *count = 0;
+        long long c = 0;
+        launches += 2;
+        if (auto e = device_shell_pulled(L.d, L.flags, nullptr, 0, &c, stream); e != cudaSuccess) return e;
+        if (auto e = dalloc(out, static_cast<size_t>(c) * 4); e != cudaSuccess) return e;
+        if (c > 0) {
+            launches += 3;
+            long long again = 0;
+            if (auto e = device_shell_pulled(L.d, L.flags, *out, c, &again, stream); e != cudaSuccess) return e;
+        }
+        *count = static_cast<int>(c);
+        return cudaSuccess;
+    }
+
     /// Ascending list of the level's cells whose flag equals (or, with
     /// equal false, differs from) `value`, into a fresh device array.
     cudaError_t cellList(const Level& L, std::uint8_t value, bool equal, std::uint32_t** out, int* count) {
@@ -553,6 +580,7 @@ struct fcfd_solver {
         fine.free_all();
         dfree(dShell); dfree(dSeed); dfree(dScratch);
         shellCount = seedCount = 0;
+        fineShellFull = false;
         fineActive = false;
         forcesFromFine = false;
     }
@@ -1562,7 +1590,7 @@ int fcfd_init_refinement(fcfd_solver* s, const fcfd_patch_box* box, int factor, 
     };
     if (auto e = s->allocLevel(s->fine, fd); e != cudaSuccess) return fail("fine buffer allocation failed", e);
     if (auto e = s->uploadLevelFlags(s->fine, ff); e != cudaSuccess) return fail("fine flag upload failed", e);
-    if (auto e = s->cellList(s->fine, FCFD_FLAG_INTERFACE, true, &s->dShell, &s->shellCount); e != cudaSuccess)
+    if (auto e = s->shellList(s->fine, false, &s->dShell, &s->shellCount); e != cudaSuccess)
         return fail("shell list failed", e);
     if (auto e = s->cellList(s->fine, FCFD_FLAG_SOLID, false, &s->dSeed, &s->seedCount); e != cudaSuccess)
         return fail("seed list failed", e);
@@ -1589,8 +1617,7 @@ int fcfd_set_refined_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {
     if (!s || !s->initialized || !s->fineActive || !ff || n != static_cast<size_t>(s->fine.n))
         return cudaErrorInvalidValue;
     if (auto e = s->uploadLevelFlags(s->fine, ff); e != cudaSuccess) return e;
-    if (auto e = s->cellList(s->fine, FCFD_FLAG_INTERFACE, true, &s->dShell, &s->shellCount); e != cudaSuccess)
-        return e;
+    if (auto e = s->shellList(s->fine, s->fineShellFull, &s->dShell, &s->shellCount); e != cudaSuccess) return e;
     if (auto e = s->cellList(s->fine, FCFD_FLAG_SOLID, false, &s->dSeed, &s->seedCount); e != cudaSuccess) return e;
     s->updateForcesFromFine();
     if (auto e = s->buildWM(s->fine, kWallSampleFine); e != cudaSuccess) return e;
@@ -1874,9 +1901,7 @@ int fcfd_q_link_info(fcfd_solver* s, int level, int* active, int* links, int* fa
 
 /// Interface-shell and seed lists of the finer level (its flags uploaded).
 static int finer_lists(fcfd_solver* s) {
-    if (auto e = s->cellList(s->finer, FCFD_FLAG_INTERFACE, true, &s->dShellFiner, &s->shellCountFiner);
-        e != cudaSuccess)
-        return e;
+    if (auto e = s->shellList(s->finer, false, &s->dShellFiner, &s->shellCountFiner); e != cudaSuccess) return e;
     return s->cellList(s->finer, FCFD_FLAG_SOLID, false, &s->dSeedFiner, &s->seedCountFiner);
 }
 
@@ -1928,6 +1953,13 @@ int fcfd_init_finer_refinement(fcfd_solver* s, const fcfd_patch_box* box, int fa
     if (auto e = static_cast<cudaError_t>(finer_lists(s)); e != cudaSuccess)
         return fail("finer target lists failed", e);
     s->finerActive = true;
+    // A finer box within one cell of the fine level's edge interpolates from
+    // the fine shell's outer layer: fill every fine interface cell from now on.
+    if (box->x0 < 2 || box->y0 < 2 || box->x1 > pd.nx - 2 || box->y1 > pd.ny - 2) {
+        s->fineShellFull = true;
+        if (auto e = s->shellList(s->fine, true, &s->dShell, &s->shellCount); e != cudaSuccess)
+            return fail("shell list failed", e);
+    }
     const long long sf = restrict_scratch_floats(s->geomFiner());
     if (sf <= 0) return fail("finer restriction sub-box is empty", cudaErrorInvalidValue);
     if (auto e = dalloc(&s->dScratchFiner, static_cast<size_t>(sf) * 4); e != cudaSuccess)
@@ -1943,6 +1975,10 @@ void fcfd_shutdown_finer_refinement(fcfd_solver* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     s->freeFiner();
+    if (s->fineShellFull && s->fineActive) {
+        s->fineShellFull = false;
+        s->shellList(s->fine, false, &s->dShell, &s->shellCount);
+    }
 }
 
 int fcfd_set_refined_finer_flags(fcfd_solver* s, const uint8_t* ff, size_t n) {

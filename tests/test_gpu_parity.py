@@ -582,12 +582,15 @@ def _three_level_case(fc, oracle_mod):
     return cd, cf.ravel(), box, ff, rbox, rf, f0
 
 
-def test_three_level_step_vs_oracle(fc, oracle_mod):
+@pytest.mark.parametrize("rbox", [(20, 10, 44, 30), (1, 10, 25, 30)])
+def test_three_level_step_vs_oracle(fc, oracle_mod, rbox):
     """Nested finer level (initFinerRefinement, lbm_solver.cpp:1209-1270):
     each fine sub-step runs two finer sub-steps and a finer -> fine
     restriction; 20 coarse steps against the oracle's replay, bit for bit on
-    all three levels."""
-    cd, cflags, box, ff, rbox, rf, f0 = _three_level_case(fc, oracle_mod)
+    all three levels. The second box starts one fine cell from the patch
+    edge, so the finer fill gathers from the outer layer of the fine shell,
+    which the fine fill then covers too."""
+    cd, cflags, box, ff, _rbox, rf, f0 = _three_level_case(fc, oracle_mod)
     tauC = 0.55
     s = make(fc, cd, cflags, tauC, 0.05)
     s.import_f32(f0)
