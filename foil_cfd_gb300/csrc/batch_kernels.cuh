@@ -47,6 +47,7 @@ batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, un
         a.uwx = a.uwy = a.uwz = nullptr;
         a.status = nullptr;
         a.qFrac = nullptr;
+        a.links = nullptr;
         a.ffMask = nullptr;
         const T* src = static_cast<const T*>(tp.f[parity]);
         T* dst = static_cast<T*>(tp.f[parity ^ 1]);

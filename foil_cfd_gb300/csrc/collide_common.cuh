@@ -52,6 +52,7 @@ struct CollideArgs {
     int* status; // staged kernel: nonzero when a pipeline wait timed out
     const std::uint8_t* qFrac;   // q-LIBB cut bytes [cell * 19 + q], or null
     const std::uint32_t* ffMask; // q-LIBB two-node bits [cell]
+    const uint2* links;          // pull-link classes per cell (launch_classify), or null
 };
 
 /// Byte offsets of the pulls of an interior cell (no periodic wrap on any
@@ -430,15 +431,29 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
     float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
     bool uwLoaded = false;
     using P = Pop<S, DEV>;
+    // The links' classes: one 8-byte word per cell when the level has them,
+    // else the 18 neighbours' flags.
+    unsigned long long lm = 0;
+    if (a.links) {
+        const uint2 w = __ldg(a.links + cell);
+        lm = static_cast<unsigned long long>(w.x) | (static_cast<unsigned long long>(w.y) << 32);
+    }
     f[0] = P::ld(src, cell, wgt(0));
 #pragma unroll
     for (int q = 1; q < kQ; ++q) {
         const unsigned X = b.sx[1 + cx(q)], Y = b.sy[1 + cy(q)], Z = b.sz[1 + cz(q)];
         const unsigned pn = X + unx * (Y + uny * Z);
-        const int nf = kind[pn] & kFlagMask;
-        const bool solid = nf == kSolid;
-        const bool slipY = is_slip_y(nf);
-        const bool slipZ = is_slip_z(nf);
+        bool solid, slipY, slipZ;
+        if (a.links) {
+            solid = (lm >> (q - 1)) & 1ull;
+            slipY = (lm >> (17 + q)) & 1ull;
+            slipZ = (lm >> (35 + q)) & 1ull;
+        } else {
+            const int nf = kind[pn] & kFlagMask;
+            solid = nf == kSolid;
+            slipY = is_slip_y(nf);
+            slipZ = is_slip_z(nf);
+        }
         const unsigned pY = X + unx * (static_cast<unsigned>(y) + uny * Z);
         const unsigned pZ = X + unx * (Y + uny * static_cast<unsigned>(z));
         const int qs = solid ? opp(q) : (slipY ? mir_y(q) : (slipZ ? mir_z(q) : q));
@@ -479,6 +494,51 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
     }
 }
 
+/// Near-wall interior cell whose wall links are all solid (bit q - 1 of
+/// `solidMask`): the pulls of gather_wall through the constant offsets --
+/// the own cell's opposite slot on a solid link, the upstream cell
+/// otherwise -- with the same interpolated bounce-back and Ladd terms.
+template <class S, bool WM, bool QL, bool DEV>
+__device__ __forceinline__ void gather_solid_links(const typename S::T* __restrict__ src, const CollideArgs& a,
+                                                   const PullOffsets& o, unsigned cell, int x, int y, int z,
+                                                   unsigned solidMask, float (&f)[kQ]) {
+    using P = Pop<S, DEV>;
+    const typename S::T* base = src + cell;
+    float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
+    if constexpr (WM) {
+        uwx = __half2float(__ushort_as_half(a.uwx[cell]));
+        uwy = __half2float(__ushort_as_half(a.uwy[cell]));
+        uwz = __half2float(__ushort_as_half(a.uwz[cell]));
+    }
+    f[0] = P::ld(base, 0, wgt(0));
+#pragma unroll
+    for (int q = 1; q < kQ; ++q) {
+        const bool solid = (solidMask >> (q - 1)) & 1u;
+        float fq = P::ld(byte_add(base, solid ? o.slice[opp(q)] : o.pull[q]), 0, wgt(q));
+        if (QL && solid) {
+            const std::uint8_t qb = a.qFrac[static_cast<long long>(cell) * kQ + q];
+            if (qb != 0) {
+                const float qf = static_cast<float>(qb) * (1.0f / 255.0f);
+                const float fOut = P::ld(byte_add(base, o.slice[q]), 0, wgt(q));
+                if (qf >= 0.5f) {
+                    const float inv2q = 0.5f / qf;
+                    fq = inv2q * fOut + (1.0f - inv2q) * fq;
+                } else if (a.ffMask[cell] & (1u << q)) {
+                    const unsigned unx = a.nx, uny = a.ny;
+                    const Nbr b = neighbours(x, y, z, a.nx, a.ny, a.nz);
+                    const unsigned pff = b.sx[1 - cx(q)] + unx * (b.sy[1 - cy(q)] + uny * b.sz[1 - cz(q)]);
+                    const float fOutFF = P::ld(src + static_cast<long long>(q) * a.n, pff, wgt(q));
+                    fq = 2.0f * qf * fOut + (1.0f - 2.0f * qf) * fOutFF;
+                }
+            }
+        }
+        if constexpr (WM) {
+            if (solid) fq += (6.0f * wgt(q)) * dot_c(q, uwx, uwy, uwz);
+        }
+        f[q] = fq;
+    }
+}
+
 template <class S, bool EXACT>
 __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, const CollideArgs& a, unsigned cell,
                                             float (&f)[kQ], const PullOffsets* o = nullptr) {
@@ -499,9 +559,21 @@ __device__ __forceinline__ void gather_fluid(const typename S::T* __restrict__ s
     if (!(k & kNearWall)) {
         if (o && interior(x, y, z, a)) gather_interior<S, DEV>(src, *o, cell, f);
         else gather_bulk<S, DEV>(src, a, neighbours(x, y, z, a.nx, a.ny, a.nz), f);
-    } else {
-        gather_wall<S, WM, QL, DEV>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
+        return;
     }
+    // Near-wall cell. With the link classes at hand, an interior cell whose
+    // only wall links are solid ones (the cells along a foil) pulls through
+    // the constant offsets, a select per link choosing its own opposite slot
+    // over the upstream one; slip links and the periodic faces take the
+    // general path.
+    if (a.links && o && interior(x, y, z, a)) {
+        const uint2 w = __ldg(a.links + cell);
+        if (w.y == 0 && (w.x >> 18) == 0) {   // no slip-wall bit (bits 18-53 of the word)
+            gather_solid_links<S, WM, QL, DEV>(src, a, *o, cell, x, y, z, w.x, f);
+            return;
+        }
+    }
+    gather_wall<S, WM, QL, DEV>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
 }
 
 /// One full cell update at (x, y, z): boundary cells by flag, fluid cells
@@ -862,6 +934,7 @@ cudaError_t launch_collide_child_impl(const void* srcv, void* dstv, const std::u
     a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
     a.status = nullptr;
     a.qFrac = p.qFrac; a.ffMask = p.ffMask;
+    a.links = p.links;
     const dim3 block(kFuseX);
     const dim3 grid(static_cast<unsigned>((d.nx + kFuseX - 1) / kFuseX), static_cast<unsigned>(d.ny / 2),
                     static_cast<unsigned>(d.nz / 2));
@@ -1121,6 +1194,7 @@ cudaError_t launch_collide_impl(const void* srcv, void* dstv, const std::uint8_t
     a.uwx = slip.uwx; a.uwy = slip.uwy; a.uwz = slip.uwz;
     a.status = p.status;
     a.qFrac = p.qFrac; a.ffMask = p.ffMask;
+    a.links = p.links;
     const T* src = static_cast<const T*>(srcv);
     T* dst = static_cast<T*>(dstv);
     const bool wm = slip.active();

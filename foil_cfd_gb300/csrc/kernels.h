@@ -39,6 +39,9 @@ struct CollideParams {
     /// cut bytes [cell * 19 + q] (q = byte / 255) and two-node bits [cell].
     const std::uint8_t* qFrac = nullptr;
     const std::uint32_t* ffMask = nullptr;
+    /// Link classes of each fluid cell's pull neighbours (launch_classify),
+    /// or null: the near-wall gather then reads the neighbours' flags.
+    const uint2* links = nullptr;
 };
 
 /// Half-bit slip field of a level (WallSlipView, lbm_core.cuh:201-208).
@@ -52,8 +55,12 @@ struct SlipField {
 enum class Storage : int { F32 = 0, F16 = 1 };
 
 // ---- step kernels (step_kernels.cu) ---------------------------------------
+/// Kind bytes, and (links not null) per fluid cell the classes of its 18
+/// pull links x - c_q as one 64-bit word (low half in .x): bit q - 1 solid,
+/// bit 17 + q free-slip y wall, bit 35 + q free-slip z wall; 0 for cells
+/// that are not fluid.
 cudaError_t launch_classify(const std::uint8_t* flags, std::uint8_t* kind,
-                            LevelDims d, cudaStream_t st);
+                            LevelDims d, cudaStream_t st, uint2* links = nullptr);
 cudaError_t launch_collide(Storage s, const void* src, void* dst,
                            const std::uint8_t* kind, LevelDims d,
                            const CollideParams& p, float* rho, float* u,

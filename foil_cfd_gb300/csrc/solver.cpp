@@ -104,6 +104,7 @@ struct Level {
     void* f[2] = {nullptr, nullptr};
     std::uint8_t* flags = nullptr;
     std::uint8_t* kind = nullptr;
+    uint2* links = nullptr;   // pull-link classes of the fluid cells (8 B per cell)
     int src = 0;
     std::vector<std::uint8_t> hostFlags, surfaceRef;
     std::uint32_t *dLinkCells = nullptr, *dLinkMasks = nullptr;
@@ -127,7 +128,7 @@ struct Level {
     }
 
     void free_all() {
-        dfree(f[0]); dfree(f[1]); dfree(flags); dfree(kind);
+        dfree(f[0]); dfree(f[1]); dfree(flags); dfree(kind); dfree(links);
         dfree(dLinkCells); dfree(dLinkMasks); dfree(dPartials);
         dfree(dQFrac); dfree(dFFMask);
         qLinks = qFallback = 0;
@@ -356,6 +357,7 @@ struct fcfd_solver {
         // Kind bytes are fetched in 16-byte-aligned row copies that may run
         // up to 31 bytes past the last row: pad the allocation.
         if (auto e = dalloc(&L.kind, static_cast<size_t>(L.n) + 64); e != cudaSuccess) return e;
+        if (auto e = dalloc(&L.links, static_cast<size_t>(L.n) * sizeof(uint2)); e != cudaSuccess) return e;
         return cudaSuccess;
     }
 
@@ -382,7 +384,7 @@ struct fcfd_solver {
         if (auto e = device_flag_classes(L.d, L.flags, stream, cls); e != cudaSuccess) return e;
         L.nReadWrite = cls[0]; L.nInlet = cls[1]; L.nUntouched = cls[2];
         ++launches;
-        if (auto e = launch_classify(L.flags, L.kind, L.d, stream); e != cudaSuccess) return e;
+        if (auto e = launch_classify(L.flags, L.kind, L.d, stream, L.links); e != cudaSuccess) return e;
         // Compact force-link list of this level (ascending cell order).
         dfree(L.dLinkCells); dfree(L.dLinkMasks); dfree(L.dPartials);
         long long links = 0;
@@ -693,6 +695,7 @@ struct fcfd_solver {
         CollideParams lp = p;
         lp.qFrac = L.dQFrac;
         lp.ffMask = L.dFFMask;
+        lp.links = L.links;
         cudaError_t e;
         if (aa) {
             e = launch_collide_aa(storage, L.f[0], L.d, lp, aaNextOdd, r, uu, vv, ww, stream);
@@ -724,6 +727,7 @@ struct fcfd_solver {
         CollideParams lp = p;
         lp.qFrac = L.dQFrac;
         lp.ffMask = L.dFFMask;
+        lp.links = L.links;
         const cudaError_t e = launch_collide_child(storage, L.f[L.src], L.f[1 - L.src], L.kind, L.d, lp,
                                                    L.wm.slip(), cf, stream);
         if (e2) cudaEventRecord(e2, stream);

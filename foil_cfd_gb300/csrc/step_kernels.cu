@@ -15,17 +15,19 @@ namespace {
 
 constexpr int kBlock1D = 256;
 
-/// kind = flag | kNearWall for fluid cells with a solid/slip pull neighbour.
+/// kind = flag | kNearWall for fluid cells with a solid/slip pull neighbour;
+/// links (when given): the classes of the 18 pull links (kernels.h).
 __global__ void classify_kernel(const std::uint8_t* __restrict__ flags,
-                                std::uint8_t* __restrict__ kind, int nx, int ny, int nz) {
+                                std::uint8_t* __restrict__ kind, int nx, int ny, int nz,
+                                uint2* __restrict__ links) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= nx) return;
     const int y = blockIdx.y, z = blockIdx.z;
     const long long cell = x + static_cast<long long>(nx) * (y + static_cast<long long>(ny) * z);
     const std::uint8_t fl = flags[cell] & kFlagMask;
     std::uint8_t out = fl;
+    unsigned long long m = 0;
     if (fl == kFluid) {
-        bool near = false;
 #pragma unroll
         for (int q = 1; q < kQ; ++q) {
             int xs = x - cx(q), ys = y - cy(q), zs = z - cz(q);
@@ -33,11 +35,14 @@ __global__ void classify_kernel(const std::uint8_t* __restrict__ flags,
             ys = ys < 0 ? ys + ny : (ys >= ny ? ys - ny : ys);
             zs = zs < 0 ? zs + nz : (zs >= nz ? zs - nz : zs);
             const int nf = flags[xs + static_cast<long long>(nx) * (ys + static_cast<long long>(ny) * zs)] & kFlagMask;
-            near |= (nf == kSolid) || is_slip_y(nf) || is_slip_z(nf);
+            if (nf == kSolid) m |= 1ull << (q - 1);
+            if (is_slip_y(nf)) m |= 1ull << (17 + q);
+            if (is_slip_z(nf)) m |= 1ull << (35 + q);
         }
-        if (near) out |= kNearWall;
+        if (m != 0) out |= kNearWall;
     }
     kind[cell] = out;
+    if (links) links[cell] = make_uint2(static_cast<unsigned>(m), static_cast<unsigned>(m >> 32));
 }
 
 template <class S>
@@ -179,9 +184,9 @@ inline dim3 plane_grid(const LevelDims& d, int bx) {
 } // namespace
 
 cudaError_t launch_classify(const std::uint8_t* flags, std::uint8_t* kind, LevelDims d,
-                            cudaStream_t st) {
+                            cudaStream_t st, uint2* links) {
     if (!flags || !kind || d.cells() <= 0) return cudaErrorInvalidValue;
-    classify_kernel<<<plane_grid(d, 128), 128, 0, st>>>(flags, kind, d.nx, d.ny, d.nz);
+    classify_kernel<<<plane_grid(d, 128), 128, 0, st>>>(flags, kind, d.nx, d.ny, d.nz, links);
     return cudaGetLastError();
 }
 
