@@ -64,6 +64,11 @@ struct CollideArgs {
 struct PullOffsets {
     long long pull[kQ];
     long long slice[kQ];
+    /// Free-slip pulls of a near-wall interior cell: the mirrored slot of the
+    /// tangentially displaced cell, (x - c_x, y, z - c_z) for a y wall and
+    /// (x - c_x, y - c_y, z) for a z wall.
+    long long slipY[kQ];
+    long long slipZ[kQ];
 };
 
 template <class T>
@@ -73,6 +78,8 @@ __host__ PullOffsets pull_offsets(int nx, int ny, long long n) {
     for (int q = 0; q < kQ; ++q) {
         o.slice[q] = q * n * static_cast<long long>(sizeof(T));
         o.pull[q] = (q * n - (cx(q) + sx * cy(q) + sxy * cz(q))) * static_cast<long long>(sizeof(T));
+        o.slipY[q] = (mir_y(q) * n - (cx(q) + sxy * cz(q))) * static_cast<long long>(sizeof(T));
+        o.slipZ[q] = (mir_z(q) * n - (cx(q) + sx * cy(q))) * static_cast<long long>(sizeof(T));
     }
     return o;
 }
@@ -494,14 +501,17 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
     }
 }
 
-/// Near-wall interior cell whose wall links are all solid (bit q - 1 of
-/// `solidMask`): the pulls of gather_wall through the constant offsets --
-/// the own cell's opposite slot on a solid link, the upstream cell
-/// otherwise -- with the same interpolated bounce-back and Ladd terms.
-template <class S, bool WM, bool QL, bool DEV>
-__device__ __forceinline__ void gather_solid_links(const typename S::T* __restrict__ src, const CollideArgs& a,
-                                                   const PullOffsets& o, unsigned cell, int x, int y, int z,
-                                                   unsigned solidMask, float (&f)[kQ]) {
+/// Near-wall interior cell (link classes lm, the 64-bit word of
+/// launch_classify): the pulls of gather_wall through the constant offsets
+/// -- the own cell's opposite slot on a solid link, the mirrored slot of the
+/// tangentially displaced cell on a slip link (SLIP: the cell has one), the
+/// upstream cell otherwise -- with the same interpolated bounce-back and
+/// Ladd terms.
+template <class S, bool WM, bool QL, bool DEV, bool SLIP>
+__device__ __forceinline__ void gather_links(const typename S::T* __restrict__ src, const CollideArgs& a,
+                                             const PullOffsets& o, unsigned cell, int x, int y, int z,
+                                             unsigned long long lm, float (&f)[kQ]) {
+    const unsigned solidMask = static_cast<unsigned>(lm) & 0x3FFFFu;
     using P = Pop<S, DEV>;
     const typename S::T* base = src + cell;
     float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
@@ -514,7 +524,13 @@ __device__ __forceinline__ void gather_solid_links(const typename S::T* __restri
 #pragma unroll
     for (int q = 1; q < kQ; ++q) {
         const bool solid = (solidMask >> (q - 1)) & 1u;
-        float fq = P::ld(byte_add(base, solid ? o.slice[opp(q)] : o.pull[q]), 0, wgt(q));
+        long long off = o.pull[q];
+        if constexpr (SLIP) {
+            if ((lm >> (35 + q)) & 1ull) off = o.slipZ[q];
+            if ((lm >> (17 + q)) & 1ull) off = o.slipY[q];
+        }
+        if (solid) off = o.slice[opp(q)];
+        float fq = P::ld(byte_add(base, off), 0, wgt(q));
         if (QL && solid) {
             const std::uint8_t qb = a.qFrac[static_cast<long long>(cell) * kQ + q];
             if (qb != 0) {
@@ -561,17 +577,17 @@ __device__ __forceinline__ void gather_fluid(const typename S::T* __restrict__ s
         else gather_bulk<S, DEV>(src, a, neighbours(x, y, z, a.nx, a.ny, a.nz), f);
         return;
     }
-    // Near-wall cell. With the link classes at hand, an interior cell whose
-    // only wall links are solid ones (the cells along a foil) pulls through
-    // the constant offsets, a select per link choosing its own opposite slot
-    // over the upstream one; slip links and the periodic faces take the
-    // general path.
+    // Near-wall cell. With the link classes at hand, an interior cell pulls
+    // through the constant offsets, a select per link among the upstream
+    // cell, its own opposite slot (solid) and the mirrored slot of the
+    // displaced cell (slip); cells on the periodic faces take the general
+    // path.
     if (a.links && o && interior(x, y, z, a)) {
         const uint2 w = __ldg(a.links + cell);
-        if (w.y == 0 && (w.x >> 18) == 0) {   // no slip-wall bit (bits 18-53 of the word)
-            gather_solid_links<S, WM, QL, DEV>(src, a, *o, cell, x, y, z, w.x, f);
-            return;
-        }
+        const unsigned long long lm = static_cast<unsigned long long>(w.x) | (static_cast<unsigned long long>(w.y) << 32);
+        if ((lm >> 18) == 0) gather_links<S, WM, QL, DEV, false>(src, a, *o, cell, x, y, z, lm, f);
+        else gather_links<S, WM, QL, DEV, true>(src, a, *o, cell, x, y, z, lm, f);
+        return;
     }
     gather_wall<S, WM, QL, DEV>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
 }
