@@ -36,6 +36,7 @@ struct Tunnel {
     void* f[2] = {nullptr, nullptr};
     std::uint8_t* flags = nullptr;
     std::uint8_t* kind = nullptr;
+    uint2* links = nullptr;   // pull-link classes of the fluid cells
     std::uint32_t* linkCells = nullptr;
     std::uint32_t* linkMasks = nullptr;
     int linkCount = 0;
@@ -89,7 +90,7 @@ struct fcfd_batch {
         if (stream) cudaStreamSynchronize(stream);
         dropGraphs();
         for (Tunnel& x : t) {
-            cudaFree(x.f[0]); cudaFree(x.f[1]); cudaFree(x.flags); cudaFree(x.kind);
+            cudaFree(x.f[0]); cudaFree(x.f[1]); cudaFree(x.flags); cudaFree(x.kind); cudaFree(x.links);
             cudaFree(x.linkCells); cudaFree(x.linkMasks);
         }
         t.clear();
@@ -137,6 +138,7 @@ struct fcfd_batch {
             BatchTunnelParam& d = table.t[i];
             d.f[0] = x.f[0]; d.f[1] = x.f[1];
             d.kind = x.kind;
+            d.links = x.links;
             d.n = x.n;
             d.nx = x.d.nx; d.ny = x.d.ny; d.nz = x.d.nz;
             d.xChunks = 1;  // a work item spans whole rows
@@ -361,12 +363,14 @@ int fcfd_batch_init(fcfd_batch* b, const fcfd_batch_tunnel* tunnels, int count, 
         for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMalloc(&y.f[k], static_cast<size_t>(y.n) * 19 * esz);
         if (e == cudaSuccess) e = cudaMalloc(&y.flags, static_cast<size_t>(y.n));
         if (e == cudaSuccess) e = cudaMalloc(&y.kind, static_cast<size_t>(y.n) + 64);
+        if (e == cudaSuccess && b->storage == Storage::F32)   // the FP16 batch step does not read them
+            e = cudaMalloc(&y.links, static_cast<size_t>(y.n) * sizeof(uint2));
         // Flags from host or device memory (a polar built on the device);
         // the link list is compacted on the device either way.
         if (e == cudaSuccess)
             e = cudaMemcpy(y.flags, in.flags, static_cast<size_t>(y.n),
                            is_device_pointer(in.flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = launch_classify(y.flags, y.kind, y.d, b->stream);
+        if (e == cudaSuccess) e = launch_classify(y.flags, y.kind, y.d, b->stream, y.links);
         long long links = 0, again = 0;
         if (e == cudaSuccess) e = device_force_links(y.d, y.flags, nullptr, nullptr, 0, &links, b->stream);
         y.linkCount = static_cast<int>(links);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector_types.h>
 
 namespace fcfd {
 
@@ -11,6 +12,7 @@ constexpr int kMaxBatchTunnels = 64;
 struct BatchTunnelParam {
     void* f[2];                  ///< A/B population buffers
     const std::uint8_t* kind;    ///< kind bytes (flag | near-wall bit)
+    const uint2* links;          ///< pull-link classes per cell (launch_classify)
     long long n;                 ///< cells
     int nx, ny, nz;
     int xChunks;                 ///< x pieces of a work item (1: whole rows)
