@@ -114,11 +114,12 @@ template <> struct ChildRecord<StoreF32> {
     /// As add, but every part of the record is read before the valid flag
     /// decides (a select keeps acc when the record is invalid), so the loads
     /// of successive neighbours do not wait on each other's flags.
-    __device__ __forceinline__ static bool add_sel(const float4* rec, long long st, float (&acc)[kQ]) {
+    __device__ __forceinline__ static bool add_sel(const float4* rec, long long st, float (&acc)[kQ],
+                                                   bool use = true) {
         float4 a[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) a[k] = __ldg(rec + k * st);
-        const bool ok = a[4].w != 0.0f;
+        const bool ok = use && a[4].w != 0.0f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             acc[4 * k] = ok ? acc[4 * k] + a[k].x : acc[4 * k];
@@ -191,11 +192,12 @@ template <> struct ChildRecord<StoreF16> {
         return true;
     }
     __device__ __forceinline__ static float4 moments(const float4* rec, long long st) { return __ldg(rec + 3 * st); }
-    __device__ __forceinline__ static bool add_sel(const float4* rec, long long st, float (&acc)[kQ]) {
+    __device__ __forceinline__ static bool add_sel(const float4* rec, long long st, float (&acc)[kQ],
+                                                   bool use = true) {
         uint4 c[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) c[k] = __ldg(reinterpret_cast<const uint4*>(rec) + k * st);
-        const bool ok = __uint_as_float(c[2].z) != 0.0f;
+        const bool ok = use && __uint_as_float(c[2].z) != 0.0f;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const unsigned w[4] = {c[k].x, c[k].y, c[k].z, c[k].w};

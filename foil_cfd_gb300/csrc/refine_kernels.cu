@@ -229,11 +229,13 @@ restrict_kernel(typename S::T* __restrict__ fc, const std::uint8_t* __restrict__
 #pragma unroll
     for (int nb = 1; nb < kQ; ++nb) {
         const int nlx = lx + cx(nb), nly = ly + cy(nb);
-        if (nlx < 0 || nlx >= rw || nly < 0 || nly >= rh) continue;
-        const int nzw = wrapi(zc + cz(nb), nz);
-        const long long tn = nlx + static_cast<long long>(rw) * (nly + static_cast<long long>(rh) * nzw);
+        // A neighbour outside the box reads the cell's own record and is
+        // dropped by the select, so no neighbour's loads wait on a branch.
+        const bool inBox = nlx >= 0 && nlx < rw && nly >= 0 && nly < rh;
+        const int nzw = zc + cz(nb) < 0 ? nz - 1 : (zc + cz(nb) >= nz ? 0 : zc + cz(nb));
+        const long long tn = inBox ? nlx + static_cast<long long>(rw) * (nly + static_cast<long long>(rh) * nzw) : t;
         // Same per-q accumulation order as summing slot by slot.
-        nStencil += ChildRecord<S>::add_sel(rec + tn, nrec, fneq) ? 1 : 0;
+        nStencil += ChildRecord<S>::add_sel(rec + tn, nrec, fneq, inBox) ? 1 : 0;
     }
     const float invS = 1.0f / static_cast<float>(nStencil);
 #pragma unroll
