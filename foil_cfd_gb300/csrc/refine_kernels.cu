@@ -40,10 +40,9 @@ constexpr int kRefineBlock = 128;
 constexpr int kRestrictBand = 2;   // coarse band skipped by the restriction
 constexpr int kRestrictBlend = 3;  // edge-blend ramp width (coarse cells)
 
-__device__ __forceinline__ int wrapi(int v, int n) {
-    v %= n;
-    return v < 0 ? v + n : v;
-}
+/// v folded into [0, n) for v in [-n, 2n): the fill's corners lie at most one
+/// cell outside the coarse domain, so a compare replaces the division.
+__device__ __forceinline__ int wrap1(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 /// Latt-Chopard projection of fneq onto the second-order Hermite space.
 __device__ __forceinline__ void regularize(float (&fneq)[kQ]) {
@@ -105,8 +104,8 @@ fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restri
     float wsum = 0.0f;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-        const int X = wrapi(ix + (c & 1), cnx), Y = wrapi(iy + ((c >> 1) & 1), cny);
-        const int Z = wrapi(iz + ((c >> 2) & 1), cnz);
+        const int X = wrap1(ix + (c & 1), cnx), Y = wrap1(iy + ((c >> 1) & 1), cny);
+        const int Z = wrap1(iz + ((c >> 2) & 1), cnz);
         corner[c] = static_cast<std::uint32_t>(X) + static_cast<std::uint32_t>(cnx)
                   * (static_cast<std::uint32_t>(Y) + static_cast<std::uint32_t>(cny) * Z);
         if ((ckind[corner[c]] & kFlagMask) == kSolid) w8[c] = 0.0f;
