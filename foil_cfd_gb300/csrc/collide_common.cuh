@@ -628,22 +628,7 @@ collide_cell_kernel(const typename S::T* __restrict__ src, typename S::T* __rest
 // rows of the airfoil patch), a row-per-block launch ends every row with a
 // partly idle warp; here consecutive threads take consecutive cells across
 // row boundaries. (x, y, z) come from two divisions by invariant integers
-// (Granlund & Montgomery 1994: q = (t + ((n - t) >> 1)) >> s, t = mulhi(m, n)).
-struct FastDiv {
-    unsigned d, m;
-    int s;
-};
-/// Divisor d >= 2: m = floor(2^32 (2^l - d) / d) + 1, s = l - 1, l = ceil(log2 d).
-inline FastDiv fast_div(unsigned d) {
-    int l = 0;
-    while ((1ull << l) < d) ++l;
-    const unsigned long long m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
-    return FastDiv{d, static_cast<unsigned>(m), l - 1};
-}
-__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv& f) {
-    const unsigned t = __umulhi(n, f.m);
-    return (t + ((n - t) >> 1)) >> f.s;
-}
+// (FastDiv, d3q19.cuh).
 
 template <class S, bool WM, bool EXACT, bool QL>
 __global__ void __launch_bounds__(kCellBlockX, S::kCellMinBlocks)

@@ -103,6 +103,26 @@ __host__ __device__ __forceinline__ bool is_slip_z(int f) {
 constexpr float kMaxSimSpeed = 0.30f;
 constexpr float kRhoFloor = 0.05f;
 
+// ---- division by an invariant integer ----------------------------------------
+// Granlund & Montgomery 1994, "Division by invariant integers using
+// multiplication": q = (t + ((n - t) >> 1)) >> s with t = mulhi(m, n), exact
+// for every 32-bit n.
+struct FastDiv {
+    unsigned d, m;
+    int s;
+};
+/// Divisor d >= 2: m = floor(2^32 (2^l - d) / d) + 1, s = l - 1, l = ceil(log2 d).
+inline FastDiv fast_div(unsigned d) {
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    const unsigned long long m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, static_cast<unsigned>(m), l - 1};
+}
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv& f) {
+    const unsigned t = __umulhi(n, f.m);
+    return (t + ((n - t) >> 1)) >> f.s;
+}
+
 // ---- population storage ---------------------------------------------------
 // FP32: the population itself. FP16: the deviation f_q - w_q as IEEE half,
 // widened to FP32 on load (deviation storage keeps the O(1) weight out of the

@@ -73,15 +73,14 @@ __global__ void __launch_bounds__(kRefineBlock)
 fill_kernel(const typename S::T* __restrict__ cT0, const typename S::T* __restrict__ cT1,
             const std::uint8_t* __restrict__ ckind, typename S::T* __restrict__ ff,
             const std::uint32_t* __restrict__ targets, int count, RefineGeom g, float invFactor,
-            float tw, float neqScale) {
+            float tw, float neqScale, FastDiv divX, FastDiv divXY) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const std::uint32_t t = targets[i];
-    const unsigned fnx = g.fine.nx, fnxy = static_cast<unsigned>(g.fine.nx) * g.fine.ny;
-    const int zf = static_cast<int>(t / fnxy);
-    const unsigned rem = t - static_cast<unsigned>(zf) * fnxy;
-    const int yf = static_cast<int>(rem / fnx);
-    const int xf = static_cast<int>(rem - static_cast<unsigned>(yf) * fnx);
+    const int zf = static_cast<int>(fdiv(t, divXY));
+    const unsigned rem = t - static_cast<unsigned>(zf) * divXY.d;
+    const int yf = static_cast<int>(fdiv(rem, divX));
+    const int xf = static_cast<int>(rem - static_cast<unsigned>(yf) * divX.d);
 
     const float gx = static_cast<float>(g.boxX0) + (static_cast<float>(xf) + 0.5f) * invFactor - 0.5f;
     const float gy = static_cast<float>(g.boxY0) + (static_cast<float>(yf) + 0.5f) * invFactor - 0.5f;
@@ -278,14 +277,16 @@ cudaError_t launch_fill_c2f(Storage s, const void* cT0, const void* cT1,
     const unsigned nb = static_cast<unsigned>((count + kRefineBlock - 1) / kRefineBlock);
     const float invF = 1.0f / static_cast<float>(g.factor);
     const bool blend = timeWeight != 0.0f;
+    const FastDiv dx = fast_div(static_cast<unsigned>(g.fine.nx));
+    const FastDiv dxy = fast_div(static_cast<unsigned>(g.fine.nx) * static_cast<unsigned>(g.fine.ny));
     if (s == Storage::F32)
         (blend ? fill_kernel<StoreF32, true> : fill_kernel<StoreF32, false>)<<<nb, kRefineBlock, 0, st>>>(
             static_cast<const float*>(cT0), static_cast<const float*>(cT1), coarseKind,
-            static_cast<float*>(fineF), targets, count, g, invF, timeWeight, neqScale);
+            static_cast<float*>(fineF), targets, count, g, invF, timeWeight, neqScale, dx, dxy);
     else
         (blend ? fill_kernel<StoreF16, true> : fill_kernel<StoreF16, false>)<<<nb, kRefineBlock, 0, st>>>(
             static_cast<const __half*>(cT0), static_cast<const __half*>(cT1), coarseKind,
-            static_cast<__half*>(fineF), targets, count, g, invF, timeWeight, neqScale);
+            static_cast<__half*>(fineF), targets, count, g, invF, timeWeight, neqScale, dx, dxy);
     return cudaGetLastError();
 }
 
