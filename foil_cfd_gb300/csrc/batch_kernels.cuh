@@ -29,6 +29,11 @@ template <class S, bool EXACT, int BX, int ROWS>
 __global__ void __launch_bounds__(BX, S::kBatchThreads / BX)
 batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, unsigned nItems, int parity) {
     using T = typename S::T;
+    // FP32: the near-wall gather reads the cells' link words (batch step
+    // 1.054 -> 0.950 ms on the polar); FP16: the same path at the 64-register
+    // cap spilled more and measured 3 % slower, so it reads the neighbours'
+    // flags.
+    constexpr bool kLinkWall = std::is_same_v<S, StoreF32>;
     const unsigned itemEnd = itemBase + nItems;
     for (unsigned item = itemBase + blockIdx.x; item < itemEnd; item += gridDim.x) {
         int lo = 0, hi = P.ntun - 1;
@@ -47,11 +52,7 @@ batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, un
         a.uwx = a.uwy = a.uwz = nullptr;
         a.status = nullptr;
         a.qFrac = nullptr;
-        // FP32: the near-wall gather reads the link classes (batch step
-        // 1.054 -> 0.950 ms on the polar); FP16: the same path at the 64-
-        // register cap spilled more and measured 3 % slower, so it reads
-        // the neighbours' flags.
-        a.links = std::is_same_v<S, StoreF32> ? tp.links : nullptr;
+        a.links = tp.links;
         a.ffMask = nullptr;
         const T* src = static_cast<const T*>(tp.f[parity]);
         T* dst = static_cast<T*>(tp.f[parity ^ 1]);
@@ -65,7 +66,7 @@ batch_collide_kernel(const __grid_constant__ BatchTable P, unsigned itemBase, un
             const unsigned z = row / ny;
             const int y = static_cast<int>(row - z * ny);
             for (int x = threadIdx.x; x < tp.nx; x += BX)
-                collide_one<S, false, EXACT>(src, dst, tp.kind, a, x, y, static_cast<int>(z));
+                collide_one<S, false, EXACT, false, kLinkWall>(src, dst, tp.kind, a, x, y, static_cast<int>(z));
         }
     }
 }

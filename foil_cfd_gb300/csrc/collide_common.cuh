@@ -64,11 +64,6 @@ struct CollideArgs {
 struct PullOffsets {
     long long pull[kQ];
     long long slice[kQ];
-    /// Free-slip pulls of a near-wall interior cell: the mirrored slot of the
-    /// tangentially displaced cell, (x - c_x, y, z - c_z) for a y wall and
-    /// (x - c_x, y - c_y, z) for a z wall.
-    long long slipY[kQ];
-    long long slipZ[kQ];
 };
 
 template <class T>
@@ -78,8 +73,6 @@ __host__ PullOffsets pull_offsets(int nx, int ny, long long n) {
     for (int q = 0; q < kQ; ++q) {
         o.slice[q] = q * n * static_cast<long long>(sizeof(T));
         o.pull[q] = (q * n - (cx(q) + sx * cy(q) + sxy * cz(q))) * static_cast<long long>(sizeof(T));
-        o.slipY[q] = (mir_y(q) * n - (cx(q) + sxy * cz(q))) * static_cast<long long>(sizeof(T));
-        o.slipZ[q] = (mir_z(q) * n - (cx(q) + sx * cy(q))) * static_cast<long long>(sizeof(T));
     }
     return o;
 }
@@ -428,8 +421,10 @@ __device__ __forceinline__ void store_cell(typename S::T* __restrict__ dst, cons
 }
 
 /// Near-wall fluid cell: the upstream flag picks the (slot, cell) pair per
-/// link; the wall-model Ladd term 6 w_q (c_q . u_w) on solid links.
-template <class S, bool WM, bool QL, bool DEV>
+/// link; the wall-model Ladd term 6 w_q (c_q . u_w) on solid links. LW: the
+/// links' classes come from the cell's link word (a.links) instead of the
+/// 18 neighbours' flags.
+template <class S, bool WM, bool QL, bool DEV, bool LW = false>
 __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ src,
                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a,
                                             const Nbr& b, unsigned cell, int y, int z, float (&f)[kQ]) {
@@ -438,10 +433,8 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
     float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
     bool uwLoaded = false;
     using P = Pop<S, DEV>;
-    // The links' classes: one 8-byte word per cell when the level has them,
-    // else the 18 neighbours' flags.
     unsigned long long lm = 0;
-    if (a.links) {
+    if constexpr (LW) {
         const uint2 w = __ldg(a.links + cell);
         lm = static_cast<unsigned long long>(w.x) | (static_cast<unsigned long long>(w.y) << 32);
     }
@@ -451,7 +444,7 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
         const unsigned X = b.sx[1 + cx(q)], Y = b.sy[1 + cy(q)], Z = b.sz[1 + cz(q)];
         const unsigned pn = X + unx * (Y + uny * Z);
         bool solid, slipY, slipZ;
-        if (a.links) {
+        if constexpr (LW) {
             solid = (lm >> (q - 1)) & 1ull;
             slipY = (lm >> (17 + q)) & 1ull;
             slipZ = (lm >> (35 + q)) & 1ull;
@@ -501,17 +494,14 @@ __device__ __forceinline__ void gather_wall(const typename S::T* __restrict__ sr
     }
 }
 
-/// Near-wall interior cell (link classes lm, the 64-bit word of
-/// launch_classify): the pulls of gather_wall through the constant offsets
-/// -- the own cell's opposite slot on a solid link, the mirrored slot of the
-/// tangentially displaced cell on a slip link (SLIP: the cell has one), the
-/// upstream cell otherwise -- with the same interpolated bounce-back and
-/// Ladd terms.
-template <class S, bool WM, bool QL, bool DEV, bool SLIP>
-__device__ __forceinline__ void gather_links(const typename S::T* __restrict__ src, const CollideArgs& a,
-                                             const PullOffsets& o, unsigned cell, int x, int y, int z,
-                                             unsigned long long lm, float (&f)[kQ]) {
-    const unsigned solidMask = static_cast<unsigned>(lm) & 0x3FFFFu;
+/// Near-wall interior cell whose wall links are all solid (bit q - 1 of
+/// `solidMask`): the pulls of gather_wall through the constant offsets --
+/// the own cell's opposite slot on a solid link, the upstream cell
+/// otherwise -- with the same interpolated bounce-back and Ladd terms.
+template <class S, bool WM, bool QL, bool DEV>
+__device__ __forceinline__ void gather_solid_links(const typename S::T* __restrict__ src, const CollideArgs& a,
+                                                   const PullOffsets& o, unsigned cell, int x, int y, int z,
+                                                   unsigned solidMask, float (&f)[kQ]) {
     using P = Pop<S, DEV>;
     const typename S::T* base = src + cell;
     float uwx = 0.0f, uwy = 0.0f, uwz = 0.0f;
@@ -524,13 +514,7 @@ __device__ __forceinline__ void gather_links(const typename S::T* __restrict__ s
 #pragma unroll
     for (int q = 1; q < kQ; ++q) {
         const bool solid = (solidMask >> (q - 1)) & 1u;
-        long long off = o.pull[q];
-        if constexpr (SLIP) {
-            if ((lm >> (35 + q)) & 1ull) off = o.slipZ[q];
-            if ((lm >> (17 + q)) & 1ull) off = o.slipY[q];
-        }
-        if (solid) off = o.slice[opp(q)];
-        float fq = P::ld(byte_add(base, off), 0, wgt(q));
+        float fq = P::ld(byte_add(base, solid ? o.slice[opp(q)] : o.pull[q]), 0, wgt(q));
         if (QL && solid) {
             const std::uint8_t qb = a.qFrac[static_cast<long long>(cell) * kQ + q];
             if (qb != 0) {
@@ -567,7 +551,7 @@ __device__ __forceinline__ void finish_cell(typename S::T* __restrict__ dst, con
 /// The 19 post-streaming populations of fluid cell (x, y, z): bulk cells by
 /// plain pulls (constant offsets away from the periodic faces when `o` is
 /// given), near-wall cells through their neighbours' flags.
-template <class S, bool WM, bool QL, bool DEV>
+template <class S, bool WM, bool QL, bool DEV, bool LW = false>
 __device__ __forceinline__ void gather_fluid(const typename S::T* __restrict__ src,
                                              const std::uint8_t* __restrict__ kind, const CollideArgs& a,
                                              std::uint8_t k, unsigned cell, int x, int y, int z, float (&f)[kQ],
@@ -577,24 +561,25 @@ __device__ __forceinline__ void gather_fluid(const typename S::T* __restrict__ s
         else gather_bulk<S, DEV>(src, a, neighbours(x, y, z, a.nx, a.ny, a.nz), f);
         return;
     }
-    // Near-wall cell. With the link classes at hand, an interior cell pulls
-    // through the constant offsets, a select per link among the upstream
-    // cell, its own opposite slot (solid) and the mirrored slot of the
-    // displaced cell (slip); cells on the periodic faces take the general
-    // path.
+    // Near-wall cell. With the link classes at hand, an interior cell whose
+    // wall links are all solid (the cells along a foil) pulls through the
+    // constant offsets, a select per link choosing its own opposite slot over
+    // the upstream cell; slip-wall cells and the periodic faces take the
+    // general path (measured the same as a slip-aware select path, which
+    // needs more registers).
     if (a.links && o && interior(x, y, z, a)) {
         const uint2 w = __ldg(a.links + cell);
-        const unsigned long long lm = static_cast<unsigned long long>(w.x) | (static_cast<unsigned long long>(w.y) << 32);
-        if ((lm >> 18) == 0) gather_links<S, WM, QL, DEV, false>(src, a, *o, cell, x, y, z, lm, f);
-        else gather_links<S, WM, QL, DEV, true>(src, a, *o, cell, x, y, z, lm, f);
-        return;
+        if (w.y == 0 && (w.x >> 18) == 0) {   // solid links only (no slip-wall bit)
+            gather_solid_links<S, WM, QL, DEV>(src, a, *o, cell, x, y, z, w.x, f);
+            return;
+        }
     }
-    gather_wall<S, WM, QL, DEV>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
+    gather_wall<S, WM, QL, DEV, LW>(src, kind, a, neighbours(x, y, z, a.nx, a.ny, a.nz), cell, y, z, f);
 }
 
 /// One full cell update at (x, y, z): boundary cells by flag, fluid cells
 /// by their 19 pulls (bulk or near-wall path) and the collision.
-template <class S, bool WM, bool EXACT, bool QL = false>
+template <class S, bool WM, bool EXACT, bool QL = false, bool LW = false>
 __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ src, typename S::T* __restrict__ dst,
                                             const std::uint8_t* __restrict__ kind, const CollideArgs& a, int x, int y,
                                             int z, const PullOffsets* o = nullptr) {
@@ -607,7 +592,7 @@ __device__ __forceinline__ void collide_one(const typename S::T* __restrict__ sr
         return;
     }
     float f[kQ];
-    gather_fluid<S, WM, QL, !EXACT>(src, kind, a, k, cell, x, y, z, f, o);
+    gather_fluid<S, WM, QL, !EXACT, LW>(src, kind, a, k, cell, x, y, z, f, o);
     finish_cell<S, EXACT>(dst, a, cell, f, o);
 }
 
