@@ -1,6 +1,8 @@
-// Per-cell building blocks of the stream-collide kernels and the two kernel
-// templates built from them: the one-cell-per-thread kernel and the staged
-// kernel that streams x-rows through shared memory with bulk async copies.
+// Per-cell building blocks of the stream-collide kernels and the kernel
+// templates built from them: the one-cell-per-thread kernels (per row and
+// over the flattened lattice), the fine collide with the restriction's child
+// sums fused in, the staged kernel that streams x-rows through shared memory
+// with bulk async copies, and the AA-pattern in-place kernels.
 //
 // Physics follows the reference step (src/sim/lbm_core.cu:213-475): per link
 // the upstream neighbour's flag selects plain streaming, half-way bounce-back

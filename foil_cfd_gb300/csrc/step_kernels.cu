@@ -1,8 +1,9 @@
-// Per-level kernels around the stream-collide: cell-kind classification,
-// equilibrium / speck / macroscopic initialisation, the NaN watchdog, FP32 <->
-// storage conversion, and the FP16-storage stream-collide (the pair-sum
-// collision body of collide_common.cuh with fused multiply-adds; the FP32
-// storage collide lives in collide_f32.cu, compiled without contraction).
+// Per-level kernels around the stream-collide: cell-kind and pull-link
+// classification, equilibrium / speck / macroscopic initialisation, the NaN
+// watchdog, FP32 <-> storage conversion, the AA layout's conversions, and the
+// FP16-storage stream-collide (the deviation collision body of
+// collide_common.cuh; the FP32 storage collide lives in collide_f32.cu,
+// compiled without contraction).
 //
 // GB300 layout choices (not in the reference): the buffers are unpadded SoA
 // and all three axes wrap periodically in the index math, so there is no
