@@ -59,6 +59,18 @@ def workload(small: bool):
     return tunnels.airfoil_tunnel()
 
 
+def reference_workload(small: bool, patch: bool = True, dims=None, chord=None, aoa=6.0):
+    """The same tunnel built with the reference's own host builders (the
+    staged geometry kit, oracle/ref_geom.py): the reference arm never loads
+    this library. None when the kit is not available."""
+    from oracle import ref_geom
+    if not ref_geom.available():
+        return None
+    if dims is None:
+        dims, chord = ((320, 96, 96), 128) if small else ((640, 192, 192), 256)
+    return ref_geom.airfoil_tunnel(*dims, chord=chord, aoa=aoa, patch=patch)
+
+
 COLLIDE_KERNEL = "auto"
 
 
@@ -787,8 +799,11 @@ def reference_cuda_leg(warmup=100, steps=100):
     if not ref_gpu.available():
         return {"unavailable": "reference cubin not built (the reference tree is only in the build container) "
                                "or nvcc missing"}
-    from oracle import oracle
-    t = headline_tunnel()
+    from oracle import oracle, ref_geom
+    h = HEADLINE
+    t = reference_workload(False, patch=False, dims=(h["nx"], h["ny"], h["nz"]), chord=h["chord"], aoa=h["aoa"])
+    if t is None:
+        return {"unavailable": "the reference's geometry builders are not staged (oracle/ref_geom.py)"}
     n = int(np.prod(t.dims))
     # Uniform start feq(1, u_in) everywhere (the oracle's equilibrium).
     f0 = oracle.equilibrium(np.ones(n), np.full(n, HEADLINE["u"]), np.zeros(n), np.zeros(n), np.float32)
@@ -807,12 +822,11 @@ def reference_cuda_leg(warmup=100, steps=100):
     # levels (wall lists from this library's host builder, byte-identical to
     # the reference's buildWallCellList); the watchdog every 200 steps.
     # Counted as coarse + 2 x fine updates.
-    import foil_cfd_gb300 as fc
-    w = workload(False)
-    sc = _scaling_of(w)
-    wc = fc.build_wall_list(w.dims, w.flags, None, 2)
-    wf = fc.build_wall_list(w.fine_dims, w.fine_flags, None, 3)
-    r3 = ref_gpu.run_full(w.dims, w.flags, sc.tau, w.u_lat, cs=0.1, wall=wc,
+    w = reference_workload(False)
+    tau3, _ = ref_geom.scaling(1.2, 30.0, 1.48e-5, w.chord_cells, w.u_lat)
+    wc = ref_geom.wall_list(w.dims, w.flags, None, 2)
+    wf = ref_geom.wall_list(w.fine_dims, w.fine_flags, None, 3)
+    r3 = ref_gpu.run_full(w.dims, w.flags, tau3, w.u_lat, cs=0.1, wall=wc,
                           fine=dict(dims=w.fine_dims, flags=w.fine_flags, box=w.box, factor=w.factor, wall=wf),
                           wm=True, warmup=10, steps=100, batch=BATCH, forces=True, watchdog=True,
                           variant="asbuilt")
@@ -989,17 +1003,23 @@ def cpu_host():
 
 def cpu_reference(t, steps):
     """The oracle port (C++ restatement, OpenMP, all host threads) on the
-    same tunnel: `steps` coarse steps after one warm-up batch."""
-    from oracle import oracle
-    import foil_cfd_gb300 as fc
+    same tunnel: `steps` coarse steps after one warm-up batch. `t` comes from
+    reference_workload (the reference's builders, scaling and wall lists)."""
+    from oracle import oracle, ref_geom
     oracle.build()
-    s = fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat)
+    if ref_geom.available():
+        tau, _ = ref_geom.scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat)
+        wall_list = ref_geom.wall_list
+    else:   # this library's builders, byte-identical (tests/test_ref_geom_kit.py)
+        import foil_cfd_gb300 as fc
+        tau = fc.compute_scaling(1.2, 30.0, 1.48e-5, t.chord_cells, t.u_lat).tau
+        wall_list = fc.build_wall_list
     f0 = oracle.init_equilibrium(t.dims, t.flags, np.float32(t.u_lat))
-    ot = oracle.OracleTunnel(t.dims, t.flags, f0, np.float32(s.tau), np.float32(t.u_lat), cs=0.1)
+    ot = oracle.OracleTunnel(t.dims, t.flags, f0, np.float32(tau), np.float32(t.u_lat), cs=0.1)
     if t.box is not None:
         ot.refine((t.box.x0, t.box.y0, t.box.x1, t.box.y1), t.factor, t.fine_flags)
-        ot.wall(1, fc.build_wall_list(t.fine_dims, t.fine_flags, sample_cells=3))
-    ot.wall(0, fc.build_wall_list(t.dims, t.flags, sample_cells=2))
+        ot.wall(1, wall_list(t.fine_dims, t.fine_flags, None, 3))
+    ot.wall(0, wall_list(t.dims, t.flags, None, 2))
     ot.step_n(1)
     t0 = time.perf_counter()
     ot.step_n(steps)
@@ -1017,12 +1037,15 @@ def cpu_config1():
     vortex (u0 0.05, tau 0.53, no LES), 1000 steps of the oracle port
     (C++ restatement of the reference step, OpenMP, all host threads)."""
     from oracle import oracle
-    from foil_cfd_gb300 import tunnels
     oracle.build()
-    t = tunnels.taylor_green_periodic(64, 0.05)
-    n = int(np.prod(t.dims))
-    f0 = oracle.equilibrium(np.ones(n), t.extra["u"], t.extra["v"], np.zeros(n), np.float32)
-    o = oracle.OracleSolver(t.dims, t.flags, np.float32(0.53), np.float32(0.0), cs=-1.0)
+    N, u0 = 64, 0.05
+    n = N ** 3
+    z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    k = 2 * np.pi / N
+    u = u0 * np.sin(k * x) * np.cos(k * y) * np.cos(k * z)
+    v = -u0 * np.cos(k * x) * np.sin(k * y) * np.cos(k * z)
+    f0 = oracle.equilibrium(np.ones(n), u.ravel(), v.ravel(), np.zeros(n), np.float32)
+    o = oracle.OracleSolver((N, N, N), np.zeros(n, np.uint8), np.float32(0.53), np.float32(0.0), cs=-1.0)
     o.set_state(f0)
     t0 = time.perf_counter()
     o.step_n(1000)
@@ -1030,6 +1053,22 @@ def cpu_config1():
     return {"workload": "config 1: 64^3 periodic Taylor-Green, u0 0.05, tau 0.53, no LES, FP32, 1000 steps",
             "value": round(n * 1000 / dt / 1e9, 5), "unit": UNIT, "seconds": round(dt, 2),
             "cores": oracle.threads(), "kind": "port", "host": cpu_host()}
+
+
+def workload_config(t, ws: int) -> dict:
+    """The `config` object of both arms' JSON lines."""
+    return {"workload": f"airfoil tunnel {t.name}: NACA 0012 at 6 deg, 256 cells/chord, u_lat 0.08, "
+                       "Re 2.4e6 (tau 0.5005), TRT + Smagorinsky Cs 0.1, iMEM wall model, one 2:1 patch "
+                       "+-0.1 chord, uniform-flow start",
+           "dims": list(t.dims), "fine_dims": list(t.fine_dims) if t.box else None,
+           "updates_per_step": t.updates_per_step(), "batch": BATCH,
+           "counting": "coarse + 2 x fine lattice updates per coarse step",
+           "l2": "populations (>10 GB) exceed the 129 MB L2; no flush needed",
+           "window": f"every timed run is at most {CHUNK} steps from the state {SETTLE} steps after the "
+                     "uniform-flow start (exact device restore between runs, outside the timed region): the "
+                     "as-specified tunnel trips the speed watchdog between 110 and 200 steps from the start, in "
+                     "the reference's own step as in this one (stability leg)",
+           "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 
 
 def dist_setup():
@@ -1109,24 +1148,18 @@ def main():
     COLLIDE_KERNEL = args.kernel
     warmup = max(args.warmup, 3)
     dist, rank, ws = dist_setup()
-    t = workload(args.small)
-
-    cfg = {"workload": f"airfoil tunnel {t.name}: NACA 0012 at 6 deg, 256 cells/chord, u_lat 0.08, "
-                       "Re 2.4e6 (tau 0.5005), TRT + Smagorinsky Cs 0.1, iMEM wall model, one 2:1 patch "
-                       "+-0.1 chord, uniform-flow start",
-           "dims": list(t.dims), "fine_dims": list(t.fine_dims) if t.box else None,
-           "updates_per_step": t.updates_per_step(), "batch": BATCH,
-           "counting": "coarse + 2 x fine lattice updates per coarse step",
-           "l2": "populations (>10 GB) exceed the 129 MB L2; no flush needed",
-           "window": f"every timed run is at most {CHUNK} steps from the state {SETTLE} steps after the "
-                     "uniform-flow start (exact device restore between runs, outside the timed region): the "
-                     "as-specified tunnel trips the speed watchdog between 110 and 200 steps from the start, in "
-                     "the reference's own step as in this one (stability leg)",
-           "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
-
     if args.impl == "reference":
         if rank != 0:
             return
+        # The tunnel and its wall lists from the reference's own host
+        # builders (staged kit), so this arm never loads this library.
+        t = reference_workload(args.small)
+        geometry = "the reference's own host builders (voxelizer.cpp, airfoil.cpp, wall_model.cpp, units.h)"
+        if t is None:
+            t = workload(args.small)
+            geometry = "this library's host builders (byte-identical to the reference's)"
+        cfg = workload_config(t, ws)
+        cfg["geometry"] = geometry
         steps = max(1, min(args.steps, 3))
         ref = cpu_reference(t, steps)
         line = {"impl": "reference", "metric": METRIC, "value": ref["value"], "unit": UNIT, "n_gpus": args.gpus,
@@ -1144,6 +1177,9 @@ def main():
                 line["reference_cuda_kernel"] = {"unavailable": str(ex)[:200]}
         print(json.dumps(line))
         return
+
+    t = workload(args.small)
+    cfg = workload_config(t, ws)
 
     if args.only_precision:
         if rank == 0:
@@ -1220,7 +1256,8 @@ def main():
         r16["vsnap"].close()
         r16["solver"] = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = {k: v for k, v in cpu_reference(t, 2).items() if k != "seconds"}
+        line["cpu_baseline"] = {k: v for k, v in cpu_reference(reference_workload(args.small) or t, 2).items()
+                                if k != "seconds"}
     if dist is not None:
         dist.barrier()
     if rank == 0:

@@ -134,8 +134,11 @@ def build(force: bool = False) -> dict:
             raise RuntimeError(f"reference snapshot build failed:\n{r.stderr[-4000:]}")
     # The reference's own solver tests, staged for relinking against this
     # library through the LBMSolver shim (oracle/relink.py).
-    from oracle import relink
+    from oracle import ref_geom, relink
     libs["relink"] = relink.stage(REFERENCE)
+    # The host geometry builders, staged the same way for the benchmark's
+    # reference arm on the GPU machine (oracle/ref_geom.py).
+    libs["geomkit"] = ref_geom.stage(REFERENCE)
     return libs
 
 

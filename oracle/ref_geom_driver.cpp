@@ -1,13 +1,16 @@
 // ORACLE - test infrastructure only. C entry points over the reference's host
 // geometry builders (src/geom/voxelizer.cpp, airfoil.cpp; vg.cpp and
-// src/platform/platform.cpp only to resolve their symbols), compiled
-// unmodified from the reference tree by ref_build.py, for golden-vector
-// generation: NACA 4-digit outlines, the clean-foil flag field (boundary
-// flags + voxelised foil + trailing-edge closure), the fine-patch flag field
-// (all fluid + foil + closure + interface shell) and the derived patch box.
+// src/platform/platform.cpp only to resolve their symbols) and its
+// computeScaling (src/sim/units.h), compiled unmodified by ref_build.py (from
+// the reference tree) and ref_geom.py (from the staged kit), for golden
+// vectors and the benchmark's reference arm: NACA 4-digit outlines, the
+// clean-foil flag field (boundary flags + voxelised foil + trailing-edge
+// closure), the fine-patch flag field (all fluid + foil + closure +
+// interface shell), the derived patch box and the lattice scaling.
 #include <cstring>
 #include <string>
 
+#include "units.h"
 #include "voxelizer.h"
 
 namespace {
@@ -107,4 +110,25 @@ extern "C" int ref_close_te(int nx, int ny, int nz, unsigned char* flags) {
     const int closed = foilcfd::closeTrailingEdgeGaps(d, f);
     std::memcpy(flags, f.data(), f.size());
     return closed;
+}
+
+// stampInterfaceShell (voxelizer.cpp) on an existing flag field.
+extern "C" void ref_stamp_interface_shell(int nx, int ny, int nz, unsigned char* flags) {
+    foilcfd::GridDims d;
+    d.nx = nx; d.ny = ny; d.nz = nz;
+    std::vector<std::uint8_t> f(flags, flags + d.cellCount());
+    foilcfd::stampInterfaceShell(d, f);
+    std::memcpy(flags, f.data(), f.size());
+}
+
+// computeScaling (units.h): tau and the clamped u_lat of a physical case.
+extern "C" void ref_compute_scaling(float chord_m, float airspeed_ms, float nu_m2s, int chord_cells, float u_lat,
+                                    float* tau, float* u_lat_out) {
+    foilcfd::PhysicalParams p;
+    p.chord_m = chord_m;
+    p.airspeed_ms = airspeed_ms;
+    p.nu_m2s = nu_m2s;
+    const foilcfd::LatticeScaling s = foilcfd::computeScaling(p, chord_cells, u_lat);
+    *tau = s.tau;
+    *u_lat_out = s.u_lat;
 }
