@@ -794,7 +794,8 @@ def reference_cuda_leg(warmup=100, steps=100):
     """The reference's own CUDA stream-collide (+ its per-step ghost-plane
     refresh) on this GPU and the same configuration: compiled from the
     reference tree as it builds it (nvcc -O3, sm_103a) into a cubin in the
-    build container, launched through the driver-API harness."""
+    build container, launched through the driver-API harness, on tunnels
+    built by the reference's own host code (reference_workload)."""
     from oracle import ref_gpu
     if not ref_gpu.available():
         return {"unavailable": "reference cubin not built (the reference tree is only in the build container) "
@@ -819,9 +820,9 @@ def reference_cuda_leg(warmup=100, steps=100):
     # the wall model on, the reference's whole refined stepN: per step the
     # collides, fills, restriction and ghost refreshes; per batch of 50 the
     # force reduction on the fine level and the wall-model update of both
-    # levels (wall lists from this library's host builder, byte-identical to
-    # the reference's buildWallCellList); the watchdog every 200 steps.
-    # Counted as coarse + 2 x fine updates.
+    # levels (wall lists from the reference's buildWallCellList, through the
+    # staged geometry kit); the watchdog every 200 steps. Counted as coarse +
+    # 2 x fine updates.
     w = reference_workload(False)
     tau3, _ = ref_geom.scaling(1.2, 30.0, 1.48e-5, w.chord_cells, w.u_lat)
     wc = ref_geom.wall_list(w.dims, w.flags, None, 2)
