@@ -117,8 +117,10 @@ def test_aa_holds_one_population_array(fc):
         taken[layout] = free0 - torch.cuda.mem_get_info()[0]
         del s
     pop = Q * 4 * n
+    # One population array (76 B per cell) saved, less the AA scratch slice;
+    # the rest (flags, kind bytes, link classes, macroscopic fields) is common.
     assert taken["ab"] - taken["aa"] >= 0.9 * (pop - 4 * n), taken
-    assert taken["aa"] < 0.6 * taken["ab"], taken
+    assert taken["aa"] < 0.65 * taken["ab"], taken
 
 
 def test_aa_refuses_other_lattices(fc):
