@@ -14,8 +14,9 @@
 //
 // Two further u_tau solves can replace the reference's (template METHOD):
 // full FP64 Newton to a relative step of 1e-8 from the same seed, and the
-// learned seed (a 3-32-32-1 network, BF16 weights in shared memory) with one
-// FP32 correction and an FP64 fallback (wallnet.cuh).
+// learned seed (a 3-32-32-1 network, BF16 weights in shared memory, its
+// hidden layer a warp-wide tensor-core contraction over the warp's 32 wall
+// cells) with one FP32 correction and an FP64 fallback (wallnet.cuh).
 //
 // Kernels in an anonymous namespace, included by two translation units:
 // wall_kernels.cu (FP16 storage and the harvest; nvcc's default multiply-add
@@ -68,24 +69,32 @@ wall_update_kernel(const typename S::T* __restrict__ f, long long n, WallListDev
     bool active = false, clamped = false;
     int fallback = 0, iters = 0;
     float yplus = 0.0f;
-    if (i < L.count) {
-        const std::uint32_t cell = L.cellIdx[i];
-        const float nX = L.nX[i], nY = L.nY[i], nZ = L.nZ[i];
-        float rho, ux, uy, uz;
+    const bool valid = i < L.count;
+    std::uint32_t cell = 0;
+    float nX = 0.0f, nY = 0.0f, nZ = 0.0f, rho = 1.0f, tx = 0.0f, ty = 0.0f, tz = 0.0f, ut = 0.0f, ys = 1.0f;
+    if (valid) {
+        cell = L.cellIdx[i];
+        nX = L.nX[i]; nY = L.nY[i]; nZ = L.nZ[i];
+        float ux, uy, uz;
         sample_velocity<S>(f, n, L.sampleIdx[i], rho, ux, uy, uz);
-
         // Tangential component.
         const float un = ux * nX + uy * nY + uz * nZ;
-        const float tx = ux - un * nX, ty = uy - un * nY, tz = uz - un * nZ;
-        const float ut = sqrtf(tx * tx + ty * ty + tz * tz);
-        if (ut < utCut) {
+        tx = ux - un * nX; ty = uy - un * nY; tz = uz - un * nZ;
+        ut = sqrtf(tx * tx + ty * ty + tz * tz);
+        ys = L.ys[i];
+    }
+    const bool on = valid && !(ut < utCut);
+    // The learned seed is evaluated by the whole warp together.
+    float netSeed = 0.0f;
+    if constexpr (kNet) netSeed = wallnet::net_seed_warp(P, net.norm, ut, ys, nu, on);
+    if (valid) {
+        if (!on) {
             // No meaningful tangential flow: plain bounce-back at this cell.
             L.uTau[i] = 0.0f;
             uwx[cell] = 0; uwy[cell] = 0; uwz[cell] = 0;
         } else {
             active = true;
             const float itx = tx / ut, ity = ty / ut, itz = tz / ut;
-            const float ys = L.ys[i];
             const float prev = L.uTau[i];
             float solved;
             if (METHOD == 0) {
@@ -93,8 +102,7 @@ wall_update_kernel(const typename S::T* __restrict__ f, long long n, WallListDev
             } else if (METHOD == 1) {
                 solved = static_cast<float>(wallnet::newton64(ut, ys, nu, wallnet::reference_seed(ut, ys, nu, prev), &iters));
             } else {
-                solved = wallnet::learned_correct(ut, ys, nu, wallnet::net_seed(P, net.norm, ut, ys, nu), &fallback,
-                                                  &iters);
+                solved = wallnet::learned_correct(ut, ys, nu, netSeed, &fallback, &iters);
             }
             const float utau = prev > 0.0f ? prev + ema * (solved - prev) : solved;
             L.uTau[i] = utau;

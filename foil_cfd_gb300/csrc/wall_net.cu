@@ -260,23 +260,26 @@ utau_solve_kernel(NetDev net, const float* __restrict__ ut, const float* __restr
     }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int fallback = 0, iters = 0;
-    bool solved = false;
+    float u = 0.0f, y = 1.0f, v = 1.0f;
+    if (i < n) { u = ut[i]; y = ys[i]; v = nu[i]; }
+    const bool solved = i < n && u > 0.0f && y > 0.0f && v > 0.0f;
+    // The network seed is evaluated by the whole warp together.
+    float seed = 0.0f;
+    if constexpr (kNet) seed = net_seed_warp(P, net.norm, u, y, v, solved);
     if (i < n) {
-        const float u = ut[i], y = ys[i], v = nu[i];
         float r = 0.0f;
-        if (u > 0.0f && y > 0.0f && v > 0.0f) {
-            solved = true;
+        if (solved) {
             const float w0 = warm ? warm[i] : 0.0f;
             if (METHOD == FCFD_UTAU_REFERENCE) {
                 r = newton_reference(u, y, v, reference_seed(u, y, v, w0));
             } else if (METHOD == FCFD_UTAU_NEWTON64) {
                 r = static_cast<float>(newton64(u, y, v, reference_seed(u, y, v, w0), &iters));
             } else if (METHOD == FCFD_UTAU_LEARNED) {
-                r = learned_correct(u, y, v, net_seed(P, net.norm, u, y, v), &fallback, &iters);
+                r = learned_correct(u, y, v, seed, &fallback, &iters);
             } else if (METHOD == FCFD_UTAU_NEWTON64_NET) {
-                r = static_cast<float>(newton64(u, y, v, net_seed(P, net.norm, u, y, v), &iters));
+                r = static_cast<float>(newton64(u, y, v, seed, &iters));
             } else {
-                r = net_seed(P, net.norm, u, y, v);
+                r = seed;
             }
         }
         out[i] = r;
