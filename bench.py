@@ -1124,6 +1124,8 @@ def main():
     ap.add_argument("--only-fp16", action="store_true", help="measure the FP16-storage solver only")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wallnet", action="store_true", help="skip the learned wall-seed leg")
+    ap.add_argument("--only-wallnet", action="store_true",
+                    help="run only the learned wall-seed leg (on the tunnel 10 steps after the start)")
     ap.add_argument("--no-polar", action="store_true", help="skip the batched-polar leg")
     ap.add_argument("--no-geometry", action="store_true", help="skip the host-vs-device geometry build leg")
     ap.add_argument("--only-geometry", action="store_true", help="run only the geometry build leg")
@@ -1199,6 +1201,13 @@ def main():
             print(json.dumps({"layout": layout_leg(tuple(int(v) for v in args.layout_dims.split(",")),
                                                    steps=args.steps, warmup=warmup, tg_steps=args.layout_tg_steps,
                                                    storages=tuple(args.layout_storage.split(",")))}))
+        return
+    if args.only_wallnet:
+        if rank == 0:
+            sol, _ = make_solver(t, "fp32")
+            if sol.step_n(SETTLE) != 0:
+                raise RuntimeError("settling steps failed")
+            print(json.dumps({"wall_seed": wall_seed_leg(sol, t)}))
         return
     if args.only_polar:
         if rank == 0:
