@@ -95,7 +95,7 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = Path(os.environ.get("GRAFT_CLOCKS_FILE", "/tmp/foilcfd_clocks.csv"))
+        self.path = Path(os.environ.get("FOILCFD_CLOCKS_FILE", "/tmp/foilcfd_clocks.csv"))
 
     def start(self):
         try:
