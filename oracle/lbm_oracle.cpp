@@ -1,7 +1,7 @@
 // ORACLE - test infrastructure only. A CPU restatement of the reference
 // FoilCFD solver step, used by tests/, __graft_entry__.smoke() and the
-// cpu_baseline leg of bench.py as the checker and the timed CPU baseline;
-// the product never links or calls it.
+// cpu_baseline leg of bench.py as the reference results to compare against
+// and the timed CPU baseline; the product never links or calls it.
 //
 // Each routine follows the reference kernel line by line in the reference's
 // own operation order (compiled with -ffp-contract=off, so no FMA is formed

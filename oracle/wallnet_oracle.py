@@ -1,7 +1,7 @@
 """ORACLE - test infrastructure only (tests/, smoke() and bench.py's
 cpu_baseline leg). FP64 numpy restatement of the learned u_tau seed's
-network and of its training gradient, the checker of the library's
-forward/backward kernels (include/foilcfd_wallnet.h).
+network and of its training gradient, against which the tests compare the
+library's forward/backward kernels (include/foilcfd_wallnet.h).
 
 The network has no counterpart in the reference (its wall model,
 src/sim/lbm_wallmodel.cu:31-196, seeds Newton from the stored u_tau or
