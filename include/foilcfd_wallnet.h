@@ -12,7 +12,10 @@
  *     log u_tau = log u_par + out_mean + out_std * (W3 . h2 + b3)
  *
  * Weights are stored and applied as BF16 with FP32 accumulation; the
- * normalisation constants stay FP32. The network output is the logarithm of
+ * normalisation constants stay FP32. Inference (the seed solves and the
+ * solver's learned wall update) runs the 32x32 layer on the tensor cores,
+ * one warp's 32 samples per contraction, each FP32 activation split into
+ * three BF16 terms. The network output is the logarithm of
  * u_tau (the fixed log u_par term only centres the target). One FP32 Newton
  * correction follows; when the relative Reichardt residual |g| / u_par after
  * it exceeds 1e-6, the cell falls back to full FP64 Newton (relative step
