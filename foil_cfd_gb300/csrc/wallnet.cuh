@@ -75,6 +75,7 @@ __device__ __forceinline__ void mma_16x8x16_bf16(float (&d)[4], const unsigned (
 /// the layer-2 activations and W3 products of its accumulator fragments;
 /// the four lanes of a sample row sum their parts by shuffles.
 __device__ __forceinline__ float net_eval_warp(const float* P, float x0, float x1, float x2) {
+    __syncwarp();   // the fragments below assume the whole warp, converged
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     // Inputs of the lane's four A-fragment rows: sample g + 8 r.
     float in[4][3];
