@@ -830,14 +830,18 @@ def reference_cuda_leg(warmup=100, steps=100):
     r3 = ref_gpu.run_full(w.dims, w.flags, tau3, w.u_lat, cs=0.1, wall=wc,
                           fine=dict(dims=w.fine_dims, flags=w.fine_flags, box=w.box, factor=w.factor, wall=wf),
                           wm=True, warmup=10, steps=100, batch=BATCH, forces=True, watchdog=True,
-                          variant="asbuilt")
+                          variant="asbuilt", wall_reps=20)
     ms3 = r3["ms"]
     out["config3"] = {"workload": f"{w.name} + {w.fine_dims[0]}x{w.fine_dims[1]}x{w.fine_dims[2]} 2:1 patch, "
                                   "wall model, FP32: the reference's refined stepN launches incl. the per-batch "
                                   "force reduction and wall-model updates and the watchdog",
                       "glups": round(w.updates_per_step() * 100 / (ms3 * 1e-3) / 1e9, 3),
                       "ms_per_step": round(ms3 / 100, 4), "steps": 100, "warmup": 10,
-                      "watchdog_trips": r3["trip_step"]}
+                      "watchdog_trips": r3["trip_step"],
+                      # wallModelUpdateKernel alone on the same lists (stats reset + kernel, mean of 20),
+                      # beside this library's wall-seed leg figures
+                      "wall_update_ms": {"coarse": round(r3["wall_ms"][0], 5), "fine": round(r3["wall_ms"][1], 5),
+                                         "wall_cells": {"coarse": len(wc["cell"]), "fine": len(wf["cell"])}}}
     return out
 
 

@@ -71,13 +71,13 @@ class RunIn(C.Structure):
     _fields_ = [("coarse", LevelIn), ("fine", LevelIn), ("refined", C.c_int), ("bx0", C.c_int), ("by0", C.c_int),
                 ("bx1", C.c_int), ("by1", C.c_int), ("factor", C.c_int), ("tau", C.c_float), ("lam", C.c_float),
                 ("cs", C.c_float), ("u_in", C.c_float), ("wm", C.c_int), ("warmup", C.c_int), ("steps", C.c_int),
-                ("batch", C.c_int), ("forces", C.c_int), ("watchdog", C.c_int)]
+                ("batch", C.c_int), ("forces", C.c_int), ("watchdog", C.c_int), ("wallReps", C.c_int)]
 
 
 class RunOut(C.Structure):
     """RefRunOut of the harness."""
     _fields_ = [("ms", C.c_double), ("trip_step", C.c_longlong), ("trip_flag", C.c_int), ("checks", C.c_int),
-                ("force", C.c_float * 3), ("steps_run", C.c_longlong)]
+                ("force", C.c_float * 3), ("steps_run", C.c_longlong), ("wall_ms", C.c_double * 2)]
 
 
 _lib = None
@@ -159,7 +159,8 @@ def _level(dims, flags, f0, wall, keep, out_f, out_utau):
 
 
 def run_full(dims, flags, tau, u_in, cs=0.1, lam=3.0 / 16.0, f0=None, wall=None, fine=None, wm=True,
-             warmup=0, steps=100, batch=100, forces=True, watchdog=True, variant="asbuilt", states=False):
+             warmup=0, steps=100, batch=100, forces=True, watchdog=True, variant="asbuilt", states=False,
+             wall_reps=0):
     """The reference's stepN (lbm_solver.cpp:1132-1390) in calls of `batch`
     steps: collide + ghost refresh, with `fine` = dict(dims, flags, box,
     factor, f0, wall) the 2:1 patch's fills, fine collides and restriction;
@@ -168,7 +169,9 @@ def run_full(dims, flags, tau, u_in, cs=0.1, lam=3.0 / 16.0, f0=None, wall=None,
     seeds both A/B buffers of a level; None starts from feq(1, u_in)
     everywhere. Returns a dict with the timed ms, the watchdog's first trip
     (step and verdict), the last force and, with `states`, the final
-    populations and u_tau of each level."""
+    populations and u_tau of each level; with `wall_reps` > 0, after the
+    timed steps, the mean ms of that many back-to-back wall-model updates
+    per level on the state they left (wall_ms: coarse, fine)."""
     keep = []
     n = int(np.prod(dims))
     outs = {}
@@ -195,13 +198,13 @@ def run_full(dims, flags, tau, u_in, cs=0.1, lam=3.0 / 16.0, f0=None, wall=None,
         need.append("wall")
     rin.tau, rin.lam, rin.cs, rin.u_in = tau, lam, cs, u_in
     rin.wm, rin.warmup, rin.steps, rin.batch = int(wm), warmup, steps, batch
-    rin.forces, rin.watchdog = int(forces), int(watchdog)
+    rin.forces, rin.watchdog, rin.wallReps = int(forces), int(watchdog), int(wall_reps)
     out = RunOut()
     L = lib(variant, tuple(need))
     if L.refgpu_run_full(C.byref(rin), C.byref(out)) != 0:
         raise RuntimeError(L.refgpu_error().decode())
     res = dict(ms=out.ms, trip_step=int(out.trip_step), trip_flag=int(out.trip_flag), checks=int(out.checks),
-               force=tuple(out.force), steps=int(out.steps_run))
+               force=tuple(out.force), steps=int(out.steps_run), wall_ms=tuple(out.wall_ms))
     res.update(outs)
     return res
 

@@ -307,6 +307,7 @@ struct RefRunIn {
     int warmup, steps, batch;
     int forces;     // force reduction once per batch
     int watchdog;   // watchdog every 200 steps
+    int wallReps;   // after the timed steps: back-to-back wall-model updates timed per level (0: none)
 };
 
 struct RefRunOut {
@@ -316,6 +317,7 @@ struct RefRunOut {
     int checks;           // watchdog checks run
     float force[3];       // the last batch's force (FP32, atomics)
     long long stepsRun;
+    double wallMs[2];     // mean ms per wall-model update (stats reset + kernel), coarse / fine; 0: not timed
 };
 
 namespace {
@@ -624,6 +626,27 @@ extern "C" int refgpu_run_full(const RefRunIn* in, RefRunOut* out) {
     cudaError_t e = cudaEventSynchronize(e1);
     float t = 0.0f;
     cudaEventElapsedTime(&t, e0, e1);
+    // The wall-model update alone, on the state the timed steps left: each
+    // level's launchWallModelUpdate `wallReps` times back to back.
+    if (good && e == cudaSuccess && in->wallReps > 0) {
+        const float utCut = 1e-3f * uIn;
+        PaddedLevel* pl[2] = {&C, &F};
+        const int cur[2] = {cs_, fs};
+        const float nu[2] = {(tau - 0.5f) / 3.0f, (tauF - 0.5f) / 3.0f};
+        for (int k = 0; k < (refined ? 2 : 1) && good; ++k) {
+            if (pl[k]->wl.count <= 0) continue;
+            good = launch_wall(*pl[k], pl[k]->f[cur[k]], nu[k], utCut);   // warm
+            cudaEventRecord(e0, nullptr);
+            for (int r = 0; r < in->wallReps && good; ++r)
+                good = launch_wall(*pl[k], pl[k]->f[cur[k]], nu[k], utCut);
+            cudaEventRecord(e1, nullptr);
+            e = cudaEventSynchronize(e1);
+            float tw = 0.0f;
+            cudaEventElapsedTime(&tw, e0, e1);
+            if (e != cudaSuccess) break;
+            out->wallMs[k] = static_cast<double>(tw) / in->wallReps;
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e == cudaSuccess) e = cudaGetLastError();
