@@ -318,6 +318,21 @@ def e2e(t, res, steps):
                        "run steps (the first run's copy is exposed)"}
 
 
+def force_leg(sol, reps=20):
+    """The momentum-exchange force reduction alone on the level forces come
+    from (the fine patch), through fcfd_force_now: host clock around each
+    call, which also waits for the stream and reads the 24-byte result back,
+    so an upper bound on the reduction's device time."""
+    for _ in range(3):
+        sol.force_now()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sol.force_now()
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    return {"ms_per_call": round(ms, 5), "calls": reps,
+            "timing": "host clock around fcfd_force_now (stream wait + reduction + 24-byte read-back)"}
+
+
 def wall_seed_leg(sol, t, epochs=150, n_harvest=2_000_000, n_synth=1_000_000, batch=2048, lr_max=3e-3):
     """Learned u_tau seed: harvested (NACA 0012 tunnels at 0-12 deg, coarse +
     patch wall cells) and synthetic samples, labelled by FP64 Newton, trained
@@ -841,7 +856,9 @@ def reference_cuda_leg(warmup=100, steps=100):
                       # wallModelUpdateKernel alone on the same lists (stats reset + kernel, mean of 20),
                       # beside this library's wall-seed leg figures
                       "wall_update_ms": {"coarse": round(r3["wall_ms"][0], 5), "fine": round(r3["wall_ms"][1], 5),
-                                         "wall_cells": {"coarse": len(wc["cell"]), "fine": len(wf["cell"])}}}
+                                         "wall_cells": {"coarse": len(wc["cell"]), "fine": len(wf["cell"])}},
+                      # forceReductionKernel alone on the fine level (accumulator reset + kernel, mean of 20)
+                      "force_reduction_ms": round(r3["force_ms"], 5)}
     return out
 
 
@@ -1242,6 +1259,8 @@ def main():
             "gpu_launches": int(r32["launches"]), "clocks": r32["clocks"],
             "force_lattice": r32["force"], "nan": bool(r32["nan"])}
     line["e2e"] = e2e(t, r32, args.steps)
+    if ws == 1:
+        line["force_reduction"] = force_leg(r32["solver"])
     if ws == 1 and not args.no_geometry:
         line["snapshot"] = snapshot_leg(r32["solver"], t)
     if not args.no_wallnet and ws == 1:

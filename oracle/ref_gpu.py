@@ -77,7 +77,8 @@ class RunIn(C.Structure):
 class RunOut(C.Structure):
     """RefRunOut of the harness."""
     _fields_ = [("ms", C.c_double), ("trip_step", C.c_longlong), ("trip_flag", C.c_int), ("checks", C.c_int),
-                ("force", C.c_float * 3), ("steps_run", C.c_longlong), ("wall_ms", C.c_double * 2)]
+                ("force", C.c_float * 3), ("steps_run", C.c_longlong), ("wall_ms", C.c_double * 2),
+                ("force_ms", C.c_double)]
 
 
 _lib = None
@@ -171,7 +172,8 @@ def run_full(dims, flags, tau, u_in, cs=0.1, lam=3.0 / 16.0, f0=None, wall=None,
     (step and verdict), the last force and, with `states`, the final
     populations and u_tau of each level; with `wall_reps` > 0, after the
     timed steps, the mean ms of that many back-to-back wall-model updates
-    per level on the state they left (wall_ms: coarse, fine)."""
+    per level on the state they left (wall_ms: coarse, fine) and, with
+    `forces`, of as many force reductions (force_ms)."""
     keep = []
     n = int(np.prod(dims))
     outs = {}
@@ -204,7 +206,8 @@ def run_full(dims, flags, tau, u_in, cs=0.1, lam=3.0 / 16.0, f0=None, wall=None,
     if L.refgpu_run_full(C.byref(rin), C.byref(out)) != 0:
         raise RuntimeError(L.refgpu_error().decode())
     res = dict(ms=out.ms, trip_step=int(out.trip_step), trip_flag=int(out.trip_flag), checks=int(out.checks),
-               force=tuple(out.force), steps=int(out.steps_run), wall_ms=tuple(out.wall_ms))
+               force=tuple(out.force), steps=int(out.steps_run), wall_ms=tuple(out.wall_ms),
+               force_ms=float(out.force_ms))
     res.update(outs)
     return res
 

@@ -318,6 +318,7 @@ struct RefRunOut {
     float force[3];       // the last batch's force (FP32, atomics)
     long long stepsRun;
     double wallMs[2];     // mean ms per wall-model update (stats reset + kernel), coarse / fine; 0: not timed
+    double forceMs;       // mean ms per force reduction (accumulator reset + kernel) on the force level
 };
 
 namespace {
@@ -645,6 +646,19 @@ extern "C" int refgpu_run_full(const RefRunIn* in, RefRunOut* out) {
             cudaEventElapsedTime(&tw, e0, e1);
             if (e != cudaSuccess) break;
             out->wallMs[k] = static_cast<double>(tw) / in->wallReps;
+        }
+        // The force reduction alone on the level forces come from.
+        if (good && e == cudaSuccess && in->forces) {
+            PaddedLevel& FL = refined ? F : C;
+            const float* ff = refined ? F.f[fs] : C.f[cs_];
+            good = launch_force(FL, ff, dForce);   // warm
+            cudaEventRecord(e0, nullptr);
+            for (int r = 0; r < in->wallReps && good; ++r) good = launch_force(FL, ff, dForce);
+            cudaEventRecord(e1, nullptr);
+            e = cudaEventSynchronize(e1);
+            float tf = 0.0f;
+            cudaEventElapsedTime(&tf, e0, e1);
+            if (e == cudaSuccess) out->forceMs = static_cast<double>(tf) / in->wallReps;
         }
     }
     cudaEventDestroy(e0);
