@@ -146,8 +146,9 @@ struct StoreF32 {
     using T = float;
     static constexpr int kBytes = 4;
     /// Resident 128-thread blocks per SM the one-cell collide is compiled
-    /// for: 51 registers (the fine-level launch measured 1.7 % faster than
-    /// with the compiler's own 56).
+    /// for: a cap of 51 registers, of which ptxas allocates 48 (the
+    /// fine-level launch measured 1.7 % faster than with the compiler's own
+    /// 56).
     static constexpr int kCellMinBlocks = 10;
     /// Resident threads per SM the batched collide is compiled for: 64
     /// registers (the FP16 batched polar measured 15 % slower at 1536
@@ -184,7 +185,8 @@ struct StoreF32 {
 struct StoreF16 {
     using T = __half;
     static constexpr int kBytes = 2;
-    /// 42 registers: the fine-level launch measured 7 % faster than at 56.
+    /// A cap of 42 registers, of which ptxas allocates 40: the fine-level
+    /// launch measured 7 % faster than at 56.
     static constexpr int kCellMinBlocks = 12;
     static constexpr int kBatchThreads = 1024;
     static constexpr int kChildMinBlocks = 8;
