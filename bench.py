@@ -1187,6 +1187,8 @@ def main():
         cfg = workload_config(t, ws)
         cfg["geometry"] = geometry
         steps = max(1, min(args.steps, 3))
+        cfg["window"] = (f"the first {steps + 1} steps from the uniform-flow start (one warm-up step, then "
+                         f"{steps} timed), inside the stable window before the speed watchdog's first trip")
         ref = cpu_reference(t, steps)
         line = {"impl": "reference", "metric": METRIC, "value": ref["value"], "unit": UNIT, "n_gpus": args.gpus,
                 "steps": steps, "warmup": 1, "ms_per_step": round(ref["seconds"] * 1e3 / steps, 1),
