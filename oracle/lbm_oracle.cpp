@@ -103,6 +103,8 @@ float h2f(uint16_t h) {
     return f;
 }
 
+/// Second-order D3Q19 equilibrium (lbm_core.cu:63-73 equilibrium19; the same
+/// body in lbm_refine.cu:44-52).
 template <class T>
 void equilibrium19(T rho, T ux, T uy, T uz, T feq[Q]) {
     const T usq = T(1.5) * (ux * ux + uy * uy + uz * uz);
@@ -112,6 +114,9 @@ void equilibrium19(T rho, T ux, T uy, T uz, T feq[Q]) {
     }
 }
 
+/// One pull stream-collide over the lattice (lbm_core.cu:213-475
+/// streamCollideKernel<WM, QL>: boundary select by neighbour flag, moments,
+/// limiter, Smagorinsky tau, TRT, Ladd term, q-LIBB links).
 template <class T>
 void collide(const Dims& d, const T* src, T* dst, const uint8_t* flags, T tau0, T lambda, T smagPre,
              T uIn, int writeMacro, T* mr, T* mu, T* mv, T* mw, const uint16_t* uwxA,
@@ -236,6 +241,8 @@ void collide(const Dims& d, const T* src, T* dst, const uint8_t* flags, T tau0, 
     }
 }
 
+/// Momentum-exchange force over fluid cells with solid links
+/// (lbm_core.cu:573-637 forceReductionKernel<WM>), summed in FP64.
 template <class T>
 void force(const Dims& d, const T* f, const uint8_t* flags, const uint16_t* uwxA, const uint16_t* uwyA,
            const uint16_t* uwzA, double out[3]) {
@@ -266,15 +273,19 @@ void force(const Dims& d, const T* f, const uint8_t* flags, const uint16_t* uwxA
 
 // ---- wall model (FP32, reference lbm_wallmodel.cu:31-196) ----------------
 constexpr float kKappa = 0.41f, kC = 7.8f;
+/// Reichardt's law u+(y+) (lbm_wallmodel.cu:30-36 reichardtUPlus).
 float reichardt(float yp) {
     return std::log(1.0f + kKappa * yp) / kKappa
          + kC * (1.0f - std::exp(-yp / 11.0f) - (yp / 11.0f) * std::exp(-yp / 3.0f));
 }
+/// du+/dy+ of Reichardt's law (lbm_wallmodel.cu:38-45 reichardtDuPlus).
 float reichardt_d(float yp) {
     return 1.0f / (1.0f + kKappa * yp)
          + kC * ((1.0f / 11.0f) * std::exp(-yp / 11.0f) - (1.0f / 11.0f) * std::exp(-yp / 3.0f)
                  + (yp / 33.0f) * std::exp(-yp / 3.0f));
 }
+/// Six FP32 Newton iterations on u_tau u+(y u_tau / nu) = u_t from the warm
+/// or fresh seed (lbm_wallmodel.cu:55-73 solveUTau).
 float solve_utau(float ut, float ys, float nu, float seed) {
     float utau = seed > 0.0f ? seed : std::fmax(0.04f * ut, std::sqrt(nu * ut / ys));
     for (int it = 0; it < 6; ++it) {
@@ -498,6 +509,8 @@ float oracle_h2f(uint16_t h) { return h2f(h); }
 
 // ---- refinement (reference lbm_refine.cu:70-429), FP32 -------------------
 
+/// Projection of f_neq onto its second-order Hermite moments
+/// (lbm_refine.cu:70-97 regularizeFneq).
 static void regularize(float fneq[Q]) {
     float pxx = 0, pyy = 0, pzz = 0, pxy = 0, pxz = 0, pyz = 0;
     for (int q = 0; q < Q; ++q) {
@@ -583,6 +596,8 @@ void oracle_fill_c2f(int cnx, int cny, int cnz, const float* cT0, const float* c
     }
 }
 
+/// Mean of the m^3 non-solid children of one coarse cell, its moments and
+/// f_neq (lbm_refine.cu:274-318 childAvgFneq).
 static bool child_avg(const float* ff, const uint8_t* fflags, const Dims& fd, int fx, int fy, int fz, int m,
                       float fneqOut[Q], float& rO, float& uxO, float& uyO, float& uzO) {
     const long long FN = fd.n();
@@ -754,7 +769,9 @@ void oracle_tunnel_wall(void* p, int level, int count, const long long* cell, co
     (level == 0 ? t->wmc : t->wmf) = true;
 }
 
-/// n coarse steps with the reference cadence; returns 0.
+/// n coarse steps with the reference cadence (lbm_solver.cpp:1132-1390
+/// stepN: coarse collide, m fine sub-steps of fill + collide, restriction,
+/// per-batch force and wall-model update); returns 0.
 int oracle_tunnel_step(void* p, int n) {
     auto* t = static_cast<Tunnel*>(p);
     const long long cn = t->cd.n();
