@@ -12,8 +12,10 @@
 //    pointers for its own launch wrappers; this library's buffers are not
 //    padded. External kernels use fcfd_lattice_view instead.
 //  * the VG/boundary-layer readouts (extractSuctionDelta99, separation onset,
-//    crossflow planes), q-LIBB switches, the finer level and seedFromCoarse:
-//    their C counterparts exist only partly or outside the solver step.
+//    crossflow planes) and seedFromCoarse: they lie outside the solver step
+//    and have no C counterpart.
+// The nested finer level and the q-LIBB link fields map onto
+// fcfd_init_finer_refinement & co. and fcfd_set_q_links / fcfd_q_link_info.
 //
 // Layout note for snapshot callers: activeDeviceF() points at the unpadded
 // SoA f[q * cellCount + cell] and fBufferBytes() reports 19 * cellCount *
@@ -76,7 +78,35 @@ struct LBMSolver::Impl {
     std::vector<std::uint8_t> flags;
     bool initialized = false;
     bool wallModel = false;
+    bool qlibb = false;   // the app's q-LIBB switch; survives re-init as in the reference
     ~Impl() { fcfd_destroy(s); }
+
+    /// Cells of a level (0 coarse, 1 fine, 2 finer); 0 when it is not active.
+    long long levelCells(int level) const {
+        if (level == 0) return initialized ? dims.cellCount() : 0;
+        if (level == 1) {
+            fcfd_refine_info r{};
+            if (fcfd_refinement_info(s, &r) != 0 || !r.active) return 0;
+            return static_cast<long long>(r.fine_dims.nx) * r.fine_dims.ny * r.fine_dims.nz;
+        }
+        fcfd_finer_info f{};
+        if (fcfd_finer_refinement_info(s, &f) != 0 || !f.active) return 0;
+        return static_cast<long long>(f.dims.nx) * f.dims.ny * f.dims.nz;
+    }
+
+    /// uploadQLevel (lbm_solver.cpp:378-404): the level's previous field goes
+    /// first; a switched-off q-LIBB, an empty link count or a field of the
+    /// wrong size leaves the level on plain half-way bounce-back.
+    void uploadQ(int level, const std::vector<std::uint8_t>& qFrac, const std::vector<std::uint32_t>& ffMask,
+                 int links, int fallback) {
+        const long long n = levelCells(level);
+        if (n == 0) return;
+        fcfd_set_q_links(s, level, nullptr, 0, nullptr, 0, 0, 0);
+        if (!qlibb || links == 0 || qFrac.size() != static_cast<std::size_t>(n) * 19 ||
+            ffMask.size() != static_cast<std::size_t>(n))
+            return;
+        fcfd_set_q_links(s, level, qFrac.data(), qFrac.size(), ffMask.data(), ffMask.size(), links, fallback);
+    }
 };
 
 LBMSolver::LBMSolver() : impl_(std::make_unique<Impl>()) {}
@@ -149,6 +179,81 @@ RefinementInfo LBMSolver::refinementInfo() const {
     r.fineScaling = from_c(fcfd_refined_scaling(&parent, c.factor));
     r.vramBytes = c.vram_bytes;
     r.forcesFromFine = c.forces_from_fine != 0;
+    fcfd_finer_info f{};
+    if (fcfd_finer_refinement_info(impl_->s, &f) == 0 && f.active) {
+        r.finerActive = true;
+        r.finerFactor = f.factor;
+        r.finerBox.x0 = f.box.x0; r.finerBox.y0 = f.box.y0; r.finerBox.x1 = f.box.x1; r.finerBox.y1 = f.box.y1;
+        r.finerDims.nx = f.dims.nx; r.finerDims.ny = f.dims.ny; r.finerDims.nz = f.dims.nz;
+        const fcfd_scaling fine = to_c(r.fineScaling);
+        r.finerScaling = from_c(fcfd_refined_scaling(&fine, f.factor));
+        r.finerVramBytes = f.vram_bytes;
+    }
+    return r;
+}
+
+bool LBMSolver::initFinerRefinement(const PatchBox& b, int m2, const std::vector<std::uint8_t>& finerFlags,
+                                    std::string* error) {
+    const fcfd_patch_box box{b.x0, b.y0, b.x1, b.y1};
+    char err[512] = {};
+    const int rc = fcfd_init_finer_refinement(impl_->s, &box, m2, finerFlags.data(), finerFlags.size(), err,
+                                              sizeof err);
+    if (rc != 0 && error) *error = err;
+    return rc == 0;
+}
+
+void LBMSolver::shutdownFinerRefinement() { fcfd_shutdown_finer_refinement(impl_->s); }
+
+void LBMSolver::setRefinedFinerFlags(const std::vector<std::uint8_t>& finerFlags) {
+    fcfd_set_refined_finer_flags(impl_->s, finerFlags.data(), finerFlags.size());
+}
+
+void LBMSolver::setRefinedFinerSurfaceReference(const std::vector<std::uint8_t>& finerCleanFlags) {
+    fcfd_set_refined_finer_surface_reference(impl_->s, finerCleanFlags.data(), finerCleanFlags.size());
+}
+
+void LBMSolver::setQLIBBEnabled(bool enabled) {
+    Impl& m = *impl_;
+    if (m.qlibb == enabled) return;
+    m.qlibb = enabled;
+    if (enabled) return;   // the next uploads build the fields
+    for (int level = 0; level < 3; ++level)
+        if (m.levelCells(level) > 0) fcfd_set_q_links(m.s, level, nullptr, 0, nullptr, 0, 0, 0);
+}
+
+bool LBMSolver::qlibbEnabled() const { return impl_->qlibb; }
+
+void LBMSolver::setCoarseQLinks(const std::vector<std::uint8_t>& qFrac, const std::vector<std::uint32_t>& ffMask,
+                                int links, int fallback) {
+    impl_->uploadQ(0, qFrac, ffMask, links, fallback);
+}
+
+void LBMSolver::setFineQLinks(const std::vector<std::uint8_t>& qFrac, const std::vector<std::uint32_t>& ffMask,
+                              int links, int fallback) {
+    impl_->uploadQ(1, qFrac, ffMask, links, fallback);
+}
+
+void LBMSolver::setFinerQLinks(const std::vector<std::uint8_t>& qFrac, const std::vector<std::uint32_t>& ffMask,
+                               int links, int fallback) {
+    impl_->uploadQ(2, qFrac, ffMask, links, fallback);
+}
+
+long long LBMSolver::fineCellCount() const { return impl_->levelCells(1); }
+
+long long LBMSolver::finerCellCount() const { return impl_->levelCells(2); }
+
+QLIBBReadout LBMSolver::qlibbReadout() const {
+    QLIBBReadout r;
+    r.enabled = impl_->qlibb;
+    if (!r.enabled) return r;
+    for (int level = 0; level < 3; ++level) {
+        int active = 0, links = 0, fallback = 0;
+        if (impl_->levelCells(level) == 0 || fcfd_q_link_info(impl_->s, level, &active, &links, &fallback) != 0 ||
+            !active)
+            continue;
+        r.links += links;
+        r.fallback += fallback;
+    }
     return r;
 }
 

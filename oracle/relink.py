@@ -5,14 +5,17 @@ FoilCFD's GPU tests (tests/m0_taylor_green.cpp, tests/m3_refine.cpp of the
 reference) drive foilcfd::LBMSolver exactly as the app does. Relinking them
 with foil_cfd_gb300/shim/lbm_solver_shim.cpp and libfoilcfd_gb300.so in place
 of the reference's lbm_*.cu / lbm_solver.cpp shows the drop-in on the
-reference's own callers.
+reference's own callers. Two more of its solver tests (tests/m1_cavity.cpp,
+tests/m4_finer.cpp: the lid-driven cavity and the nested finer level) are
+staged and relinked too (LINK_ONLY), which shows that every LBMSolver member
+they call has a definition; they have not been run on a GPU.
 
 `stage()` runs in the build container, where the reference tree is mounted:
-it copies the handful of files those two tests compile from (their test
+it copies the handful of files those tests compile from (their test
 headers and the src/sim headers they include) into oracle/_ref/relink/, a
 git-ignored build directory that travels with the working tree to the GPU
 machine (the reference tree itself is not there). `build()` compiles and
-links the two programs with g++ wherever it runs; `run()` executes one.
+links one program with g++ wherever it runs; `run()` executes one.
 Nothing here is part of the product.
 """
 from __future__ import annotations
@@ -27,14 +30,18 @@ ROOT = HERE.parent
 KIT = HERE / "_ref" / "relink"
 OUT = HERE / "_build"
 SHIM = ROOT / "foil_cfd_gb300" / "shim" / "lbm_solver_shim.cpp"
-TESTS = ("m0_taylor_green", "m3_refine")
-# What the two tests compile from (reference-relative paths).
-FILES = ["src/sim/lbm_solver.h", "src/sim/lbm_core.cuh", "src/sim/lbm_refine.cuh", "src/sim/units.h",
-         "tests/lbm_test_util.h", "tests/test_util.h"] + [f"tests/{t}.cpp" for t in TESTS]
+TESTS = ("m0_taylor_green", "m3_refine")     # relinked and run on the GPU
+LINK_ONLY = ("m1_cavity", "m4_finer")        # relinked in the build container only
+# What the tests compile from (reference-relative paths).
+COMMON = ["src/sim/lbm_solver.h", "src/sim/lbm_core.cuh", "src/sim/lbm_refine.cuh", "src/sim/units.h",
+          "tests/lbm_test_util.h", "tests/test_util.h"]
+FILES = COMMON + [f"tests/{t}.cpp" for t in TESTS + LINK_ONLY]
 
 
-def staged() -> bool:
-    return all((KIT / f).exists() for f in FILES)
+def staged(test: str | None = None) -> bool:
+    """The shared headers and one test's source (default: the GPU-run tests')."""
+    tests = (test,) if test else TESTS
+    return all((KIT / f).exists() for f in COMMON + [f"tests/{t}.cpp" for t in tests])
 
 
 def stage(reference: Path) -> Path:
@@ -60,7 +67,7 @@ def _cuda() -> Path:
 
 def build(test: str) -> Path:
     """Compile and link one relinked reference test; returns the program."""
-    if not staged():
+    if not staged(test):
         raise RuntimeError("reference test sources not staged (oracle/relink.py stage, build container)")
     from foil_cfd_gb300 import build_lib
     lib = build_lib.build()
