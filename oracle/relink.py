@@ -5,10 +5,9 @@ FoilCFD's GPU tests (tests/m0_taylor_green.cpp, tests/m3_refine.cpp of the
 reference) drive foilcfd::LBMSolver exactly as the app does. Relinking them
 with foil_cfd_gb300/shim/lbm_solver_shim.cpp and libfoilcfd_gb300.so in place
 of the reference's lbm_*.cu / lbm_solver.cpp shows the drop-in on the
-reference's own callers. Two more of its solver tests (tests/m1_cavity.cpp,
-tests/m4_finer.cpp: the lid-driven cavity and the nested finer level) are
-staged and relinked too (LINK_ONLY), which shows that every LBMSolver member
-they call has a definition; they have not been run on a GPU.
+reference's own callers. Two more of its solver tests run the same way:
+tests/m1_cavity.cpp (the lid-driven cavity against Ghia et al.) and
+tests/m4_finer.cpp (the nested finer level).
 
 `stage()` runs in the build container, where the reference tree is mounted:
 it copies the handful of files those tests compile from (their test
@@ -30,16 +29,15 @@ ROOT = HERE.parent
 KIT = HERE / "_ref" / "relink"
 OUT = HERE / "_build"
 SHIM = ROOT / "foil_cfd_gb300" / "shim" / "lbm_solver_shim.cpp"
-TESTS = ("m0_taylor_green", "m3_refine")     # relinked and run on the GPU
-LINK_ONLY = ("m1_cavity", "m4_finer")        # relinked in the build container only
+TESTS = ("m0_taylor_green", "m3_refine", "m1_cavity", "m4_finer")
 # What the tests compile from (reference-relative paths).
 COMMON = ["src/sim/lbm_solver.h", "src/sim/lbm_core.cuh", "src/sim/lbm_refine.cuh", "src/sim/units.h",
           "tests/lbm_test_util.h", "tests/test_util.h"]
-FILES = COMMON + [f"tests/{t}.cpp" for t in TESTS + LINK_ONLY]
+FILES = COMMON + [f"tests/{t}.cpp" for t in TESTS]
 
 
 def staged(test: str | None = None) -> bool:
-    """The shared headers and one test's source (default: the GPU-run tests')."""
+    """The shared headers and one test's source (default: every test's)."""
     tests = (test,) if test else TESTS
     return all((KIT / f).exists() for f in COMMON + [f"tests/{t}.cpp" for t in tests])
 

@@ -2,8 +2,8 @@
 tests/m3_refine.cpp, tests/m1_cavity.cpp and tests/m4_finer.cpp) compile
 against the reference's src/sim/lbm_solver.h and link against this library
 through foil_cfd_gb300/shim/lbm_solver_shim.cpp: every LBMSolver member they
-call has a definition over the C ABI. Running them needs a GPU; the first two
-run in tests/test_gpu_relinked_reference.py."""
+call has a definition over the C ABI. Running them needs a GPU
+(tests/test_gpu_relinked_reference.py)."""
 import pytest
 
 
