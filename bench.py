@@ -1186,7 +1186,7 @@ def main():
             geometry = "this library's host builders (byte-identical to the reference's)"
         cfg = workload_config(t, ws)
         cfg["geometry"] = geometry
-        steps = max(1, min(args.steps, 3))
+        steps = max(1, min(args.steps, 5))   # ~10-15 s of host work on the config-3 tunnel
         cfg["window"] = (f"the first {steps + 1} steps from the uniform-flow start (one warm-up step, then "
                          f"{steps} timed), inside the stable window before the speed watchdog's first trip")
         ref = cpu_reference(t, steps)
@@ -1293,7 +1293,7 @@ def main():
         r16["vsnap"].close()
         r16["solver"] = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = {k: v for k, v in cpu_reference(reference_workload(args.small) or t, 2).items()
+        line["cpu_baseline"] = {k: v for k, v in cpu_reference(reference_workload(args.small) or t, 5).items()
                                 if k != "seconds"}
     if dist is not None:
         dist.barrier()
