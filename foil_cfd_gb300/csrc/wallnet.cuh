@@ -6,7 +6,7 @@
 // the Newton solvers built from them.
 //
 // Reichardt's all-y+ law and its Newton solve follow the reference's wall
-// model (src/sim/lbm_wallmodel.cu:31-95): u+ = ln(1 + kappa y+)/kappa
+// model (src/sim/lbm_wallmodel.cu:30-73): u+ = ln(1 + kappa y+)/kappa
 // + C (1 - e^{-y+/11} - (y+/11) e^{-y+/3}), g(u_tau) = u_tau u+(y u_tau/nu)
 // - u_par, kappa = 0.41, C = 7.8.
 #pragma once

@@ -3,7 +3,7 @@
  * iMEM wall model.
  *
  * The reference solves Reichardt's law for u_tau at every wall cell with six
- * FP32 Newton iterations from a warm seed (src/sim/lbm_wallmodel.cu:60-95).
+ * FP32 Newton iterations from a warm seed (src/sim/lbm_wallmodel.cu:47-73, solveUTau).
  * This extension supplies the initial guess from a small network instead:
  *
  *     x = ((log u_par, log y, log nu) - in_mean) / in_std
