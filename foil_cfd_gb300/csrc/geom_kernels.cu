@@ -1,18 +1,18 @@
 // On-device geometry builders: the flag fields, patch box and cell lists the
 // solver keys off, built where they are used instead of on the host.
 //
-// * Airfoil rasterisation (src/geom/voxelizer.cpp:60-160, voxelizeAirfoil):
+// * Airfoil rasterisation (src/geom/voxelizer.cpp:62-153, voxelizeAirfoil):
 //   the outline rotated about the quarter chord and scaled to the anchor,
 //   one warp per lattice row intersecting the row's cell-centre line with
 //   every edge under the half-open rule, the crossings sorted, and the
 //   cells between crossing pairs marked in a 2-D mask.
 // * Flag field (buildBoundaryFlags, closeTrailingEdgeGaps, stampInterfaceShell,
-//   voxelizer.cpp:28-57, 162-196, 225-247): one thread per cell evaluates the
+//   voxelizer.cpp:28-60, 155-183, 223-245): one thread per cell evaluates the
 //   base flag (domain faces, all fluid or an input field), the extruded mask
 //   over fluid, the single-cell trailing-edge closure judged on the
 //   pre-closure field (the +-y neighbours' pre-closure flags are recomputed,
 //   so the pass is out of place without a copy) and the interface shell.
-// * Patch box (derivePatchBox, voxelizer.cpp:280-318): a min/max reduction
+// * Patch box (derivePatchBox, voxelizer.cpp:265-301): a min/max reduction
 //   of the solid cells' x and y.
 // * Cell lists in ascending cell order (ordered stream compaction: per-tile
 //   counts, one scan over the tiles, a scatter that re-evaluates the tile):

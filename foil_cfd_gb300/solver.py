@@ -543,7 +543,7 @@ def layout_anchor(dims, frac=(0.3, 0.5)):
 
 
 def fine_anchor(anchor, box, factor):
-    """makeFineLayout (voxelizer.cpp:203-223): the coarse anchor moved to the
+    """makeFineLayout (voxelizer.cpp:203-221): the coarse anchor moved to the
     patch origin and scaled by the factor, in FP32 arithmetic."""
     f = np.float32(factor)
     return (float(f * (np.float32(anchor[0]) - np.float32(box.x0))),

@@ -8,7 +8,7 @@
 * ``airfoil_tunnel``: 640x192x192, NACA 0012 at 6 deg, 256 cells/chord, one
   2:1 patch around the section +- 0.1 chord (the reference's fine-patch
   flags: fluid base, voxelised foil, trailing-edge closure, interface shell,
-  src/geom/voxelizer.cpp:200-250).
+  src/geom/voxelizer.cpp:223-263).
 Geometry follows the reference's DomainLayout defaults: quarter chord at
 0.3 nx, 0.5 ny (src/geom/voxelizer.h:57-90).
 """

@@ -63,7 +63,7 @@ enum {
 int fcfd_device_build_flags(const fcfd_dims* dims, int base, const uint8_t* d_in, const fcfd_foil* foil,
                             int close_gaps, int shell_cells, uint8_t* d_out, void* stream, int* closed);
 
-/* derivePatchBox (voxelizer.cpp:280-318) of a device flag field; an all-zero
+/* derivePatchBox (voxelizer.cpp:265-301) of a device flag field; an all-zero
  * box when the field has no solid cell. */
 int fcfd_device_derive_patch_box(const fcfd_dims* dims, const uint8_t* d_flags, int mx0, int mx1, int my0, int my1,
                                  int clearance, void* stream, fcfd_patch_box* box);

@@ -417,14 +417,14 @@ int fcfd_boundary_flags(const fcfd_dims* dims, uint8_t* flags, size_t n);
  * Returns the point count, or -1 on a bad digit string / small buffer. */
 int fcfd_naca4(const char* digits, int points_per_surface, float* xy,
                int cap_points);
-/* voxelizeAirfoil (voxelizer.h:99-116, voxelizer.cpp:60-160) with the
+/* voxelizeAirfoil (voxelizer.h:99-116, voxelizer.cpp:62-153) with the
  * DomainLayout anchor given in lattice cells: Fluid cells whose centres lie
  * inside the rotated, scaled outline become Solid (x in 1..nx-2, y in
  * 1..ny-2, every z). An outline of fewer than 20 points stamps nothing. */
 int fcfd_voxelize_airfoil(const fcfd_dims* dims, const float* xy, int npts,
                           float aoa_deg, int chord_cells, float anchor_x,
                           float anchor_y, uint8_t* flags, size_t n);
-/* closeTrailingEdgeGaps (voxelizer.h:118-125, voxelizer.cpp:162-187):
+/* closeTrailingEdgeGaps (voxelizer.h:118-125, voxelizer.cpp:155-183):
  * returns the number of single-cell gaps closed. */
 int fcfd_close_trailing_edge_gaps(const fcfd_dims* dims, uint8_t* flags,
                                   size_t n);
